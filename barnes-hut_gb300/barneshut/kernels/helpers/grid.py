@@ -1,0 +1,52 @@
+"""Host-side grid helpers with the semantics of
+python-bh/barneshut/kernels/helpers/grid.py:5-48 (used for grid sizing and by
+callers of the reference helpers; the device computes the per-step box)."""
+import math
+
+import numpy as np
+
+
+def next_perfect_square(n):
+    """Smallest perfect square >= n (n itself when n is one)."""
+    r = math.sqrt(n)
+    if r == 0 or math.fmod(n, r) != 0:
+        c = math.ceil(r)
+        return float(c * c)
+    return n
+
+
+def get_bounding_box(points):
+    """Square bounding box ((min_x, min_y), (max_x, max_y)): the shorter
+    side's maximum is extended so both edges have the same length."""
+    pts = np.asarray(points)
+    mn = pts.min(axis=0)[:2]
+    mx = pts.max(axis=0)[:2]
+    min_x, min_y = float(mn[0]), float(mn[1])
+    max_x, max_y = float(mx[0]), float(mx[1])
+    xe, ye = max_x - min_x, max_y - min_y
+    if xe > ye:
+        max_y += xe - ye
+    elif ye > xe:
+        max_x += ye - xe
+    assert (max_x - min_x) - (max_y - min_y) < 0.00001
+    return (min_x, min_y), (max_x, max_y)
+
+
+def get_neighbor_cells(point, grid_dim):
+    """Chebyshev-1 neighbours of box (x, y) inside the grid, x-major order."""
+    x, y = point
+    cells = []
+    for i in range(max(0, x - 1), min(grid_dim - 1, x + 1) + 1):
+        for j in range(max(0, y - 1), min(grid_dim - 1, y + 1) + 1):
+            if (i, j) != (x, y):
+                cells.append((i, j))
+    return cells
+
+
+def remove_bottom_left_neighbors(point, neighbors):
+    """Drop the four neighbours that precede (x, y) in x-major order's mutual
+    update: (x-1, y-1), (x-1, y), (x, y-1), (x+1, y-1)."""
+    x, y = point
+    drop = {(x - 1, y - 1), (x - 1, y), (x, y - 1), (x + 1, y - 1)}
+    neighbors[:] = [c for c in neighbors if c not in drop]
+    return neighbors

@@ -1,0 +1,30 @@
+#!/usr/bin/env python3
+"""Input generator with the interface of python-bh/bin/gen_input.py:15-33:
+gen_input.py <distribution> <num_particles> <fout> [--seed S]
+distributions: normal, gauss (as the reference), uniform01, cluster (seeded)."""
+import argparse
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.realpath(__file__))))
+
+from barneshut.gb300 import particle_io, workloads  # noqa: E402
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("distribution")
+    ap.add_argument("num_particles", type=int)
+    ap.add_argument("fout")
+    ap.add_argument("--seed", type=int, default=None)
+    a = ap.parse_args()
+    n = a.num_particles
+    if a.distribution in ("normal", "gauss"):
+        data = workloads.gen_input(n, a.distribution, seed=a.seed)
+    elif a.distribution == "uniform01":
+        data = workloads.uniform(n, seed=0 if a.seed is None else a.seed)
+    elif a.distribution == "cluster":
+        data = workloads.cluster_mixture(n, seed=1 if a.seed is None else a.seed)
+    else:
+        sys.exit(f"unknown distribution {a.distribution}")
+    print(f"Using distribution {a.distribution}")
+    particle_io.write_particles(a.fout, *data)

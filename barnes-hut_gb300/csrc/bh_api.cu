@@ -1,0 +1,522 @@
+// bh_api.cu -- host side of the C ABI declared in include/bh_gb300.h.
+//
+// A plan is a host object: the system table, the workspace layout and the
+// launch sequence of each step phase.  It allocates no device memory; the
+// caller binds one workspace buffer.  Kernels read the plan's device tables
+// and a device-side epoch that selects the current state buffer, so a step
+// captured into a CUDA graph replays correctly.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/bh_gb300.h"
+#include "bh_internal.cuh"
+
+using namespace bh;
+
+struct bh_plan {
+    bh_params params;
+    int nsys = 0;
+    std::vector<SysDesc> sys;
+    std::vector<long long> poff, boff, coff, goff, lvl;
+    int Lmax = 1;
+    long long n_total = 0, B_total = 0, C_total = 0, NG_total = 0;
+    // workspace layout (byte offsets)
+    size_t ws_bytes = 0;
+    size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_lvl;
+    size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
+    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_tiles, o_mom, o_rec,
+        o_rec2;
+    void *ws = nullptr;
+    int device = -1;
+    DevPlan dev;
+    bool has_tree = false;
+    bool acc_stale = true;  // next bh_evaluate overwrites instead of accumulating
+    // graph cache
+    cudaGraphExec_t gexec = nullptr;
+    int gsteps = 0;
+    cudaStream_t gstream = nullptr;
+    char err[512];
+};
+
+static int fail(bh_plan *p, int code, const char *fmt, ...) {
+    if (p) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(p->err, sizeof(p->err), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+static int cuda_fail(bh_plan *p, cudaError_t e, const char *what) {
+    return fail(p, BH_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(p, call, what)                                  \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_fail(p, e_, what); \
+    } while (0)
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+static thread_local char g_create_err[256] = "";
+
+extern "C" int bh_grid_dim(long long n, int ppb) {
+    // base.py:223-231 with helpers/grid.py:5-8 (next_perfect_square)
+    if (n <= 0) return 0;
+    double nleaves = ppb == 1 ? 1.0 : (double)n / (0.7 * (double)ppb);
+    double r = std::sqrt(nleaves);
+    if (r == 0.0 || std::fmod(nleaves, r) != 0.0) {
+        double c = std::ceil(r);
+        nleaves = c * c;
+    }
+    return (int)std::sqrt(nleaves);
+}
+
+static int auto_group(long long n, int G) {
+    double nb = G > 0 ? (double)n / ((double)G * G) : 0.0;
+    if (nb >= 32.0) return 1;
+    if (nb >= 8.0) return 2;
+    if (nb >= 2.0) return 4;
+    return 8;
+}
+
+extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const int *grid_dim,
+                              const bh_params *params) {
+    if (!out) return BH_ERR_INVALID;
+    *out = nullptr;
+    if (nsys < 1 || !n || !params) {
+        snprintf(g_create_err, sizeof(g_create_err), "bh_plan_create: nsys < 1 or null argument");
+        return BH_ERR_INVALID;
+    }
+    bh_plan *p = new (std::nothrow) bh_plan();
+    if (!p) return BH_ERR_INVALID;
+    p->err[0] = 0;
+    p->params = *params;
+    const bh_params &pr = p->params;
+    auto bad = [&](const char *msg) {
+        snprintf(g_create_err, sizeof(g_create_err), "bh_plan_create: %s", msg);
+        delete p;
+        return BH_ERR_INVALID;
+    };
+    if (!(pr.tick_seconds == pr.tick_seconds) || !std::isfinite(pr.grav_constant)) return bad("bad constants");
+    if (!(pr.softening >= 0.0) || !(pr.cutoff_r2 >= 0.0)) return bad("negative softening/cutoff");
+    if (pr.precision < 0 || pr.precision > 2) return bad("precision");
+    if (pr.group_dim < 0 || pr.group_dim > 8 || (pr.group_dim & (pr.group_dim - 1))) return bad("group_dim");
+    const bool flat = !(pr.theta > 0.0);
+    p->nsys = nsys;
+    p->sys.resize(nsys);
+    p->poff.assign(nsys + 1, 0);
+    p->boff.assign(nsys + 1, 0);
+    p->coff.assign(nsys + 1, 0);
+    p->goff.assign(nsys + 1, 0);
+    for (int s = 0; s < nsys; s++) {
+        if (n[s] < 0 || n[s] > (1LL << 30)) return bad("particle count out of range [0, 2^30]");
+        int G = grid_dim && grid_dim[s] > 0 ? grid_dim[s] : bh_grid_dim(n[s], 1000);
+        if (G < 1) G = 1;
+        if (G > 32768) return bad("grid_dim > 32768");
+        SysDesc &d = p->sys[s];
+        memset(&d, 0, sizeof(d));
+        d.n = n[s];
+        d.poff = p->poff[s];
+        d.G = G;
+        int L = 0;
+        long long cells = 0;
+        for (int g = G;;) {
+            d.lvg[L] = g;
+            d.lvoff[L] = cells;
+            cells += (long long)g * g;
+            L++;
+            if (g == 1) break;
+            g = (g + 1) / 2;
+        }
+        d.L = L;
+        int TG = flat ? 1 : (pr.group_dim > 0 ? pr.group_dim : auto_group(n[s], G));
+        if (!flat) {
+            // children of cells rejected at level l+1 (edge s >= 2 boxes): a rejected cell
+            // intersects the group widened by s/theta, so at most (TG/2 + 2/theta + 2)^2 of
+            // them, four children each.  Keep that within the kernel's frontier (1024).
+            double bound = 4.0 * std::pow(TG / 2.0 + 2.0 / pr.theta + 2.0, 2.0);
+            while (bound > 1024.0 && TG > 1) {
+                TG /= 2;
+                bound = 4.0 * std::pow(TG / 2.0 + 2.0 / pr.theta + 2.0, 2.0);
+            }
+            if (bound > 1024.0) return bad("theta too small for the traversal frontier (theta >= 0.15)");
+        }
+        d.TG = TG;
+        d.NGs = (G + TG - 1) / TG;
+        d.boff = p->boff[s];
+        d.coff = p->coff[s];
+        d.goff = p->goff[s];
+        p->poff[s + 1] = p->poff[s] + n[s];
+        p->boff[s + 1] = p->boff[s] + (long long)G * G;
+        p->coff[s + 1] = p->coff[s] + cells;
+        p->goff[s + 1] = p->goff[s] + (long long)d.NGs * d.NGs;
+        if (L > p->Lmax) p->Lmax = L;
+    }
+    p->n_total = p->poff[nsys];
+    p->B_total = p->boff[nsys];
+    p->C_total = p->coff[nsys];
+    p->NG_total = p->goff[nsys];
+    if (p->n_total >= (1LL << 31) || p->C_total >= (1LL << 31) || p->B_total >= (1LL << 31))
+        return bad("total particles, boxes or cells >= 2^31");
+    // level tables: prefix of level-l cell counts over systems
+    p->lvl.assign((size_t)p->Lmax * (nsys + 1), 0);
+    for (int l = 0; l < p->Lmax; l++)
+        for (int s = 0; s < nsys; s++) {
+            long long c = l < p->sys[s].L ? (long long)p->sys[s].lvg[l] * p->sys[s].lvg[l] : 0;
+            p->lvl[(size_t)l * (nsys + 1) + s + 1] = p->lvl[(size_t)l * (nsys + 1) + s] + c;
+        }
+    // workspace layout
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t r = o;
+        o = align_up(o + (bytes ? bytes : 1), 256);
+        return r;
+    };
+    const size_t N = (size_t)p->n_total, B = (size_t)p->B_total, C = (size_t)p->C_total;
+    p->o_sys = take(sizeof(SysDesc) * nsys);
+    p->o_dyn = take(sizeof(SysDyn) * nsys);
+    p->o_glob = take(sizeof(Globals));
+    p->o_poff = take(sizeof(long long) * (nsys + 1));
+    p->o_boff = take(sizeof(long long) * (nsys + 1));
+    p->o_coff = take(sizeof(long long) * (nsys + 1));
+    p->o_goff = take(sizeof(long long) * (nsys + 1));
+    p->o_lvl = take(sizeof(long long) * p->lvl.size());
+    for (int b = 0; b < 2; b++) {
+        p->o_X[b] = take(8 * N);
+        p->o_Y[b] = take(8 * N);
+        p->o_VX[b] = take(8 * N);
+        p->o_VY[b] = take(8 * N);
+        p->o_M[b] = take(8 * N);
+        p->o_PID[b] = take(4 * N);
+    }
+    p->o_AX = take(8 * N);
+    p->o_AY = take(8 * N);
+    p->o_P = take(16 * N);
+    p->o_key = take(4 * N);
+    p->o_slot = take(4 * N);
+    p->o_skey = take(4 * N);
+    p->o_counts = take(4 * B);
+    p->o_bstart = take(4 * (B + 1));
+    p->o_tiles = take(4 * (B / 4096 + 2));
+    p->o_mom = take(48 * C);
+    p->o_rec = take(16 * C);
+    p->o_rec2 = take(16 * C);
+    p->ws_bytes = o;
+    *out = p;
+    return BH_OK;
+}
+
+extern "C" int bh_plan_destroy(bh_plan *p) {
+    if (!p) return BH_ERR_INVALID;
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    if (p->gstream) cudaStreamDestroy(p->gstream);
+    delete p;
+    return BH_OK;
+}
+
+// bh_last_error(NULL) reports the last bh_plan_create failure of this thread.
+extern "C" const char *bh_last_error(const bh_plan *p) { return p ? p->err : g_create_err; }
+
+extern "C" int bh_workspace_size(const bh_plan *p, size_t *bytes) {
+    if (!p || !bytes) return BH_ERR_INVALID;
+    *bytes = p->ws_bytes;
+    return BH_OK;
+}
+
+static void fill_dev(bh_plan *p) {
+    char *w = (char *)p->ws;
+    DevPlan &d = p->dev;
+    memset(&d, 0, sizeof(d));
+    d.nsys = p->nsys;
+    d.Lmax = p->Lmax;
+    d.n_total = p->n_total;
+    d.B_total = p->B_total;
+    d.C_total = p->C_total;
+    d.NG_total = p->NG_total;
+    d.sys = (const SysDesc *)(w + p->o_sys);
+    d.dyn = (SysDyn *)(w + p->o_dyn);
+    d.glob = (Globals *)(w + p->o_glob);
+    d.poff_tab = (const long long *)(w + p->o_poff);
+    d.boff_tab = (const long long *)(w + p->o_boff);
+    d.coff_tab = (const long long *)(w + p->o_coff);
+    d.goff_tab = (const long long *)(w + p->o_goff);
+    d.lvl_tab = (const long long *)(w + p->o_lvl);
+    for (int b = 0; b < 2; b++) {
+        d.X[b] = (double *)(w + p->o_X[b]);
+        d.Y[b] = (double *)(w + p->o_Y[b]);
+        d.VX[b] = (double *)(w + p->o_VX[b]);
+        d.VY[b] = (double *)(w + p->o_VY[b]);
+        d.M[b] = (double *)(w + p->o_M[b]);
+        d.PID[b] = (int *)(w + p->o_PID[b]);
+    }
+    d.AX = (double *)(w + p->o_AX);
+    d.AY = (double *)(w + p->o_AY);
+    d.P = (float4 *)(w + p->o_P);
+    d.key = (int *)(w + p->o_key);
+    d.slot = (int *)(w + p->o_slot);
+    d.skey = (int *)(w + p->o_skey);
+    d.counts = (int *)(w + p->o_counts);
+    d.box_start = (int *)(w + p->o_bstart);
+    d.tile_sums = (int *)(w + p->o_tiles);
+    d.mom = (double *)(w + p->o_mom);
+    d.rec = (float4 *)(w + p->o_rec);
+    d.rec2 = (float4 *)(w + p->o_rec2);
+    const bh_params &pr = p->params;
+    d.gconst = pr.grav_constant;
+    d.dt = pr.tick_seconds;
+    d.eps2 = pr.softening * pr.softening;
+    d.cutoff = pr.cutoff_r2;
+    d.theta2_f = (float)(pr.theta * pr.theta);
+    d.eps2_f = (float)d.eps2;
+    d.cut_f = (float)d.cutoff;
+    d.flat = pr.theta > 0.0 ? 0 : 1;
+    d.prec = pr.precision;
+    d.learned = (pr.flags & BH_FLAG_LEARNED) ? 1 : 0;
+    d.mlp = nullptr;
+}
+
+extern "C" int bh_bind(bh_plan *p, void *workspace, size_t bytes, void *stream) {
+    if (!p) return BH_ERR_INVALID;
+    if (!workspace || bytes < p->ws_bytes)
+        return fail(p, BH_ERR_WORKSPACE, "workspace of %zu bytes < required %zu", bytes, p->ws_bytes);
+    if (((uintptr_t)workspace) & 255) return fail(p, BH_ERR_WORKSPACE, "workspace not 256-byte aligned");
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(p, cudaGetDevice(&p->device), "cudaGetDevice");
+    CK(p, force_init(), "force kernel attributes");
+    p->ws = workspace;
+    fill_dev(p);
+    char *w = (char *)workspace;
+    CK(p, cudaMemcpyAsync(w + p->o_sys, p->sys.data(), sizeof(SysDesc) * p->nsys, cudaMemcpyHostToDevice, st), "upload sys");
+    CK(p, cudaMemcpyAsync(w + p->o_poff, p->poff.data(), 8 * (p->nsys + 1), cudaMemcpyHostToDevice, st), "upload poff");
+    CK(p, cudaMemcpyAsync(w + p->o_boff, p->boff.data(), 8 * (p->nsys + 1), cudaMemcpyHostToDevice, st), "upload boff");
+    CK(p, cudaMemcpyAsync(w + p->o_coff, p->coff.data(), 8 * (p->nsys + 1), cudaMemcpyHostToDevice, st), "upload coff");
+    CK(p, cudaMemcpyAsync(w + p->o_goff, p->goff.data(), 8 * (p->nsys + 1), cudaMemcpyHostToDevice, st), "upload goff");
+    CK(p, cudaMemcpyAsync(w + p->o_lvl, p->lvl.data(), 8 * p->lvl.size(), cudaMemcpyHostToDevice, st), "upload lvl");
+    CK(p, cudaMemsetAsync(w + p->o_dyn, 0, sizeof(SysDyn) * p->nsys, st), "zero dyn");
+    CK(p, cudaMemsetAsync(w + p->o_glob, 0, sizeof(Globals), st), "zero globals");
+    CK(p, cudaStreamSynchronize(st), "bind sync");
+    p->has_tree = false;
+    p->acc_stale = true;
+    if (p->gexec) {
+        cudaGraphExecDestroy(p->gexec);
+        p->gexec = nullptr;
+        p->gsteps = 0;
+    }
+    return BH_OK;
+}
+
+static int need_bound(bh_plan *p) {
+    if (!p) return BH_ERR_INVALID;
+    if (!p->ws) return fail(p, BH_ERR_WORKSPACE, "no workspace bound (call bh_bind)");
+    return BH_OK;
+}
+
+extern "C" int bh_load(bh_plan *p, const double *x, const double *y, const double *m,
+                       const double *vx, const double *vy, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (p->n_total && (!x || !y || !m || !vx || !vy)) return fail(p, BH_ERR_INVALID, "null input array");
+    CK(p, launch_load(p->dev, x, y, m, vx, vy, 0, (cudaStream_t)stream), "load");
+    p->has_tree = false;
+    p->acc_stale = true;
+    return BH_OK;
+}
+
+extern "C" int bh_load_records(bh_plan *p, const double *rec, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (p->n_total && !rec) return fail(p, BH_ERR_INVALID, "null records");
+    CK(p, launch_load(p->dev, rec + 0, rec + 1, rec + 2, rec + 3, rec + 4, 10, (cudaStream_t)stream), "load records");
+    p->has_tree = false;
+    p->acc_stale = true;
+    return BH_OK;
+}
+
+extern "C" int bh_store_records(bh_plan *p, double *rec, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (p->n_total && !rec) return fail(p, BH_ERR_INVALID, "null records");
+    CK(p, launch_store(p->dev, p->has_tree ? 1 : 0, rec, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                       (cudaStream_t)stream), "store records");
+    return BH_OK;
+}
+
+extern "C" int bh_store(bh_plan *p, double *x, double *y, double *vx, double *vy, double *ax,
+                        double *ay, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    CK(p, launch_store(p->dev, p->has_tree ? 1 : 0, nullptr, x, y, vx, vy, ax, ay, (cudaStream_t)stream), "store");
+    return BH_OK;
+}
+
+static int enqueue_tree(bh_plan *p, cudaStream_t st) {
+    CK(p, launch_prologue(p->dev, st), "prologue");
+    CK(p, launch_bbox(p->dev, st), "bbox");
+    CK(p, launch_place(p->dev, st), "place");
+    CK(p, launch_scan(p->dev, st), "scan");
+    CK(p, launch_scatter(p->dev, st), "scatter");
+    return BH_OK;
+}
+
+extern "C" int bh_create_tree(bh_plan *p, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    r = enqueue_tree(p, (cudaStream_t)stream);
+    if (r) return r;
+    p->has_tree = true;
+    p->acc_stale = true;
+    return BH_OK;
+}
+
+extern "C" int bh_summarize(bh_plan *p, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (!p->has_tree) return fail(p, BH_ERR_INVALID, "summarize before create_tree");
+    CK(p, launch_summarize(p->dev, (cudaStream_t)stream), "summarize");
+    return BH_OK;
+}
+
+extern "C" int bh_evaluate(bh_plan *p, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (!p->has_tree) return fail(p, BH_ERR_INVALID, "evaluate before create_tree");
+    CK(p, launch_force(p->dev, false, !p->acc_stale, (cudaStream_t)stream), "evaluate");
+    p->acc_stale = false;
+    return BH_OK;
+}
+
+extern "C" int bh_timestep(bh_plan *p, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    CK(p, launch_tick(p->dev, (cudaStream_t)stream), "timestep");
+    p->acc_stale = true;
+    return BH_OK;
+}
+
+static int enqueue_steps(bh_plan *p, int nsteps, cudaStream_t st) {
+    for (int k = 0; k < nsteps; k++) {
+        int r = enqueue_tree(p, st);
+        if (r) return r;
+        CK(p, launch_summarize(p->dev, st), "summarize");
+        CK(p, launch_force(p->dev, true, false, st), "force+tick");
+    }
+    return BH_OK;
+}
+
+extern "C" int bh_step(bh_plan *p, int nsteps, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (nsteps < 0) return fail(p, BH_ERR_INVALID, "nsteps < 0");
+    r = enqueue_steps(p, nsteps, (cudaStream_t)stream);
+    if (r) return r;
+    if (nsteps > 0) {
+        p->has_tree = true;
+        p->acc_stale = true;
+    }
+    return BH_OK;
+}
+
+extern "C" int bh_step_graph(bh_plan *p, int nsteps, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (nsteps < 0) return fail(p, BH_ERR_INVALID, "nsteps < 0");
+    if (nsteps == 0) return BH_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!p->gexec || p->gsteps != nsteps) {
+        if (p->gexec) {
+            cudaGraphExecDestroy(p->gexec);
+            p->gexec = nullptr;
+        }
+        if (!p->gstream) CK(p, cudaStreamCreateWithFlags(&p->gstream, cudaStreamNonBlocking), "graph stream");
+        cudaGraph_t g;
+        CK(p, cudaStreamBeginCapture(p->gstream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        int er = enqueue_steps(p, nsteps, p->gstream);
+        cudaError_t e = cudaStreamEndCapture(p->gstream, &g);
+        if (er) return er;
+        if (e != cudaSuccess) return cuda_fail(p, e, "end capture");
+        e = cudaGraphInstantiate(&p->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(p, e, "graph instantiate");
+        p->gsteps = nsteps;
+    }
+    CK(p, cudaGraphLaunch(p->gexec, st), "graph launch");
+    p->has_tree = true;
+    p->acc_stale = true;
+    return BH_OK;
+}
+
+extern "C" int bh_error_flags(bh_plan *p, unsigned *flags, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (!flags) return fail(p, BH_ERR_INVALID, "null flags");
+    cudaStream_t st = (cudaStream_t)stream;
+    Globals g;
+    CK(p, cudaMemcpyAsync(&g, (char *)p->ws + p->o_glob, sizeof(g), cudaMemcpyDeviceToHost, st), "read flags");
+    CK(p, cudaStreamSynchronize(st), "sync");
+    CK(p, cudaMemsetAsync((char *)p->ws + p->o_glob + offsetof(Globals, err), 0, sizeof(unsigned), st), "clear flags");
+    *flags = g.err;
+    return g.err ? fail(p, BH_ERR_DEVICE, "device error flags 0x%x", g.err) : BH_OK;
+}
+
+extern "C" int bh_pair_counts(bh_plan *p, long long *near_pairs, long long *far_pairs, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    Globals g;
+    CK(p, cudaMemcpyAsync(&g, (char *)p->ws + p->o_glob, sizeof(g), cudaMemcpyDeviceToHost, st), "read counts");
+    CK(p, cudaStreamSynchronize(st), "sync");
+    if (near_pairs) *near_pairs = (long long)g.near_pairs;
+    if (far_pairs) *far_pairs = (long long)g.far_pairs;
+    return BH_OK;
+}
+
+extern "C" int bh_direct_sample(bh_plan *p, int sys, const long long *targets, long long nt,
+                                double *ax, double *ay, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (sys < 0 || sys >= p->nsys) return fail(p, BH_ERR_INVALID, "system %d out of range", sys);
+    if (nt < 0 || (nt > 0 && (!targets || !ax || !ay))) return fail(p, BH_ERR_INVALID, "bad targets");
+    CK(p, launch_direct(p->dev, sys, targets, nt, ax, ay, (cudaStream_t)stream), "direct sample");
+    return BH_OK;
+}
+
+extern "C" int bh_box_moments(bh_plan *p, int sys, double *out, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (sys < 0 || sys >= p->nsys || !out) return fail(p, BH_ERR_INVALID, "bad box_moments args");
+    if (!p->has_tree) return fail(p, BH_ERR_INVALID, "box_moments before create_tree/summarize");
+    CK(p, launch_box_com(p->dev, sys, out, (cudaStream_t)stream), "box moments");
+    return BH_OK;
+}
+
+extern "C" int bh_grid_info(bh_plan *p, int sys, double *out, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (sys < 0 || sys >= p->nsys || !out) return fail(p, BH_ERR_INVALID, "bad grid_info args");
+    cudaStream_t st = (cudaStream_t)stream;
+    SysDyn dy;
+    CK(p, cudaMemcpyAsync(&dy, (char *)p->ws + p->o_dyn + sizeof(SysDyn) * sys, sizeof(dy),
+                          cudaMemcpyDeviceToHost, st), "read grid info");
+    CK(p, cudaStreamSynchronize(st), "sync");
+    out[0] = dy.minx;
+    out[1] = dy.miny;
+    out[2] = dy.step;
+    out[3] = (double)p->sys[sys].G;
+    out[4] = (double)p->sys[sys].n;
+    return BH_OK;
+}
+
+extern "C" int bh_diagnostics(bh_plan *p, int sys, int want_potential, double *out, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (sys < 0 || sys >= p->nsys || !out) return fail(p, BH_ERR_INVALID, "bad diagnostics args");
+    CK(p, launch_diag(p->dev, sys, want_potential, out, (cudaStream_t)stream), "diagnostics");
+    return BH_OK;
+}

@@ -1,0 +1,535 @@
+// bh_force.cu -- box-tiled force evaluation with the tick fused into its epilogue.
+//
+// Replaces g_evaluate_boxes (python-bh/barneshut/kernels/grid_decomposition/gpu/grid.py:116-157,
+// with d_self_self_grav / d_self_other_grav / d_self_COM_grav at :211-268) and, when the tick is
+// fused, g_tick_particles (gpu/grid.py:159-174).  The interaction semantics follow the reference
+// CPU path (kernels/grid_decomposition/sequential/evaluation.py:73-109 with
+// kernels/gravity/cpu_numba.py:30-92) in flat mode, and this project's opening-angle rule in
+// theta mode.
+//
+// One CTA per target group (TG x TG leaf boxes).  The CTA walks the cell pyramid level by level
+// (all threads test one frontier cell each; accepted cells, rejected leaves and children are
+// compacted with a block scan, so list order is deterministic), stages far entries (centre of
+// mass in the group frame, mass) and near-box particles (float4, shifted into the group frame)
+// in shared memory, and every thread accumulates one target particle over a slice of the staged
+// entries.  Lists that outgrow shared memory are evaluated and emptied on the fly.
+//
+// Pair arithmetic: a += m_j (x_j - x_t) * rcp(r^2 + eps^2) in FP32 (rcp.approx), far-field
+// contributions Kahan-compensated when requested; BH_PREC_FP64 runs the same lists in FP64.
+// Positions are box-relative offsets rounded once from FP64, so dx keeps ~1e-7 of a box edge.
+#include "bh_internal.cuh"
+
+namespace bh {
+
+constexpr int FT = 128;        // threads per CTA
+constexpr int FAR_CAP = 1024;  // far entries per flush
+constexpr int NEAR_CAP = 256;  // near boxes per flush
+constexpr int SRC_CAP = 1024;  // near sources per staging pass
+constexpr int FR_CAP = 1024;   // traversal frontier (cells per level)
+constexpr int MAX_TG = 8;
+
+template <typename R> struct Src;
+template <> struct Src<float> { using T = float4; };
+template <> struct Src<double> { struct T { double x, y, m; int idx, pad; }; };
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+template <typename R> __device__ __forceinline__ R rinv(R x);
+template <> __device__ __forceinline__ float rinv<float>(float x) { return rcp_approx(x); }
+template <> __device__ __forceinline__ double rinv<double>(double x) { return 1.0 / x; }
+
+__device__ __forceinline__ void src_get(const float4 &e, float &x, float &y, float &m, int &idx) {
+    x = e.x; y = e.y; m = e.z; idx = __float_as_int(e.w);
+}
+__device__ __forceinline__ void src_get(const Src<double>::T &e, double &x, double &y, double &m, int &idx) {
+    x = e.x; y = e.y; m = e.m; idx = e.idx;
+}
+
+__device__ __forceinline__ int block_scan_packed(int v, int *sh, int *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    int pre = x - v;
+    for (int k = 0; k < w; k++) pre += sh[k];
+    int tot = 0;
+    for (int k = 0; k < nw; k++) tot += sh[k];
+    *total = tot;
+    __syncthreads();
+    return pre;
+}
+
+template <typename R> struct Acc {
+    R nx, ny, fx, fy, cx, cy;
+};
+
+template <typename R, bool KAHAN>
+__device__ __forceinline__ void far_add(Acc<R> &a, R tx, R ty) {
+    if (KAHAN) {
+        R yx = tx - a.cx, t = a.fx + yx;
+        a.cx = (t - a.fx) - yx;
+        a.fx = t;
+        R yy = ty - a.cy, u = a.fy + yy;
+        a.cy = (u - a.fy) - yy;
+        a.fy = u;
+    } else {
+        a.fx += tx;
+        a.fy += ty;
+    }
+}
+
+template <typename R, bool KAHAN, bool TEST, bool EXACT>
+__global__ void __launch_bounds__(FT) k_force(DevPlan d, int tick, int accumulate) {
+    using S = typename Src<R>::T;
+    extern __shared__ __align__(16) unsigned char smem[];
+    S *far = reinterpret_cast<S *>(smem);                       // FAR_CAP
+    S *src = far + FAR_CAP;                                     // SRC_CAP
+    R *red = reinterpret_cast<R *>(src + SRC_CAP);              // 4 x FT
+    float2 *nshift = reinterpret_cast<float2 *>(red + 4 * FT);  // NEAR_CAP
+    int *nbox = reinterpret_cast<int *>(nshift + NEAR_CAP);     // NEAR_CAP (first particle)
+    int *ncnt = nbox + NEAR_CAP;                                // NEAR_CAP
+    int *npre = ncnt + NEAR_CAP;                                // NEAR_CAP + 1
+    int *front0 = npre + NEAR_CAP + 4;                          // FR_CAP
+    int *front1 = front0 + FR_CAP;                              // FR_CAP
+    __shared__ int sh_scan[32];
+    __shared__ int s_nfar, s_nnear, s_nnext, s_ovf;
+    __shared__ int s_col0[MAX_TG + 1], s_colpre[MAX_TG + 1];
+    __shared__ unsigned long long s_npairs, s_fpairs;
+
+    const int tid = threadIdx.x;
+    const int nxt = (d.glob->epoch + 1) & 1;
+    const double *Xs = d.X[nxt], *Ys = d.Y[nxt], *Ms = d.M[nxt];
+
+    for (long long g = blockIdx.x; g < d.NG_total; g += gridDim.x) {
+        const int s = find_seg(d.goff_tab, d.nsys, g);
+        const SysDesc &sd = d.sys[s];
+        const SysDyn &dy = d.dyn[s];
+        const long long lg = g - sd.goff;
+        const int TG = sd.TG, G = sd.G;
+        const int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
+        const int gx0 = gi * TG, gy0 = gj * TG;
+        const int gx1 = min(G, gx0 + TG), gy1 = min(G, gy0 + TG);
+        const int ncol = gx1 - gx0;
+        if (tid < ncol) {
+            long long b0 = sd.boff + (long long)(gx0 + tid) * G + gy0;
+            int st = d.box_start[b0];
+            s_col0[tid] = st;
+            s_colpre[tid + 1] = d.box_start[b0 + (gy1 - gy0)] - st;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            s_colpre[0] = 0;
+            for (int c = 1; c <= ncol; c++) s_colpre[c] += s_colpre[c - 1];
+            s_npairs = 0;
+            s_fpairs = 0;
+        }
+        __syncthreads();
+        const int nt = s_colpre[ncol];
+        if (nt == 0) {
+            __syncthreads();
+            continue;
+        }
+        const float step_f = __double2float_rn(dy.step);
+        const float W_f = __fmul_rn((float)TG, step_f);
+        const double gox = box_origin(dy.minx, gx0, dy.step), goy = box_origin(dy.miny, gy0, dy.step);
+        const R eps2 = (R)(sizeof(R) == 4 ? (double)d.eps2_f : d.eps2);
+        const R cut = (R)(sizeof(R) == 4 ? (double)d.cut_f : d.cutoff);
+
+        for (int c0 = 0; c0 < nt; c0 += FT) {
+            const int ntc = min(FT, nt - c0);
+            const int nslice = FT / ntc;
+            const bool active = tid < nslice * ntc;
+            const int tl = active ? tid % ntc : 0, slice = active ? tid / ntc : 0;
+            // target
+            int ti = 0;
+            R tx = 0, ty = 0;
+            double txd = 0, tyd = 0;
+            {
+                int u = c0 + tl, c = 0;
+                while (c + 1 < ncol && s_colpre[c + 1] <= u) c++;
+                ti = s_col0[c] + (u - s_colpre[c]);
+                if (sizeof(R) == 4) {
+                    float4 p = d.P[ti];
+                    int lb = d.skey[ti] - (int)sd.boff;
+                    int kx = lb / G, ky = lb - kx * G;
+                    tx = (R)__fadd_rn(__fmul_rn((float)(kx - gx0), step_f), p.x);
+                    ty = (R)__fadd_rn(__fmul_rn((float)(ky - gy0), step_f), p.y);
+                } else {
+                    tx = (R)(Xs[ti] - gox);
+                    ty = (R)(Ys[ti] - goy);
+                }
+                if (EXACT) {
+                    txd = Xs[ti];
+                    tyd = Ys[ti];
+                }
+            }
+            Acc<R> acc = {0, 0, 0, 0, 0, 0};
+
+            auto flush_far = [&]() {
+                __syncthreads();
+                const int nf = s_nfar;
+                if (active) {
+                    for (int k = slice; k < nf; k += nslice) {
+                        R sx, sy, sm;
+                        int sidx;
+                        src_get(far[k], sx, sy, sm, sidx);
+                        R dx = sx - tx, dyy = sy - ty;
+                        R r2 = dx * dx + dyy * dyy;
+                        R inv = rinv<R>(r2 + eps2);
+                        if (TEST && !(r2 > cut)) inv = 0;
+                        R w = sm * inv;
+                        far_add<R, KAHAN>(acc, w * dx, w * dyy);
+                    }
+                }
+                if (tid == 0) s_fpairs += (unsigned long long)ntc * nf;
+                __syncthreads();
+                if (tid == 0) s_nfar = 0;
+                __syncthreads();
+            };
+
+            auto flush_near = [&]() {
+                __syncthreads();
+                const int nn = s_nnear;
+                {
+                    constexpr int IT = NEAR_CAP / FT;
+                    int v[IT], sum = 0;
+#pragma unroll
+                    for (int k = 0; k < IT; k++) {
+                        int e = tid * IT + k;
+                        v[k] = e < nn ? ncnt[e] : 0;
+                        sum += v[k];
+                    }
+                    int tot;
+                    int pre = block_scan_packed(sum, sh_scan, &tot);
+#pragma unroll
+                    for (int k = 0; k < IT; k++) {
+                        int e = tid * IT + k;
+                        if (e < nn) npre[e] = pre;
+                        pre += v[k];
+                    }
+                    if (tid == 0) npre[nn] = tot;
+                }
+                __syncthreads();
+                const int total = npre[nn];
+                for (int s0 = 0; s0 < total; s0 += SRC_CAP) {
+                    const int ns = min(SRC_CAP, total - s0);
+                    for (int j = tid; j < ns; j += FT) {
+                        int J = s0 + j;
+                        int lo = 0, hi = nn;  // npre[lo] <= J < npre[hi]
+                        while (hi - lo > 1) {
+                            int mid = (lo + hi) >> 1;
+                            if (npre[mid] <= J) lo = mid; else hi = mid;
+                        }
+                        int idx = nbox[lo] + (J - npre[lo]);
+                        if (sizeof(R) == 4) {
+                            float4 p = d.P[idx];
+                            float2 sh = nshift[lo];
+                            float4 q = make_float4(__fadd_rn(sh.x, p.x), __fadd_rn(sh.y, p.y), p.z, p.w);
+                            reinterpret_cast<float4 *>(src)[j] = q;
+                        } else {
+                            typename Src<double>::T q;
+                            q.x = Xs[idx] - gox;
+                            q.y = Ys[idx] - goy;
+                            q.m = Ms[idx];
+                            q.idx = idx;
+                            q.pad = 0;
+                            reinterpret_cast<typename Src<double>::T *>(src)[j] = q;
+                        }
+                    }
+                    __syncthreads();
+                    if (active) {
+                        for (int j = slice; j < ns; j += nslice) {
+                            R sx, sy, sm;
+                            int sidx;
+                            src_get(src[j], sx, sy, sm, sidx);
+                            R dx = sx - tx, dyy = sy - ty;
+                            R r2 = dx * dx + dyy * dyy;
+                            R inv = rinv<R>(r2 + eps2);
+                            if (TEST) {
+                                bool keep = r2 > cut;
+                                if (EXACT) {
+                                    R band = cut * (R)1e-3;
+                                    R diff = r2 - cut;
+                                    if (diff <= band && diff >= -band) {
+                                        double ex = __dsub_rn(txd, Xs[sidx]), ey = __dsub_rn(tyd, Ys[sidx]);
+                                        double e2 = __dmul_rn(ex, ex);
+                                        e2 = __dadd_rn(e2, __dmul_rn(ey, ey));
+                                        keep = e2 > d.cutoff;
+                                    }
+                                }
+                                if (!keep) inv = 0;
+                            }
+                            R w = sm * inv;
+                            acc.nx += w * dx;
+                            acc.ny += w * dyy;
+                        }
+                    }
+                    if (tid == 0) s_npairs += (unsigned long long)ntc * ns;
+                    __syncthreads();
+                }
+                if (tid == 0) s_nnear = 0;
+                __syncthreads();
+            };
+
+            // append helper state
+            if (tid == 0) {
+                s_nfar = 0;
+                s_nnear = 0;
+                s_ovf = 0;
+            }
+            __syncthreads();
+
+            auto emit = [&](int kind, int cell_or_box, int l, int ci, int cj, float rx, float ry,
+                            float M, int *front_next, int gc) {
+                // kind: 0 none, 1 far, 2 near, 3 open
+                int nch = 0;
+                if (kind == 3) {
+                    for (int a = 0; a < 2; a++)
+                        for (int b = 0; b < 2; b++)
+                            if (2 * ci + a < gc && 2 * cj + b < gc) nch++;
+                }
+                int packed = (kind == 1 ? 1 : 0) | ((kind == 2 ? 1 : 0) << 10) | (nch << 20);
+                int tot;
+                int pre = block_scan_packed(packed, sh_scan, &tot);
+                if (kind == 1) {
+                    int pos = s_nfar + (pre & 1023);
+                    if (sizeof(R) == 4) {
+                        reinterpret_cast<float4 *>(far)[pos] = make_float4(rx, ry, M, __int_as_float(cell_or_box));
+                    } else {
+                        // FP64 centre of mass in the group frame from the FP64 moments
+                        const double *q = d.mom + 6 * (long long)cell_or_box;
+                        typename Src<double>::T e;
+                        double ox = box_origin(dy.minx, ci << l, dy.step) - gox;
+                        double oy = box_origin(dy.miny, cj << l, dy.step) - goy;
+                        e.x = ox + q[1] / q[0];
+                        e.y = oy + q[2] / q[0];
+                        e.m = q[0];
+                        e.idx = cell_or_box;
+                        e.pad = 0;
+                        reinterpret_cast<typename Src<double>::T *>(far)[pos] = e;
+                    }
+                } else if (kind == 2) {
+                    int pos = s_nnear + ((pre >> 10) & 1023);
+                    int st = d.box_start[cell_or_box];
+                    nbox[pos] = st;
+                    ncnt[pos] = d.box_start[cell_or_box + 1] - st;
+                    int lb = cell_or_box - (int)sd.boff;
+                    int kx = lb / G, ky = lb - kx * G;
+                    nshift[pos] = make_float2(__fmul_rn((float)(kx - gx0), step_f),
+                                              __fmul_rn((float)(ky - gy0), step_f));
+                } else if (kind == 3) {
+                    int pos = s_nnext + (pre >> 20);
+                    if (pos + nch > FR_CAP) {
+                        s_ovf = 1;
+                    } else {
+                        for (int a = 0; a < 2; a++)
+                            for (int b = 0; b < 2; b++)
+                                if (2 * ci + a < gc && 2 * cj + b < gc)
+                                    front_next[pos++] = (2 * ci + a) * gc + (2 * cj + b);
+                    }
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    s_nfar += tot & 1023;
+                    s_nnear += (tot >> 10) & 1023;
+                    s_nnext += tot >> 20;
+                }
+                __syncthreads();
+            };
+
+            if (d.flat) {
+                const long long B = (long long)G * G;
+                for (long long q0 = 0; q0 < B; q0 += FT) {
+                    if (s_nfar + FT > FAR_CAP) flush_far();
+                    if (s_nnear + FT > NEAR_CAP) flush_near();
+                    long long b = q0 + tid;
+                    int kind = 0, bx = 0, byy = 0;
+                    float rx = 0, ry = 0, M = 0;
+                    if (b < B) {
+                        bx = (int)(b / G);
+                        byy = (int)(b - (long long)bx * G);
+                        long long gb = sd.boff + b;
+                        if (d.box_start[gb + 1] > d.box_start[gb]) {
+                            if (abs(bx - gx0) <= 1 && abs(byy - gy0) <= 1) {
+                                kind = 2;
+                            } else {
+                                float4 r = d.rec[sd.coff + b];
+                                rx = __fadd_rn(__fmul_rn((float)(bx - gx0), step_f), r.x);
+                                ry = __fadd_rn(__fmul_rn((float)(byy - gy0), step_f), r.y);
+                                M = r.z;
+                                kind = 1;
+                            }
+                        }
+                    }
+                    int id = kind == 2 ? (int)(sd.boff + b) : (int)(sd.coff + b);
+                    emit(kind, id, 0, bx, byy, rx, ry, M, front1, 0);
+                }
+            } else {
+                int *fr = front0, *fn = front1;
+                if (tid == 0) fr[0] = 0;
+                int nfr = 1;
+                const float theta2 = d.theta2_f;
+                for (int l = sd.L - 1; l >= 0; l--) {
+                    const int gl = sd.lvg[l];
+                    const int gc = l > 0 ? sd.lvg[l - 1] : 0;
+                    if (tid == 0) s_nnext = 0;
+                    __syncthreads();
+                    for (int q0 = 0; q0 < nfr; q0 += FT) {
+                        if (s_nfar + FT > FAR_CAP) flush_far();
+                        if (s_nnear + FT > NEAR_CAP) flush_near();
+                        int q = q0 + tid;
+                        int kind = 0, ci = 0, cj = 0, id = 0;
+                        float rx = 0, ry = 0, M = 0;
+                        if (q < nfr) {
+                            int loc = fr[q];
+                            ci = loc / gl;
+                            cj = loc - ci * gl;
+                            long long cell = sd.coff + sd.lvoff[l] + loc;
+                            float4 r = d.rec[cell];
+                            if (r.z > 0.f) {
+                                int lo_x = ci << l, hi_x = (ci + 1) << l;
+                                int lo_y = cj << l, hi_y = (cj + 1) << l;
+                                bool overlap = lo_x < gx1 && hi_x > gx0 && lo_y < gy1 && hi_y > gy0;
+                                bool accept = false;
+                                if (!overlap) {
+                                    rx = __fadd_rn(__fmul_rn((float)(lo_x - gx0), step_f), r.x);
+                                    ry = __fadd_rn(__fmul_rn((float)(lo_y - gy0), step_f), r.y);
+                                    float dxo = fmaxf(0.f, fmaxf(-rx, __fsub_rn(rx, W_f)));
+                                    float dyo = fmaxf(0.f, fmaxf(-ry, __fsub_rn(ry, W_f)));
+                                    float d2 = __fadd_rn(__fmul_rn(dxo, dxo), __fmul_rn(dyo, dyo));
+                                    float s_f = ldexpf(step_f, l);
+                                    accept = __fmul_rn(s_f, s_f) < __fmul_rn(theta2, d2);
+                                }
+                                M = r.z;
+                                if (accept) {
+                                    kind = 1;
+                                    id = (int)cell;
+                                } else if (l == 0) {
+                                    kind = 2;
+                                    id = (int)(sd.boff + loc);
+                                } else {
+                                    kind = 3;
+                                }
+                            }
+                        }
+                        emit(kind, id, l, ci, cj, rx, ry, M, fn, gc);
+                    }
+                    int *t = fr;
+                    fr = fn;
+                    fn = t;
+                    // an overflowed frontier may hold unwritten slots: abandon the walk
+                    // (flagged; the host bounds theta and group size so this cannot happen)
+                    nfr = s_ovf ? 0 : min(s_nnext, FR_CAP);
+                    if (s_ovf && tid == 0) raise_err(d.glob, 2u /*BH_DEV_LIST_OVERFLOW*/);
+                }
+            }
+            flush_far();
+            flush_near();
+
+            // reduce slices and write
+            R farx = acc.fx - acc.cx, fary = acc.fy - acc.cy;
+            if (active) {
+                red[4 * tid + 0] = acc.nx;
+                red[4 * tid + 1] = acc.ny;
+                red[4 * tid + 2] = farx;
+                red[4 * tid + 3] = fary;
+            }
+            __syncthreads();
+            if (active && slice == 0) {
+                R sx = 0, sy = 0;
+                for (int k = 0; k < nslice; k++) {
+                    const R *r = red + 4 * (tl + k * ntc);
+                    sx += r[0] + r[2];
+                    sy += r[1] + r[3];
+                }
+                double ax = d.gconst * (double)sx, ay = d.gconst * (double)sy;
+                if (accumulate) {
+                    ax += (double)d.AX[ti];
+                    ay += (double)d.AY[ti];
+                }
+                d.AX[ti] = ax;
+                d.AY[ti] = ay;
+                if (tick) {
+                    double vx = d.VX[nxt][ti] + ax * d.dt, vy = d.VY[nxt][ti] + ay * d.dt;
+                    d.VX[nxt][ti] = vx;
+                    d.VY[nxt][ti] = vy;
+                    d.X[nxt][ti] = Xs[ti] + vx * d.dt;
+                    d.Y[nxt][ti] = Ys[ti] + vy * d.dt;
+                }
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            atomicAdd(&d.glob->near_pairs, s_npairs);
+            atomicAdd(&d.glob->far_pairs, s_fpairs);
+        }
+        __syncthreads();
+    }
+}
+
+template <typename R>
+static size_t force_smem() {
+    using S = typename Src<R>::T;
+    return sizeof(S) * (FAR_CAP + SRC_CAP) + sizeof(R) * 4 * FT + sizeof(float2) * NEAR_CAP +
+           sizeof(int) * (3 * NEAR_CAP + 4) + sizeof(int) * 2 * FR_CAP;
+}
+
+template <typename R, bool KAHAN, bool TEST, bool EXACT>
+static cudaError_t launch_force_t(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
+    auto k = k_force<R, KAHAN, TEST, EXACT>;
+    size_t sm = force_smem<R>();
+    long long grid = d.NG_total;
+    if (grid > (1LL << 30)) grid = 1LL << 30;
+    if (grid < 1) grid = 1;
+    k<<<(unsigned)grid, FT, sm, st>>>(d, tick ? 1 : 0, accumulate ? 1 : 0);
+    return cudaGetLastError();
+}
+
+template <typename R, bool KAHAN, bool TEST, bool EXACT>
+static cudaError_t init_force_t() {
+    return cudaFuncSetAttribute(k_force<R, KAHAN, TEST, EXACT>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)force_smem<R>());
+}
+
+// Raise the dynamic shared-memory limit of every instantiation once (outside
+// any stream capture).
+cudaError_t force_init() {
+    cudaError_t e;
+    if ((e = init_force_t<double, false, true, false>()) != cudaSuccess) return e;
+    if ((e = init_force_t<double, false, false, false>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, true, true, true>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, true, true, false>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, true, false, false>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, false, true, true>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, false, true, false>()) != cudaSuccess) return e;
+    return init_force_t<float, false, false, false>();
+}
+
+cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
+    if (d.n_total == 0) return cudaSuccess;
+    const bool test = d.cutoff > 0.0 || d.eps2 == 0.0;
+    const bool exact = d.cutoff > 0.0;
+    if (d.prec == 2) {
+        if (test) return launch_force_t<double, false, true, false>(d, tick, accumulate, st);
+        return launch_force_t<double, false, false, false>(d, tick, accumulate, st);
+    }
+    if (d.prec == 1) {
+        if (exact) return launch_force_t<float, true, true, true>(d, tick, accumulate, st);
+        if (test) return launch_force_t<float, true, true, false>(d, tick, accumulate, st);
+        return launch_force_t<float, true, false, false>(d, tick, accumulate, st);
+    }
+    if (exact) return launch_force_t<float, false, true, true>(d, tick, accumulate, st);
+    if (test) return launch_force_t<float, false, true, false>(d, tick, accumulate, st);
+    return launch_force_t<float, false, false, false>(d, tick, accumulate, st);
+}
+
+}  // namespace bh

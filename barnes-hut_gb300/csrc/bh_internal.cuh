@@ -1,0 +1,153 @@
+// bh_internal.cuh -- device-side layout shared by the kernels and the host
+// layer of libbh_gb300.
+//
+// Data layout in HBM (one workspace, carved by bh_api.cu):
+//   * particle state, double-buffered, box-sorted between steps, SoA FP64:
+//       X[2], Y[2], VX[2], VY[2], M[2] (n_total doubles each), PID[2] (int32)
+//     The up-to-date state is buffer (epoch + 1) & 1; the step prologue
+//     increments epoch, placement reads buffer epoch & 1 and scatters into
+//     buffer (epoch + 1) & 1, which summarize / force / tick then use.  The
+//     buffer choice is read on the device, so a captured CUDA graph of one
+//     step replays correctly any number of times.
+//   * P: packed float4 per box-sorted particle (x - box origin, y - box origin,
+//     mass, sorted index as int bits) -- the only array the force kernel
+//     streams for near-field sources.
+//   * AX, AY: FP64 accelerations, box-sorted order (aligned with the state).
+//   * key / slot: box key and rank-in-box per particle (placement output);
+//     skey: box key per box-sorted particle.
+//   * counts, box_start: per-box histogram and exclusive prefix (int32),
+//     concatenated over systems; box_start[b] is a global particle index.
+//   * mom: FP64 moments (M, Sx, Sy, Sxx, Sxy, Syy about the cell origin) for
+//     every pyramid cell; rec / rec2: float records the force kernel reads
+//     (centre of mass relative to the cell origin, mass; normalised second
+//     moments about the centre of mass).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace bh {
+
+constexpr int MAX_LEVELS = 16;  // G <= 32768
+
+struct SysDesc {
+    long long n, poff;  // particle count, first particle (concatenated)
+    long long boff;     // first box in counts / box_start
+    long long coff;     // first pyramid cell (leaves first)
+    long long goff;     // first target group
+    int G, L, TG, NGs;  // boxes per side, pyramid levels, group dim, groups per side
+    int lvg[MAX_LEVELS];         // cells per side per level
+    long long lvoff[MAX_LEVELS]; // first cell of each level, relative to coff
+};
+
+struct SysDyn {
+    unsigned long long bbmin[2];  // ordered bits of min x, min y (atomicMin)
+    unsigned long long bbmax[2];  // ordered bits of max x, max y (atomicMax)
+    double minx, miny, step;      // square bounding box origin and box edge
+};
+
+struct Globals {
+    unsigned int epoch;
+    unsigned int err;
+    unsigned long long near_pairs, far_pairs;
+};
+
+struct MlpDev;  // learned correction weights (bh_mlp.cu)
+
+struct DevPlan {
+    int nsys, Lmax;
+    long long n_total, B_total, C_total, NG_total;
+    const SysDesc *sys;
+    SysDyn *dyn;
+    Globals *glob;
+    const long long *poff_tab;  // nsys + 1 particle offsets
+    const long long *boff_tab;  // nsys + 1 box offsets
+    const long long *coff_tab;  // nsys + 1 cell offsets
+    const long long *goff_tab;  // nsys + 1 group offsets
+    const long long *lvl_tab;   // Lmax x (nsys + 1): prefix of level-l cells over systems
+    double *X[2], *Y[2], *VX[2], *VY[2], *M[2];
+    int *PID[2];
+    double *AX, *AY;  // accelerations, box-sorted order
+    float4 *P;
+    int *key, *slot, *skey;
+    int *counts, *box_start, *tile_sums;
+    double *mom;
+    float4 *rec, *rec2;
+    // parameters
+    double gconst, dt, eps2, cutoff;
+    float theta2_f, eps2_f, cut_f;
+    int flat, prec, learned;
+    const MlpDev *mlp;
+};
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ unsigned long long ord_bits(double d) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double unord_bits(unsigned long long u) {
+    u = (u & 0x8000000000000000ull) ? (u & ~0x8000000000000000ull) : ~u;
+    return __longlong_as_double((long long)u);
+}
+
+// index of the segment containing v in a sorted offset table tab[0..n]
+// (tab[0] = 0 <= v < tab[n]); n is small (systems).
+__device__ __forceinline__ int find_seg(const long long *tab, int n, long long v) {
+    int lo = 0, hi = n;  // invariant tab[lo] <= v < tab[hi]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (tab[mid] <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Square bounding box exactly as python-bh/barneshut/kernels/helpers/grid.py:10-26
+// and base.py:233-239 compute it (no FMA contraction).
+__device__ __forceinline__ void square_bbox(double mnx, double mny, double mxx, double mxy, int G,
+                                            double *step) {
+    double xe = __dsub_rn(mxx, mnx), ye = __dsub_rn(mxy, mny);
+    if (xe > ye) mxy = __dadd_rn(mxy, __dsub_rn(xe, ye));
+    else if (ye > xe) mxx = __dadd_rn(mxx, __dsub_rn(ye, xe));
+    *step = __ddiv_rn(__dsub_rn(mxx, mnx), (double)G);
+}
+
+// Box index of one coordinate: clip(floor((p - mn) / step), 0, G - 1)
+// (implementations/sequential.py:32-34; gpu/grid.py:37-40).
+__device__ __forceinline__ int box_key1(double p, double mn, double step, int G) {
+    if (!(step > 0.0)) return 0;
+    double k = floor(__ddiv_rn(__dsub_rn(p, mn), step));
+    k = fmin(fmax(k, 0.0), (double)(G - 1));
+    return (int)k;
+}
+
+// Origin of leaf box k along one axis: mn + k * step, FP64, no contraction.
+__device__ __forceinline__ double box_origin(double mn, int k, double step) {
+    return __dadd_rn(mn, __dmul_rn((double)k, step));
+}
+
+__device__ __forceinline__ void raise_err(Globals *g, unsigned f) {
+    if ((atomicOr(&g->err, 0u) & f) == 0) atomicOr(&g->err, f);
+}
+
+}  // namespace bh
+
+// kernel launch wrappers (bh_tree.cu, bh_force.cu, bh_misc.cu)
+namespace bh {
+cudaError_t launch_prologue(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_bbox(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_place(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_scan(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st);
+cudaError_t force_init();
+cudaError_t launch_tick(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_load(const DevPlan &d, const double *x, const double *y, const double *m,
+                        const double *vx, const double *vy, long long rec_stride,
+                        cudaStream_t st);
+cudaError_t launch_store(const DevPlan &d, int has_tree, double *rec, double *x, double *y, double *vx,
+                         double *vy, double *ax, double *ay, cudaStream_t st);
+cudaError_t launch_direct(const DevPlan &d, int sys, const long long *targets, long long nt,
+                          double *ax, double *ay, cudaStream_t st);
+cudaError_t launch_diag(const DevPlan &d, int sys, int want_pot, double *out, cudaStream_t st);
+cudaError_t launch_box_com(const DevPlan &d, int sys, double *out, cudaStream_t st);
+}  // namespace bh

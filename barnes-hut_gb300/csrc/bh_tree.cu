@@ -1,0 +1,399 @@
+// bh_tree.cu -- create_tree and summarize kernels.
+//
+// create_tree = prologue -> bbox -> place -> scan (3 phases) -> scatter.
+//   Replaces set_particles_bounding_box (python-bh/barneshut/implementations/base.py:211-239),
+//   g_place_particles, g_calculate_box_cumm, g_sort_particles
+//   (python-bh/barneshut/kernels/grid_decomposition/gpu/grid.py:15-76).
+// summarize = leaf moments (segmented warp reduction) -> pyramid levels -> records.
+//   Replaces g_summarize (gpu/grid.py:78-114) and calc_COM (internals/cloud.py:9-17).
+#include "bh_internal.cuh"
+
+namespace bh {
+
+constexpr int TPB = 256;
+constexpr int SCAN_TILE = 4096;  // counts per scan tile (256 threads x 16)
+
+static inline unsigned grid_for(long long n, int tpb, long long cap = 152LL * 16) {
+    long long b = (n + tpb - 1) / tpb;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (unsigned)b;
+}
+
+// ----------------------------------------------------------------- prologue
+// Zero the box histogram and the leaf moments, reset the bounding-box
+// accumulators and pair counters, advance the state epoch.
+__global__ void k_prologue(DevPlan d) {
+    long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    if (tid == 0) {
+        d.glob->epoch += 1;
+        d.glob->near_pairs = 0;
+        d.glob->far_pairs = 0;
+    }
+    if (tid < d.nsys) {
+        d.dyn[tid].bbmin[0] = d.dyn[tid].bbmin[1] = ~0ull;
+        d.dyn[tid].bbmax[0] = d.dyn[tid].bbmax[1] = 0ull;
+    }
+    for (long long b = tid; b < d.B_total; b += stride) {
+        d.counts[b] = 0;
+        int s = find_seg(d.boff_tab, d.nsys, b);
+        long long c = d.sys[s].coff + (b - d.sys[s].boff);
+        double *q = d.mom + 6 * c;
+#pragma unroll
+        for (int k = 0; k < 6; k++) q[k] = 0.0;
+    }
+}
+
+// --------------------------------------------------------------------- bbox
+// Min / max of x and y per system on the ordered-integer image of the doubles
+// (integer min/max, no FP64 pipe work).  Each block reduces a contiguous tile.
+__global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
+    const int cur = d.glob->epoch & 1;
+    const double *X = d.X[cur], *Y = d.Y[cur];
+    __shared__ unsigned long long red[4][TPB / 32];
+    __shared__ int sys0;
+    const long long tile = (long long)TPB * 16;
+    for (long long t0 = (long long)blockIdx.x * tile; t0 < d.n_total; t0 += (long long)gridDim.x * tile) {
+        long long t1 = t0 + tile < d.n_total ? t0 + tile : d.n_total;
+        if (threadIdx.x == 0) sys0 = find_seg(d.poff_tab, d.nsys, t0);
+        __syncthreads();
+        int s_first = sys0;
+        bool one_sys = d.poff_tab[s_first + 1] >= t1;
+        unsigned long long mn0 = ~0ull, mn1 = ~0ull, mx0 = 0, mx1 = 0;
+        int cs = s_first;
+        for (long long i = t0 + threadIdx.x; i < t1; i += TPB) {
+            if (!one_sys) {
+                int s = find_seg(d.poff_tab, d.nsys, i);
+                if (s != cs) {
+                    if (mx0 | mx1) {
+                        atomicMin(&d.dyn[cs].bbmin[0], mn0); atomicMin(&d.dyn[cs].bbmin[1], mn1);
+                        atomicMax(&d.dyn[cs].bbmax[0], mx0); atomicMax(&d.dyn[cs].bbmax[1], mx1);
+                    }
+                    mn0 = mn1 = ~0ull; mx0 = mx1 = 0; cs = s;
+                }
+            }
+            unsigned long long ux = ord_bits(X[i]), uy = ord_bits(Y[i]);
+            mn0 = ux < mn0 ? ux : mn0; mx0 = ux > mx0 ? ux : mx0;
+            mn1 = uy < mn1 ? uy : mn1; mx1 = uy > mx1 ? uy : mx1;
+        }
+        if (!one_sys) {
+            if (mx0 | mx1) {
+                atomicMin(&d.dyn[cs].bbmin[0], mn0); atomicMin(&d.dyn[cs].bbmin[1], mn1);
+                atomicMax(&d.dyn[cs].bbmax[0], mx0); atomicMax(&d.dyn[cs].bbmax[1], mx1);
+            }
+        } else {
+            for (int o = 16; o; o >>= 1) {
+                unsigned long long a = __shfl_xor_sync(0xffffffffu, mn0, o); mn0 = a < mn0 ? a : mn0;
+                a = __shfl_xor_sync(0xffffffffu, mn1, o); mn1 = a < mn1 ? a : mn1;
+                a = __shfl_xor_sync(0xffffffffu, mx0, o); mx0 = a > mx0 ? a : mx0;
+                a = __shfl_xor_sync(0xffffffffu, mx1, o); mx1 = a > mx1 ? a : mx1;
+            }
+            int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+            if (l == 0) { red[0][w] = mn0; red[1][w] = mn1; red[2][w] = mx0; red[3][w] = mx1; }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int k = 1; k < TPB / 32; k++) {
+                    mn0 = red[0][k] < mn0 ? red[0][k] : mn0; mn1 = red[1][k] < mn1 ? red[1][k] : mn1;
+                    mx0 = red[2][k] > mx0 ? red[2][k] : mx0; mx1 = red[3][k] > mx1 ? red[3][k] : mx1;
+                }
+                atomicMin(&d.dyn[s_first].bbmin[0], mn0); atomicMin(&d.dyn[s_first].bbmin[1], mn1);
+                atomicMax(&d.dyn[s_first].bbmax[0], mx0); atomicMax(&d.dyn[s_first].bbmax[1], mx1);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// -------------------------------------------------------------------- place
+// FP64 box keys (bit-exact with the reference), warp-aggregated histogram:
+// lanes with the same key elect one leader that adds the group's size; each
+// lane's rank in the group plus the leader's old count is its slot in the box.
+__global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
+    const int cur = d.glob->epoch & 1;
+    const double *X = d.X[cur], *Y = d.Y[cur];
+    const int lane = threadIdx.x & 31;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    long long base = (long long)blockIdx.x * blockDim.x;
+    for (; base < d.n_total; base += stride) {
+        long long i = base + threadIdx.x;
+        int key = -1;
+        if (i < d.n_total) {
+            int s = find_seg(d.poff_tab, d.nsys, i);
+            const SysDesc &sd = d.sys[s];
+            SysDyn &dy = d.dyn[s];
+            double mnx = unord_bits(dy.bbmin[0]), mny = unord_bits(dy.bbmin[1]);
+            double mxx = unord_bits(dy.bbmax[0]), mxy = unord_bits(dy.bbmax[1]);
+            double step;
+            square_bbox(mnx, mny, mxx, mxy, sd.G, &step);
+            if (i == sd.poff) { dy.minx = mnx; dy.miny = mny; dy.step = step; }
+            double x = X[i], y = Y[i];
+            if (!(isfinite(x) && isfinite(y))) raise_err(d.glob, 1u /*BH_DEV_NAN_POSITION*/);
+            int kx = box_key1(x, mnx, step, sd.G), ky = box_key1(y, mny, step, sd.G);
+            key = (int)(sd.boff + (long long)kx * sd.G + ky);
+        }
+        unsigned peers = __match_any_sync(0xffffffffu, key);
+        int leader = __ffs(peers) - 1;
+        int rank = __popc(peers & ((1u << lane) - 1u));
+        int old = 0;
+        if (lane == leader && key >= 0) old = atomicAdd(&d.counts[key], __popc(peers));
+        old = __shfl_sync(0xffffffffu, old, leader);
+        if (i < d.n_total) {
+            d.key[i] = key;
+            d.slot[i] = old + rank;
+        }
+    }
+}
+
+// --------------------------------------------------------------------- scan
+// Exclusive scan of the box histogram (all systems concatenated; systems are
+// laid out in particle order, so the global prefix is the global particle
+// index of each box's first particle).  Phase 1: per-tile sums; phase 2: one
+// block scans the tile sums; phase 3: per-tile scan plus carry.
+__device__ __forceinline__ int block_excl_scan(int v, int *sh, int *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int t = lane < nw ? sh[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < nw) sh[lane] = t;
+    }
+    __syncthreads();
+    int pre = (w ? sh[w - 1] : 0) + x - v;
+    if (total) *total = sh[nw - 1];
+    __syncthreads();
+    return pre;
+}
+
+__global__ void __launch_bounds__(TPB) k_scan_tiles(DevPlan d) {
+    __shared__ int sh[32];
+    long long t0 = (long long)blockIdx.x * SCAN_TILE;
+    int s = 0;
+    for (int k = threadIdx.x; k < SCAN_TILE; k += TPB) {
+        long long b = t0 + k;
+        if (b < d.B_total) s += d.counts[b];
+    }
+    int tot;
+    block_excl_scan(s, sh, &tot);
+    if (threadIdx.x == 0) d.tile_sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(DevPlan d, int ntiles) {
+    __shared__ int sh[32];
+    int carry = 0;
+    for (int t0 = 0; t0 < ntiles; t0 += 1024) {
+        int t = t0 + threadIdx.x;
+        int v = t < ntiles ? d.tile_sums[t] : 0;
+        int tot;
+        int p = block_excl_scan(v, sh, &tot);
+        if (t < ntiles) d.tile_sums[t] = carry + p;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) d.box_start[d.B_total] = carry;
+}
+
+__global__ void __launch_bounds__(TPB) k_scan_apply(DevPlan d) {
+    __shared__ int sh[32];
+    long long t0 = (long long)blockIdx.x * SCAN_TILE;
+    // each thread owns 16 consecutive counts
+    long long b0 = t0 + (long long)threadIdx.x * 16;
+    int v[16], s = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        v[k] = (b0 + k < d.B_total) ? d.counts[b0 + k] : 0;
+        s += v[k];
+    }
+    int pre = block_excl_scan(s, sh, nullptr) + d.tile_sums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        if (b0 + k < d.B_total) d.box_start[b0 + k] = pre;
+        pre += v[k];
+    }
+}
+
+// ------------------------------------------------------------------ scatter
+// Counting-sort scatter into box order: destination = box_start[key] + slot.
+// Writes the FP64 state of the next buffer, the packed float4 record (offsets
+// from the box origin computed in FP64, rounded once to float) and the
+// per-sorted-particle key.
+__global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
+    const int cur = d.glob->epoch & 1, nxt = cur ^ 1;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < d.n_total; i += stride) {
+        int key = d.key[i];
+        int dst = d.box_start[key] + d.slot[i];
+        int s = find_seg(d.boff_tab, d.nsys, key);
+        const SysDesc &sd = d.sys[s];
+        const SysDyn &dy = d.dyn[s];
+        int lb = (int)(key - sd.boff);
+        int kx = lb / sd.G, ky = lb - kx * sd.G;
+        double x = d.X[cur][i], y = d.Y[cur][i], m = d.M[cur][i];
+        d.X[nxt][dst] = x;
+        d.Y[nxt][dst] = y;
+        d.VX[nxt][dst] = d.VX[cur][i];
+        d.VY[nxt][dst] = d.VY[cur][i];
+        d.M[nxt][dst] = m;
+        d.PID[nxt][dst] = d.PID[cur][i];
+        float ox = __double2float_rn(__dsub_rn(x, box_origin(dy.minx, kx, dy.step)));
+        float oy = __double2float_rn(__dsub_rn(y, box_origin(dy.miny, ky, dy.step)));
+        d.P[dst] = make_float4(ox, oy, __double2float_rn(m), __int_as_float(dst));
+        d.skey[dst] = key;
+    }
+}
+
+// ------------------------------------------------------------- leaf moments
+// Segmented warp reduction over the box-sorted particles: lanes holding the
+// same box key are contiguous; an inclusive segmented scan of the float
+// contributions (offsets are box-relative, so 32 terms in FP32 are exact to
+// ~1e-7 of a box) ends in the segment's last lane, which adds the partial
+// into the box's FP64 moments with FP64 atomics.
+__global__ void __launch_bounds__(TPB) k_leaf_moments(DevPlan d) {
+    const int lane = threadIdx.x & 31;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < d.n_total; base += stride) {
+        long long i = base + threadIdx.x;
+        int key = -1;
+        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (i < d.n_total) {
+            key = d.skey[i];
+            float4 p = d.P[i];
+            v[0] = p.z;
+            v[1] = p.z * p.x;
+            v[2] = p.z * p.y;
+            v[3] = v[1] * p.x;
+            v[4] = v[1] * p.y;
+            v[5] = v[2] * p.y;
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int k2 = __shfl_up_sync(0xffffffffu, key, o);
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                float y = __shfl_up_sync(0xffffffffu, v[c], o);
+                if (lane >= o && k2 == key) v[c] += y;
+            }
+        }
+        int knext = __shfl_down_sync(0xffffffffu, key, 1);
+        bool tail = (lane == 31) || (knext != key);
+        if (tail && key >= 0) {
+            int s = find_seg(d.boff_tab, d.nsys, key);
+            long long c = d.sys[s].coff + (key - d.sys[s].boff);
+            double *q = d.mom + 6 * c;
+#pragma unroll
+            for (int k = 0; k < 6; k++) atomicAdd(q + k, (double)v[k]);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ pyramid
+// Level-l cell = sum of its (up to) four level-(l-1) children, moments shifted
+// from the child origin to the parent origin (FP64).
+__global__ void __launch_bounds__(TPB) k_pyramid_level(DevPlan d, int l) {
+    const long long *tab = d.lvl_tab + (long long)l * (d.nsys + 1);
+    long long total = tab[d.nsys];
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        int s = find_seg(tab, d.nsys, t);
+        const SysDesc &sd = d.sys[s];
+        double step = d.dyn[s].step;
+        long long loc = t - tab[s];
+        int gl = sd.lvg[l], gc = sd.lvg[l - 1];
+        int i = (int)(loc / gl), j = (int)(loc - (long long)i * gl);
+        double p[6] = {0, 0, 0, 0, 0, 0};
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++) {
+                int ci = 2 * i + a, cj = 2 * j + b;
+                if (ci >= gc || cj >= gc) continue;
+                const double *c = d.mom + 6 * (sd.coff + sd.lvoff[l - 1] + (long long)ci * gc + cj);
+                double dx = (double)(a << (l - 1)) * step, dy = (double)(b << (l - 1)) * step;
+                double M = c[0], Sx = c[1], Sy = c[2];
+                p[0] += M;
+                p[1] += Sx + M * dx;
+                p[2] += Sy + M * dy;
+                p[3] += c[3] + 2.0 * dx * Sx + M * dx * dx;
+                p[4] += c[4] + dx * Sy + dy * Sx + M * dx * dy;
+                p[5] += c[5] + 2.0 * dy * Sy + M * dy * dy;
+            }
+        double *q = d.mom + 6 * (sd.coff + sd.lvoff[l] + loc);
+#pragma unroll
+        for (int k = 0; k < 6; k++) q[k] = p[k];
+    }
+}
+
+// Float records: centre of mass relative to the cell origin and mass; second
+// moments about the centre of mass normalised by M s^2 (s = cell edge).
+__global__ void __launch_bounds__(TPB) k_records(DevPlan d) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < d.C_total; c += stride) {
+        const double *q = d.mom + 6 * c;
+        double M = q[0];
+        if (M > 0.0) {
+            double cx = q[1] / M, cy = q[2] / M;
+            d.rec[c] = make_float4(__double2float_rn(cx), __double2float_rn(cy), __double2float_rn(M), 0.f);
+            int s = find_seg(d.coff_tab, d.nsys, c);
+            const SysDesc &sd = d.sys[s];
+            long long loc = c - sd.coff;
+            int l = 0;
+            while (l + 1 < sd.L && sd.lvoff[l + 1] <= loc) l++;
+            double sz = (double)(1 << l) * d.dyn[s].step;
+            double nrm = 1.0 / (M * sz * sz);
+            double ixx = q[3] - q[1] * cx, ixy = q[4] - q[1] * cy, iyy = q[5] - q[2] * cy;
+            d.rec2[c] = make_float4(__double2float_rn(ixx * nrm), __double2float_rn(ixy * nrm),
+                                    __double2float_rn(iyy * nrm), 0.f);
+        } else {
+            d.rec[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+            d.rec2[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ launches
+cudaError_t launch_prologue(const DevPlan &d, cudaStream_t st) {
+    long long n = d.B_total > d.nsys ? d.B_total : d.nsys;
+    k_prologue<<<grid_for(n, TPB), TPB, 0, st>>>(d);
+    return cudaGetLastError();
+}
+cudaError_t launch_bbox(const DevPlan &d, cudaStream_t st) {
+    if (d.n_total == 0) return cudaSuccess;
+    k_bbox<<<grid_for(d.n_total, TPB * 16, 152LL * 8), TPB, 0, st>>>(d);
+    return cudaGetLastError();
+}
+cudaError_t launch_place(const DevPlan &d, cudaStream_t st) {
+    if (d.n_total == 0) return cudaSuccess;
+    k_place<<<grid_for(d.n_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
+    return cudaGetLastError();
+}
+cudaError_t launch_scan(const DevPlan &d, cudaStream_t st) {
+    int ntiles = (int)((d.B_total + SCAN_TILE - 1) / SCAN_TILE);
+    if (ntiles < 1) ntiles = 1;
+    k_scan_tiles<<<ntiles, TPB, 0, st>>>(d);
+    k_scan_sums<<<1, 1024, 0, st>>>(d, ntiles);
+    k_scan_apply<<<ntiles, TPB, 0, st>>>(d);
+    return cudaGetLastError();
+}
+cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
+    if (d.n_total == 0) return cudaSuccess;
+    k_scatter<<<grid_for(d.n_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
+    return cudaGetLastError();
+}
+cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st) {
+    if (d.n_total > 0) k_leaf_moments<<<grid_for(d.n_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
+    for (int l = 1; l < d.Lmax; l++) {
+        // level-l cell count across systems is known on the host side of the
+        // plan; the kernel reads it from lvl_tab, so launch a generous grid.
+        k_pyramid_level<<<152 * 4, TPB, 0, st>>>(d, l);
+    }
+    k_records<<<grid_for(d.C_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
+    return cudaGetLastError();
+}
+
+}  // namespace bh

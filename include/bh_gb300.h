@@ -1,0 +1,190 @@
+/*
+ * bh_gb300.h -- C ABI of the GB300-native 2D grid-decomposition Barnes-Hut step.
+ *
+ * The reference (ut-parla/barnes-hut, python-bh) has no native FFI: its
+ * single-GPU implementation calls Numba CUDA kernels from Python.  The entry
+ * points below are the calls that implementation makes, one per step phase
+ * of its step interface (python-bh/barneshut/implementations/base.py:94-135):
+ * each declaration cites the reference code it replaces.
+ *
+ * Conventions
+ *  - Every function returns an int status (BH_OK == 0) and never aborts;
+ *    bh_last_error(plan) gives a one-line message for the last failure.
+ *  - All device work is asynchronous on the stream passed as `void *stream`
+ *    (a cudaStream_t; NULL is the legacy default stream).
+ *  - The library allocates no device memory.  The caller queries
+ *    bh_workspace_size() and passes one device buffer to bh_bind(); all
+ *    per-system state lives inside it.  A plan holds no global state, so
+ *    several plans may be used concurrently from different host threads
+ *    (python-bh/bin/run_2d_concurrent.py:53-87 runs instances in threads).
+ *  - A plan steps `nsys` independent systems at once (particles, boxes and
+ *    pyramid cells are concatenated); nsys = 1 is the reference's case.
+ *  - Device pointers passed in are plain `double *` arrays of the
+ *    concatenated particles in original particle (pid) order.
+ */
+#ifndef BH_GB300_H
+#define BH_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BH_OK 0
+#define BH_ERR_INVALID 1   /* invalid argument (checked on the host) */
+#define BH_ERR_CUDA 2      /* a CUDA runtime call failed */
+#define BH_ERR_WORKSPACE 3 /* no workspace bound, or too small */
+#define BH_ERR_DEVICE 4    /* a kernel raised a device error flag */
+#define BH_ERR_TIMEOUT 5   /* a bounded device wait gave up */
+
+/* device error flags (bh_error_flags) */
+#define BH_DEV_NAN_POSITION 1u   /* a non-finite position reached placement */
+#define BH_DEV_LIST_OVERFLOW 2u  /* an interaction-list frontier overflowed */
+#define BH_DEV_BAD_KEY 4u        /* a box key fell outside [0, G*G) */
+#define BH_DEV_WAIT_TIMEOUT 8u   /* a bounded spin-wait expired */
+
+/* precision of the pairwise force arithmetic */
+#define BH_PREC_FP32 0       /* FP32 pairs, plain far-field sum */
+#define BH_PREC_FP32_KAHAN 1 /* FP32 pairs, Kahan-compensated far-field sum */
+#define BH_PREC_FP64 2       /* FP64 pairs (precision study) */
+
+/* bh_params.flags */
+#define BH_FLAG_LEARNED 1 /* apply the learned far-field correction (weights bound) */
+
+typedef struct bh_params {
+    double grav_constant; /* [bh] grav_constant (python-bh/configs/default.ini) */
+    double tick_seconds;  /* [bh] tick_seconds: dt of v += a dt; x += v dt */
+    double softening;     /* Plummer epsilon; 0 = none (the reference has none) */
+    double cutoff_r2;     /* pairs with unsoftened r^2 <= cutoff_r2 contribute 0.
+                             1e-5 = the reference CPU kernels (cpu_numba.py:36);
+                             0 = skip only coincident points (reference GPU). */
+    double theta;         /* opening angle; <= 0 = the reference's flat far field
+                             (3x3 neighbourhood direct, every other box's COM) */
+    int group_dim;        /* target group = group_dim^2 leaf boxes (1, 2, 4, 8;
+                             0 = automatic); forced to 1 in flat mode */
+    int precision;        /* BH_PREC_* */
+    int flags;            /* BH_FLAG_* */
+    int reserved;
+} bh_params;
+
+typedef struct bh_plan bh_plan;
+
+/* Grid sizing of the reference: nleaves = n / (0.7 * ppb), rounded up to a
+ * perfect square, G = sqrt(nleaves).
+ * Replaces python-bh/barneshut/implementations/base.py:211-231 and
+ * kernels/helpers/grid.py:5-8. */
+int bh_grid_dim(long long n, int max_particles_per_box);
+
+/* Create a plan for nsys systems with n[s] particles and grid_dim[s] boxes per
+ * side (grid_dim[s] <= 0: bh_grid_dim(n[s], 1000)).  Host only, no CUDA call.
+ * Replaces SingleGPUBarnesHut.__init__ (implementations/singlegpu.py:18-26). */
+int bh_plan_create(bh_plan **plan, int nsys, const long long *n, const int *grid_dim,
+                   const bh_params *params);
+int bh_plan_destroy(bh_plan *plan);
+/* Message of the last failure on this plan; bh_last_error(NULL) gives the
+ * last bh_plan_create failure of the calling thread. */
+const char *bh_last_error(const bh_plan *plan);
+
+/* Device bytes the plan needs (state double buffers, keys, box table, cell
+ * pyramid, tables).  Host only. */
+int bh_workspace_size(const bh_plan *plan, size_t *bytes);
+
+/* Bind a device workspace (>= bh_workspace_size bytes, 256-byte aligned) on
+ * the current device, upload the system tables and zero the counters.
+ * Replaces the device allocations of singlegpu.py:28-39 (__init_device_arrays). */
+int bh_bind(bh_plan *plan, void *workspace, size_t bytes, void *stream);
+
+/* Upload the particle state from device arrays in pid order (concatenated
+ * over systems): positions x, y, masses m, velocities vx, vy (each n_total
+ * doubles).  Accelerations start at zero.
+ * Replaces cuda.to_device(self.particles) (singlegpu.py:37) of the file
+ * reader's N x 10 record (base.py:47-72). */
+int bh_load(bh_plan *plan, const double *x, const double *y, const double *m, const double *vx,
+            const double *vy, void *stream);
+
+/* Same, from the reference's N x 10 float64 particle record (field order
+ * px, py, mass, vx, vy, ax, ay, gx, gy, pid: internals/particle.py:3-15),
+ * as a device array in row order.  Rows are loaded in order; pid = row. */
+int bh_load_records(bh_plan *plan, const double *records, void *stream);
+
+/* Write the current state as N x 10 float64 records in pid order (gx, gy =
+ * the particle's box, ax, ay = the last accelerations) into a device array.
+ * Replaces ensure_particles_id_ordered (singlegpu.py:101-103). */
+int bh_store_records(bh_plan *plan, double *records, void *stream);
+
+/* Same as SoA arrays (any pointer may be NULL to skip that field). */
+int bh_store(bh_plan *plan, double *x, double *y, double *vx, double *vy, double *ax,
+             double *ay, void *stream);
+
+/* Square bounding box, box keys, box histogram, exclusive scan and the
+ * counting-sort scatter into box order (FP64 keys, bit-exact with the
+ * reference: box index (gx, gy) = clip(floor((p - min) / step), 0, G-1)).
+ * Replaces create_tree (singlegpu.py:41-67): set_particles_bounding_box
+ * (base.py:211-239), g_place_particles, g_calculate_box_cumm and
+ * g_sort_particles (kernels/grid_decomposition/gpu/grid.py:15-76). */
+int bh_create_tree(bh_plan *plan, void *stream);
+
+/* Per-box FP64 mass, centre of mass and second moments (segmented warp
+ * reduction over the box-sorted particles), the cell pyramid and the float
+ * cell records the force kernel reads.
+ * Replaces summarize (singlegpu.py:69-77) and g_summarize (gpu/grid.py:78-114). */
+int bh_summarize(bh_plan *plan, void *stream);
+
+/* a += forces (reference semantics: accelerations accumulate until the tick
+ * zeroes them).  Replaces evaluate (singlegpu.py:79-92) and g_evaluate_boxes
+ * (gpu/grid.py:116-157) with the CPU path's semantics selected by params
+ * (evaluation.py:73-109, cpu_numba.py:30-92). */
+int bh_evaluate(bh_plan *plan, void *stream);
+
+/* v += a dt; a = 0; x += v dt.  Replaces timestep (singlegpu.py:94-99) and
+ * g_tick_particles (gpu/grid.py:159-174). */
+int bh_timestep(bh_plan *plan, void *stream);
+
+/* nsteps rounds of create_tree, summarize, evaluate with the tick fused into
+ * the force epilogue (accelerations are overwritten, not accumulated, and
+ * kept for bh_store).  Replaces the round loop of BaseBarnesHut.run
+ * (base.py:104-127) with evaluation_rounds = 1. */
+int bh_step(bh_plan *plan, int nsteps, void *stream);
+
+/* bh_step captured once into a CUDA graph (per nsteps value) and replayed. */
+int bh_step_graph(bh_plan *plan, int nsteps, void *stream);
+
+/* Synchronise the stream and read (then clear) the device error flags. */
+int bh_error_flags(bh_plan *plan, unsigned *flags, void *stream);
+
+/* Pair interactions of the last force evaluation, counted exactly by the
+ * force kernel: near = particle-particle, far = particle-cell (synchronises). */
+int bh_pair_counts(bh_plan *plan, long long *near_pairs, long long *far_pairs, void *stream);
+
+/* Leaf-box centres of mass of system `sys` from the last bh_summarize, in the
+ * reference's layout: out[(gx * G + gy) * 3 + {0, 1, 2}] = (cx, cy, M), zeros
+ * for an empty box (device array of G*G*3 doubles).  Replaces reading the
+ * COM grid d_COMs (singlegpu.py:38,69-77; gpu/grid.py:78-114). */
+int bh_box_moments(bh_plan *plan, int sys, double *out, void *stream);
+
+/* Square bounding box of system `sys` from the last bh_create_tree into host
+ * out[5] = {min_x, min_y, step, grid_dim, n} (synchronises).  Replaces the
+ * attributes min_xy, step, grid_dim that set_particles_bounding_box sets
+ * (base.py:211-239). */
+int bh_grid_info(bh_plan *plan, int sys, double *out, void *stream);
+
+/* FP64 direct sum on the device for nt targets (indices into the
+ * concatenated pid order, device array) of system `sys`, no cutoff, the
+ * plan's softening: a_t = G sum_{j != t} m_j (x_j - x_t) / (r^2 + eps^2).
+ * Outputs ax, ay (device, nt doubles).  Replaces nsquared_acc_check
+ * (base.py:16-32) of the --check accuracy sampler (base.py:149-205). */
+int bh_direct_sample(bh_plan *plan, int sys, const long long *targets, long long nt,
+                     double *ax, double *ay, void *stream);
+
+/* FP64 diagnostics of system `sys` into out[4] (device doubles):
+ * kinetic energy, momentum x, momentum y, and the potential energy
+ * sum_{i<j} G m_i m_j ln(sqrt(r^2 + eps^2)) by an FP64 direct sum (O(n^2):
+ * pass want_potential = 0 to skip it for large n).  No reference
+ * counterpart (the reference reports no energies). */
+int bh_diagnostics(bh_plan *plan, int sys, int want_potential, double *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BH_GB300_H */

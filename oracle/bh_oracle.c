@@ -1,0 +1,675 @@
+/*
+ * bh_oracle.c -- CPU oracle for the 2D grid-decomposition Barnes-Hut step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: the tests, the smoke
+ * check and the CPU-baseline leg of bench.py call it; the product (the CUDA
+ * library and its Python host layer) never links, loads or calls it.
+ *
+ * Parity is pinned: the reference CPU path (python-bh, run unmodified under a
+ * numba stub) produced the golden vectors in tests/golden/ref_*.npz, and
+ * tests/test_oracle_golden.py checks this file against every one of them.
+ *
+ * Contents
+ *   1. oref_grid_dim      grid sizing      python-bh/barneshut/implementations/base.py:13,211-239,
+ *                                          python-bh/barneshut/kernels/helpers/grid.py:5-8
+ *   2. oref_bbox          square bbox      kernels/helpers/grid.py:10-26, base.py:233-239
+ *   3. oref_keys          box keys         implementations/sequential.py:32-34
+ *   4. oref_reference_evaluate
+ *                         the reference CPU evaluation, same loop and
+ *                         accumulation order:
+ *                           sort            implementations/sequential.py:37-52
+ *                           COM             internals/cloud.py:9-17,93-104
+ *                           com_concat_dedup kernels/grid_decomposition/sequential/evaluation.py:73-109
+ *                           neighbours      kernels/helpers/grid.py:28-48
+ *                           pair kernels    kernels/gravity/cpu_numba.py:30-92 (r^2 <= 1e-5 -> 0)
+ *   5. oref_tick          kick-drift tick  kernels/grid_decomposition/gpu/grid.py:159-174
+ *                         (the reference CPU tick never runs: grid_decomposition/box.py:26-30)
+ *   6. oref_direct        FP64 direct sum  implementations/base.py:16-32 (optionally softened)
+ *   7. oref_moments / oref_theta_evaluate
+ *                         FP64 restatement of this project's opening-angle
+ *                         (theta) far field.  It has no reference counterpart
+ *                         (the only related reference item is the unused
+ *                         `theta` key, configs/pykokkos.ini:11).  The cell
+ *                         acceptance test is evaluated in float exactly as the
+ *                         CUDA kernel evaluates it, so both sides build the same
+ *                         interaction lists; the pair arithmetic here is FP64.
+ *
+ * Build: gcc -O2 -fopenmp -ffp-contract=off -fPIC -shared (no FMA contraction:
+ * the reference is plain IEEE double arithmetic).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define REF_EPS 1e-5 /* cpu_numba.py:36,59,81 */
+
+/* ------------------------------------------------------------------ 1 -- */
+int oref_grid_dim(long long n, int ppb)
+{
+    /* base.py:223-231: nleaves = n / (0.7 * ppb) (or 1 when ppb == 1),
+     * next_perfect_square (helpers/grid.py:5-8), G = int(sqrt(nleaves)). */
+    double nleaves;
+    if (ppb == 1)
+        nleaves = 1.0;
+    else
+        nleaves = (double)n / (0.7 * (double)ppb);
+    double r = sqrt(nleaves);
+    if (fmod(nleaves, r) != 0.0 || r == 0.0) {
+        double c = ceil(r);
+        nleaves = c * c;
+    }
+    return (int)sqrt(nleaves);
+}
+
+/* ------------------------------------------------------------------ 2 -- */
+void oref_bbox(long long n, const double *x, const double *y, int G, double *out)
+{
+    /* out = {min_x, min_y, max_x, max_y, step} after squaring the box. */
+    double mnx = x[0], mny = y[0], mxx = x[0], mxy = y[0];
+    for (long long i = 1; i < n; i++) {
+        if (x[i] < mnx) mnx = x[i];
+        if (x[i] > mxx) mxx = x[i];
+        if (y[i] < mny) mny = y[i];
+        if (y[i] > mxy) mxy = y[i];
+    }
+    double xe = mxx - mnx, ye = mxy - mny;
+    if (xe > ye)
+        mxy += (xe - ye);
+    else if (ye > xe)
+        mxx += (ye - xe);
+    out[0] = mnx;
+    out[1] = mny;
+    out[2] = mxx;
+    out[3] = mxy;
+    out[4] = (mxx - mnx) / (double)G;
+}
+
+/* ------------------------------------------------------------------ 3 -- */
+static inline int ref_key1(double p, double mn, double step, int G)
+{
+    double k = floor((p - mn) / step);
+    if (k < 0.0) k = 0.0;
+    if (k > (double)(G - 1)) k = (double)(G - 1);
+    return (int)k;
+}
+
+void oref_keys(long long n, const double *x, const double *y, int G, const double *bb,
+               int *kx, int *ky)
+{
+    for (long long i = 0; i < n; i++) {
+        kx[i] = ref_key1(x[i], bb[0], bb[4], G);
+        ky[i] = ref_key1(y[i], bb[1], bb[4], G);
+    }
+}
+
+/* ------------------------------------------------------------------ 4 -- */
+typedef struct {
+    double gx, gy, px, py, m, vx, vy, ax, ay, pid;
+} rrec;
+
+static int cmp_rrec(const void *pa, const void *pb)
+{
+    /* numpy structured sort with order=[gx, gy]: ties are broken by the
+     * remaining fields in field order (px, py, mass, vx, vy, ax, ay, pid). */
+    const double *a = (const double *)pa, *b = (const double *)pb;
+    for (int k = 0; k < 10; k++) {
+        if (a[k] < b[k]) return -1;
+        if (a[k] > b[k]) return 1;
+    }
+    return 0;
+}
+
+static inline void ref_pair_fk(double dx0, double dx1, double G, double *f0, double *f1)
+{
+    /* cpu_numba.py: distSqr = 0.; distSqr += dx[k]**2; fk = G*dx[k]*distSqr**-1
+     * if distSqr > eps else 0 */
+    double d2 = 0.0;
+    d2 = d2 + dx0 * dx0;
+    d2 = d2 + dx1 * dx1;
+    if (d2 > REF_EPS) {
+        double inv = pow(d2, -1.0);
+        *f0 = (G * dx0) * inv;
+        *f1 = (G * dx1) * inv;
+    } else {
+        *f0 = 0.0;
+        *f1 = 0.0;
+    }
+}
+
+/*
+ * One reference evaluation.  Inputs in particle (pid) order.  Outputs:
+ * ax/ay (pid order), kx/ky (pid order), coms[G*G*3] (cx, cy, M; zeros for an
+ * empty box), bb[5] (see oref_bbox).  G <= 0 derives G from ppb.  Returns G.
+ */
+int oref_reference_evaluate(long long n, const double *x, const double *y, const double *m,
+                            const double *vx, const double *vy, int G, int ppb, double gconst,
+                            double *ax, double *ay, int *kx, int *ky, double *coms, double *bb)
+{
+    if (n <= 0) return 0;
+    if (G <= 0) G = oref_grid_dim(n, ppb);
+    oref_bbox(n, x, y, G, bb);
+    rrec *r = (rrec *)malloc(sizeof(rrec) * (size_t)n);
+    for (long long i = 0; i < n; i++) {
+        r[i].gx = (double)ref_key1(x[i], bb[0], bb[4], G);
+        r[i].gy = (double)ref_key1(y[i], bb[1], bb[4], G);
+        r[i].px = x[i];
+        r[i].py = y[i];
+        r[i].m = m[i];
+        r[i].vx = vx[i];
+        r[i].vy = vy[i];
+        r[i].ax = 0.0;
+        r[i].ay = 0.0;
+        r[i].pid = (double)i;
+    }
+    qsort(r, (size_t)n, sizeof(rrec), cmp_rrec);
+    long long B = (long long)G * G;
+    long long *start = (long long *)calloc((size_t)B + 1, sizeof(long long));
+    long long *cnt = (long long *)calloc((size_t)B, sizeof(long long));
+    for (long long i = 0; i < n; i++) cnt[(long long)r[i].gx * G + (long long)r[i].gy]++;
+    for (long long b = 0; b < B; b++) start[b + 1] = start[b] + cnt[b];
+    /* COMs: cloud.py:9-17 */
+    for (long long b = 0; b < B; b++) {
+        double M = 0.0, sx = 0.0, sy = 0.0;
+        if (cnt[b] == 0) {
+            coms[3 * b] = coms[3 * b + 1] = coms[3 * b + 2] = 0.0;
+            continue;
+        }
+        for (long long i = start[b]; i < start[b + 1]; i++) {
+            double mass = r[i].m;
+            sx += r[i].px * mass;
+            sy += r[i].py * mass;
+            M += mass;
+        }
+        coms[3 * b] = sx / M;
+        coms[3 * b + 1] = sy / M;
+        coms[3 * b + 2] = M;
+    }
+    long long maxc = 1;
+    for (long long b = 0; b < B; b++)
+        if (cnt[b] > maxc) maxc = cnt[b];
+    double *f1 = (double *)malloc(sizeof(double) * 2 * (size_t)(maxc > B ? maxc : B));
+    double *f2 = (double *)malloc(sizeof(double) * 2 * (size_t)maxc);
+    int *nb = (int *)malloc(sizeof(int) * 8 * 2);
+    long long *coml = (long long *)malloc(sizeof(long long) * (size_t)B);
+
+    for (int bx = 0; bx < G; bx++) {
+        for (int by = 0; by < G; by++) {
+            long long b = (long long)bx * G + by;
+            if (cnt[b] == 0) continue;
+            long long s0 = start[b], na = cnt[b];
+            /* get_neighbor_cells (helpers/grid.py:28-37) */
+            int xs = bx > 0 ? bx - 1 : bx, xe = bx < G - 1 ? bx + 1 : bx;
+            int ys = by > 0 ? by - 1 : by, ye = by < G - 1 ? by + 1 : by;
+            int nnb = 0;
+            for (int i = xs; i <= xe; i++)
+                for (int j = ys; j <= ye; j++)
+                    if (!(i == bx && j == by)) {
+                        nb[2 * nnb] = i;
+                        nb[2 * nnb + 1] = j;
+                        nnb++;
+                    }
+            /* COM list of every other non-empty, non-neighbour box */
+            long long ncom = 0;
+            for (int i = 0; i < G; i++)
+                for (int j = 0; j < G; j++) {
+                    long long c = (long long)i * G + j;
+                    if (cnt[c] == 0 || c == b) continue;
+                    int isnb = 0;
+                    for (int k = 0; k < nnb; k++)
+                        if (nb[2 * k] == i && nb[2 * k + 1] == j) isnb = 1;
+                    if (!isnb) coml[ncom++] = c;
+                }
+            if (ncom) {
+                /* self_other_numba_1 (cpu_numba.py:72-92) */
+                for (long long j = 0; j < na; j++) f1[2 * j] = f1[2 * j + 1] = 0.0;
+                for (long long ii = 0; ii < ncom; ii++) {
+                    const double *c = coms + 3 * coml[ii];
+                    for (long long j = 0; j < na; j++) {
+                        double fa, fb;
+                        ref_pair_fk(r[s0 + j].px - c[0], r[s0 + j].py - c[1], gconst, &fa, &fb);
+                        f1[2 * j] = f1[2 * j] - fa * c[2];
+                        f1[2 * j + 1] = f1[2 * j + 1] - fb * c[2];
+                    }
+                }
+                for (long long j = 0; j < na; j++) {
+                    r[s0 + j].ax = r[s0 + j].ax + f1[2 * j];
+                    r[s0 + j].ay = r[s0 + j].ay + f1[2 * j + 1];
+                }
+            }
+            /* remove_bottom_left_neighbors (helpers/grid.py:39-48), then the
+             * mutual update self_other_numba_2 (cpu_numba.py:49-70) */
+            for (int k = 0; k < nnb; k++) {
+                int i2 = nb[2 * k], j2 = nb[2 * k + 1];
+                if ((i2 == bx - 1 && j2 == by - 1) || (i2 == bx - 1 && j2 == by) ||
+                    (i2 == bx && j2 == by - 1) || (i2 == bx + 1 && j2 == by - 1))
+                    continue;
+                long long c = (long long)i2 * G + j2;
+                if (cnt[c] == 0) continue;
+                long long t0 = start[c], nbb = cnt[c];
+                for (long long j = 0; j < na; j++) f1[2 * j] = f1[2 * j + 1] = 0.0;
+                for (long long i = 0; i < nbb; i++) f2[2 * i] = f2[2 * i + 1] = 0.0;
+                for (long long i = 0; i < nbb; i++) {
+                    for (long long j = 0; j < na; j++) {
+                        double fa, fb;
+                        ref_pair_fk(r[s0 + j].px - r[t0 + i].px, r[s0 + j].py - r[t0 + i].py,
+                                    gconst, &fa, &fb);
+                        f1[2 * j] = f1[2 * j] - fa * r[t0 + i].m;
+                        f2[2 * i] = f2[2 * i] + fa * r[s0 + j].m;
+                        f1[2 * j + 1] = f1[2 * j + 1] - fb * r[t0 + i].m;
+                        f2[2 * i + 1] = f2[2 * i + 1] + fb * r[s0 + j].m;
+                    }
+                }
+                for (long long j = 0; j < na; j++) {
+                    r[s0 + j].ax = r[s0 + j].ax + f1[2 * j];
+                    r[s0 + j].ay = r[s0 + j].ay + f1[2 * j + 1];
+                }
+                for (long long i = 0; i < nbb; i++) {
+                    r[t0 + i].ax = r[t0 + i].ax + f2[2 * i];
+                    r[t0 + i].ay = r[t0 + i].ay + f2[2 * i + 1];
+                }
+            }
+            /* self_self_numba (cpu_numba.py:30-47) */
+            for (long long j = 0; j < na; j++) f1[2 * j] = f1[2 * j + 1] = 0.0;
+            for (long long i = 0; i < na; i++) {
+                for (long long j = i + 1; j < na; j++) {
+                    double fa, fb;
+                    ref_pair_fk(r[s0 + j].px - r[s0 + i].px, r[s0 + j].py - r[s0 + i].py, gconst,
+                                &fa, &fb);
+                    f1[2 * i] = f1[2 * i] + fa * r[s0 + j].m;
+                    f1[2 * j] = f1[2 * j] - fa * r[s0 + i].m;
+                    f1[2 * i + 1] = f1[2 * i + 1] + fb * r[s0 + j].m;
+                    f1[2 * j + 1] = f1[2 * j + 1] - fb * r[s0 + i].m;
+                }
+            }
+            for (long long j = 0; j < na; j++) {
+                r[s0 + j].ax = r[s0 + j].ax + f1[2 * j];
+                r[s0 + j].ay = r[s0 + j].ay + f1[2 * j + 1];
+            }
+        }
+    }
+    for (long long i = 0; i < n; i++) {
+        long long p = (long long)r[i].pid;
+        ax[p] = r[i].ax;
+        ay[p] = r[i].ay;
+        kx[p] = (int)r[i].gx;
+        ky[p] = (int)r[i].gy;
+    }
+    free(r);
+    free(start);
+    free(cnt);
+    free(f1);
+    free(f2);
+    free(nb);
+    free(coml);
+    return G;
+}
+
+/* ------------------------------------------------------------------ 5 -- */
+void oref_tick(long long n, double *x, double *y, double *vx, double *vy, const double *ax,
+               const double *ay, double dt)
+{
+    for (long long i = 0; i < n; i++) {
+        vx[i] = vx[i] + ax[i] * dt;
+        vy[i] = vy[i] + ay[i] * dt;
+        x[i] = x[i] + vx[i] * dt;
+        y[i] = y[i] + vy[i] * dt;
+    }
+}
+
+/* Multi-step reference run: per step evaluate + restated tick.  State is
+ * updated in place (pid order); ax/ay hold the last step's accelerations. */
+int oref_reference_run(long long n, double *x, double *y, const double *m, double *vx,
+                       double *vy, int G, int ppb, double gconst, double dt, int nsteps,
+                       double *ax, double *ay)
+{
+    int *kx = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int *ky = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int Gd = G > 0 ? G : oref_grid_dim(n, ppb);
+    double *coms = (double *)malloc(sizeof(double) * 3 * (size_t)Gd * (size_t)Gd);
+    double bb[5];
+    for (int s = 0; s < nsteps; s++) {
+        oref_reference_evaluate(n, x, y, m, vx, vy, Gd, ppb, gconst, ax, ay, kx, ky, coms, bb);
+        oref_tick(n, x, y, vx, vy, ax, ay, dt);
+    }
+    free(kx);
+    free(ky);
+    free(coms);
+    return Gd;
+}
+
+/* ------------------------------------------------------------------ 6 -- */
+/* a_t = G sum_{j != t, r^2 > cutoff} m_j (x_j - x_t) / (r^2 + eps2).  With
+ * cutoff < 0 only j == t is skipped (base.py:16-32, no cutoff). */
+void oref_direct(long long n, const double *x, const double *y, const double *m, double gconst,
+                 double eps2, double cutoff, long long nt, const long long *targets, double *ax,
+                 double *ay, int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+    for (long long k = 0; k < nt; k++) {
+        long long t = targets ? targets[k] : k;
+        double xt = x[t], yt = y[t], sx = 0.0, sy = 0.0;
+        for (long long j = 0; j < n; j++) {
+            if (j == t) continue;
+            double dx = x[j] - xt, dy = y[j] - yt;
+            double r2 = dx * dx + dy * dy;
+            if (cutoff >= 0.0 && !(r2 > cutoff)) continue;
+            double w = m[j] / (r2 + eps2);
+            sx += w * dx;
+            sy += w * dy;
+        }
+        ax[k] = gconst * sx;
+        ay[k] = gconst * sy;
+    }
+}
+
+/* Direct FP64 potential energy: sum_{i<j} G m_i m_j * 0.5*ln(r^2 + eps2). */
+double oref_potential(long long n, const double *x, const double *y, const double *m,
+                      double gconst, double eps2, int nthreads)
+{
+    double tot = 0.0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : tot)
+#endif
+    for (long long i = 0; i < n; i++) {
+        double s = 0.0;
+        for (long long j = i + 1; j < n; j++) {
+            double dx = x[j] - x[i], dy = y[j] - y[i];
+            s += m[j] * 0.5 * log(dx * dx + dy * dy + eps2);
+        }
+        tot += m[i] * s;
+    }
+    return gconst * tot;
+}
+
+/* ------------------------------------------------------------------ 7 -- */
+/*
+ * Cell pyramid.  Level 0 is the G x G leaf grid; level l has
+ * G_l = ceil(G_{l-1} / 2) cells per side; the top level has one cell.  Cell
+ * (l, i, j) covers leaves [i 2^l, (i+1) 2^l) x [j 2^l, (j+1) 2^l) clipped to
+ * the grid and has origin (min_x + (i 2^l) step, min_y + (j 2^l) step).
+ * Moments (FP64) are relative to the cell origin: M, Sx, Sy, Sxx, Sxy, Syy.
+ * Cells are stored level by level, column-major in i (index i*G_l + j).
+ */
+int oref_num_levels(int G)
+{
+    int L = 0, g = G;
+    while (g > 1) {
+        g = (g + 1) / 2;
+        L++;
+    }
+    return L + 1;
+}
+
+long long oref_pyramid_cells(int G)
+{
+    long long tot = 0;
+    int g = G;
+    for (;;) {
+        tot += (long long)g * g;
+        if (g == 1) break;
+        g = (g + 1) / 2;
+    }
+    return tot;
+}
+
+static void shift_moments(const double *c, double dx, double dy, double *p)
+{
+    double M = c[0], Sx = c[1], Sy = c[2];
+    p[0] += M;
+    p[1] += Sx + M * dx;
+    p[2] += Sy + M * dy;
+    p[3] += c[3] + 2.0 * dx * Sx + M * dx * dx;
+    p[4] += c[4] + dx * Sy + dy * Sx + M * dx * dy;
+    p[5] += c[5] + 2.0 * dy * Sy + M * dy * dy;
+}
+
+/*
+ * Leaf moments + pyramid.  kx/ky: box keys per particle (pid order), bb from
+ * oref_bbox.  mom: pyramid_cells*6 doubles.  rec: pyramid_cells*4 floats
+ * {cx_off, cy_off, M, 0} where cx_off = (float)(Sx/M) is the centre of mass
+ * relative to the cell origin (zeros for an empty cell).
+ */
+void oref_moments(long long n, const double *x, const double *y, const double *m, int G,
+                  const double *bb, const int *kx, const int *ky, double *mom, float *rec)
+{
+    long long ncell = oref_pyramid_cells(G);
+    memset(mom, 0, sizeof(double) * 6 * (size_t)ncell);
+    double step = bb[4];
+    for (long long i = 0; i < n; i++) {
+        long long b = (long long)kx[i] * G + ky[i];
+        double ox = bb[0] + (double)kx[i] * step, oy = bb[1] + (double)ky[i] * step;
+        double dx = x[i] - ox, dy = y[i] - oy, mm = m[i];
+        double *q = mom + 6 * b;
+        q[0] += mm;
+        q[1] += mm * dx;
+        q[2] += mm * dy;
+        q[3] += mm * dx * dx;
+        q[4] += mm * dx * dy;
+        q[5] += mm * dy * dy;
+    }
+    long long off = 0, poff;
+    int g = G, l = 0;
+    while (g > 1) {
+        int gp = (g + 1) / 2;
+        poff = off + (long long)g * g;
+        for (int i = 0; i < gp; i++)
+            for (int j = 0; j < gp; j++) {
+                double *p = mom + 6 * (poff + (long long)i * gp + j);
+                for (int a = 0; a < 2; a++)
+                    for (int c = 0; c < 2; c++) {
+                        int ci = 2 * i + a, cj = 2 * j + c;
+                        if (ci >= g || cj >= g) continue;
+                        double dxs = (double)(a << l) * step, dys = (double)(c << l) * step;
+                        shift_moments(mom + 6 * (off + (long long)ci * g + cj), dxs, dys, p);
+                    }
+            }
+        off = poff;
+        g = gp;
+        l++;
+    }
+    for (long long c = 0; c < ncell; c++) {
+        double *q = mom + 6 * c;
+        if (q[0] > 0.0) {
+            rec[4 * c] = (float)(q[1] / q[0]);
+            rec[4 * c + 1] = (float)(q[2] / q[0]);
+            rec[4 * c + 2] = (float)q[0];
+        } else {
+            rec[4 * c] = rec[4 * c + 1] = rec[4 * c + 2] = 0.0f;
+        }
+        rec[4 * c + 3] = 0.0f;
+    }
+}
+
+/*
+ * Opening-angle evaluation, FP64 pair arithmetic.  Target groups are TG x TG
+ * leaf boxes (TG a power of two).  For every group the pyramid is walked from
+ * the top; a non-empty cell that does not overlap the group is accepted as a
+ * monopole when (2^l step)^2 < theta^2 d^2, d the distance from the group's
+ * square [0, TG step]^2 to the cell's centre of mass; the test is evaluated
+ * in float with the same operation order as the CUDA kernel.  Rejected leaf
+ * boxes are summed particle by particle.  theta <= 0 selects the flat mode of
+ * the reference (TG must be 1): the 3x3 neighbourhood directly, every other
+ * non-empty leaf box as a monopole.  Pairs whose unsoftened r^2 <= cutoff are
+ * skipped (cutoff = 1e-5 reproduces cpu_numba.py; 0 skips coincident points).
+ * Output ax/ay in pid order.  counts[0..1] = near / far pair interactions.
+ */
+int oref_theta_evaluate(long long n, const double *x, const double *y, const double *m, int G,
+                        int TG, double theta, double eps2, double cutoff, double gconst,
+                        double *ax, double *ay, long long *counts, int nthreads)
+{
+    if (n <= 0) return 0;
+    double bb[5];
+    oref_bbox(n, x, y, G, bb);
+    int *kx = (int *)malloc(sizeof(int) * (size_t)n), *ky = (int *)malloc(sizeof(int) * (size_t)n);
+    oref_keys(n, x, y, G, bb, kx, ky);
+    long long B = (long long)G * G, ncell = oref_pyramid_cells(G);
+    int L = oref_num_levels(G);
+    double *mom = (double *)malloc(sizeof(double) * 6 * (size_t)ncell);
+    float *rec = (float *)malloc(sizeof(float) * 4 * (size_t)ncell);
+    oref_moments(n, x, y, m, G, bb, kx, ky, mom, rec);
+    long long *lvoff = (long long *)malloc(sizeof(long long) * (size_t)(L + 1));
+    int *lvg = (int *)malloc(sizeof(int) * (size_t)(L + 1));
+    {
+        long long off = 0;
+        int g = G;
+        for (int l = 0; l < L; l++) {
+            lvoff[l] = off;
+            lvg[l] = g;
+            off += (long long)g * g;
+            g = (g + 1) / 2;
+        }
+    }
+    /* particles grouped by box (pid lists) */
+    long long *bstart = (long long *)calloc((size_t)B + 1, sizeof(long long));
+    long long *order = (long long *)malloc(sizeof(long long) * (size_t)n);
+    for (long long i = 0; i < n; i++) bstart[(long long)kx[i] * G + ky[i] + 1]++;
+    for (long long b = 0; b < B; b++) bstart[b + 1] += bstart[b];
+    {
+        long long *cur = (long long *)malloc(sizeof(long long) * (size_t)B);
+        memcpy(cur, bstart, sizeof(long long) * (size_t)B);
+        for (long long i = 0; i < n; i++) order[cur[(long long)kx[i] * G + ky[i]]++] = i;
+        free(cur);
+    }
+    const float step_f = (float)bb[4];
+    const float theta2_f = (float)(theta * theta);
+    const int flat = theta <= 0.0;
+    if (flat) TG = 1;
+    const int NGs = (G + TG - 1) / TG;
+    const float W_f = (float)TG * step_f;
+    long long cnt_near = 0, cnt_far = 0;
+
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : cnt_near, cnt_far)
+#endif
+    for (long long gidx = 0; gidx < (long long)NGs * NGs; gidx++) {
+        int gi = (int)(gidx / NGs), gj = (int)(gidx % NGs);
+        int gx0 = gi * TG, gy0 = gj * TG;
+        int gx1 = gx0 + TG < G ? gx0 + TG : G, gy1 = gy0 + TG < G ? gy0 + TG : G;
+        long long nt = 0;
+        for (int bx = gx0; bx < gx1; bx++) nt += bstart[(long long)bx * G + gy1] - bstart[(long long)bx * G + gy0];
+        if (nt == 0) continue;
+        /* interaction lists: far cells (level, index) and near leaf boxes */
+        long long cap = 4 * ncell + 16;
+        long long *far = (long long *)malloc(sizeof(long long) * (size_t)cap);
+        long long *near = (long long *)malloc(sizeof(long long) * (size_t)B);
+        long long nfar = 0, nnear = 0;
+        if (flat) {
+            for (int i = 0; i < G; i++)
+                for (int j = 0; j < G; j++) {
+                    long long c = (long long)i * G + j;
+                    if (bstart[c + 1] == bstart[c]) continue;
+                    if (abs(i - gx0) <= 1 && abs(j - gy0) <= 1)
+                        near[nnear++] = c;
+                    else
+                        far[nfar++] = c;
+                }
+        } else {
+            long long *fr = (long long *)malloc(sizeof(long long) * (size_t)cap);
+            long long *nx = (long long *)malloc(sizeof(long long) * (size_t)cap);
+            long long nfr = 1, nnx;
+            fr[0] = 0; /* the single top cell, index within its level */
+            for (int l = L - 1; l >= 0; l--) {
+                nnx = 0;
+                int gl = lvg[l];
+                for (long long q = 0; q < nfr; q++) {
+                    long long ci_ = fr[q];
+                    int ci = (int)(ci_ / gl), cj = (int)(ci_ % gl);
+                    long long cell = lvoff[l] + ci_;
+                    if (!(mom[6 * cell] > 0.0)) continue;
+                    int lo_x = ci << l, hi_x = (ci + 1) << l, lo_y = cj << l, hi_y = (cj + 1) << l;
+                    int overlap = lo_x < gx1 && hi_x > gx0 && lo_y < gy1 && hi_y > gy0;
+                    int accept = 0;
+                    if (!overlap) {
+                        float rx = (float)(lo_x - gx0) * step_f + rec[4 * cell];
+                        float ry = (float)(lo_y - gy0) * step_f + rec[4 * cell + 1];
+                        float dxo = fmaxf(0.0f, fmaxf(-rx, rx - W_f));
+                        float dyo = fmaxf(0.0f, fmaxf(-ry, ry - W_f));
+                        float d2 = dxo * dxo + dyo * dyo;
+                        float s_f = ldexpf(step_f, l);
+                        accept = (s_f * s_f) < (theta2_f * d2);
+                    }
+                    if (accept) {
+                        far[nfar++] = cell;
+                    } else if (l == 0) {
+                        near[nnear++] = ci_;
+                    } else {
+                        int gc = lvg[l - 1];
+                        for (int a = 0; a < 2; a++)
+                            for (int c = 0; c < 2; c++) {
+                                int ch_i = 2 * ci + a, ch_j = 2 * cj + c;
+                                if (ch_i < gc && ch_j < gc) nx[nnx++] = (long long)ch_i * gc + ch_j;
+                            }
+                    }
+                }
+                long long *t = fr;
+                fr = nx;
+                nx = t;
+                nfr = nnx;
+            }
+            free(fr);
+            free(nx);
+        }
+        long long nsrc = 0;
+        for (long long q = 0; q < nnear; q++) nsrc += bstart[near[q] + 1] - bstart[near[q]];
+        cnt_near += nt * nsrc;
+        cnt_far += nt * nfar;
+        for (int bx = gx0; bx < gx1; bx++) {
+            for (long long k = bstart[(long long)bx * G + gy0]; k < bstart[(long long)bx * G + gy1]; k++) {
+                long long t = order[k];
+                double xt = x[t], yt = y[t], sx = 0.0, sy = 0.0;
+                for (long long q = 0; q < nnear; q++)
+                    for (long long kk = bstart[near[q]]; kk < bstart[near[q] + 1]; kk++) {
+                        long long j = order[kk];
+                        double dx = x[j] - xt, dy = y[j] - yt;
+                        double r2 = dx * dx + dy * dy;
+                        if (!(r2 > cutoff)) continue;
+                        double w = m[j] / (r2 + eps2);
+                        sx += w * dx;
+                        sy += w * dy;
+                    }
+                for (long long q = 0; q < nfar; q++) {
+                    long long cell = far[q];
+                    int l = 0;
+                    while (l + 1 < L && lvoff[l + 1] <= cell) l++;
+                    long long ci_ = cell - lvoff[l];
+                    int ci = (int)(ci_ / lvg[l]), cj = (int)(ci_ % lvg[l]);
+                    const double *qm = mom + 6 * cell;
+                    double cx = (bb[0] + (double)(ci << l) * bb[4]) + qm[1] / qm[0];
+                    double cy = (bb[1] + (double)(cj << l) * bb[4]) + qm[2] / qm[0];
+                    double dx = cx - xt, dy = cy - yt;
+                    double r2 = dx * dx + dy * dy;
+                    if (!(r2 > cutoff)) continue;
+                    double w = qm[0] / (r2 + eps2);
+                    sx += w * dx;
+                    sy += w * dy;
+                }
+                ax[t] = gconst * sx;
+                ay[t] = gconst * sy;
+            }
+        }
+        free(far);
+        free(near);
+    }
+    if (counts) {
+        counts[0] = cnt_near;
+        counts[1] = cnt_far;
+    }
+    free(kx);
+    free(ky);
+    free(mom);
+    free(rec);
+    free(lvoff);
+    free(lvg);
+    free(bstart);
+    free(order);
+    return G;
+}

@@ -1,0 +1,99 @@
+"""The C-ABI library: loads, exports every declared symbol, validates
+arguments on the host (no GPU needed for any of this)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    syms = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            txt = open(os.path.join(inc, f)).read()
+            syms |= set(re.findall(r"^\s*(?:int|const char \*|void)\s*\*?\s*(bh_\w+)\s*\(", txt, re.M))
+    return syms
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from barneshut.gb300 import native
+
+    return native.load_library()
+
+
+def test_every_declared_symbol_exported(lib):
+    from barneshut.gb300 import native
+
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in sorted(syms):
+        assert hasattr(lib, s), f"{s} declared in include/ but not exported"
+    assert syms <= set(native.EXPORTS)
+
+
+def test_grid_dim_matches_reference_formula(lib):
+    from barneshut.implementations.base import reference_grid_dim
+
+    for n in (2, 33, 600, 1000, 10_000, 1 << 20, 10_000_000):
+        for ppb in (1, 2, 4, 23, 60, 1000):
+            assert lib.bh_grid_dim(n, ppb) == reference_grid_dim(n, ppb), (n, ppb)
+    assert lib.bh_grid_dim(10_000, 60) == 16
+    assert lib.bh_grid_dim(10_000_000, 1000) == 120  # python-bh/data/frontera runs: 120 x 120
+
+
+def _create(lib, n, G, **kw):
+    from barneshut.gb300 import native
+
+    prm = native.make_params(**kw)
+    h = ctypes.c_void_p()
+    na = (ctypes.c_longlong * len(n))(*n)
+    ga = (ctypes.c_int * len(G))(*G)
+    rc = lib.bh_plan_create(ctypes.byref(h), len(n), na, ga, ctypes.byref(prm))
+    return rc, h
+
+
+def test_plan_create_validates_on_host(lib):
+    from barneshut.gb300 import native
+
+    rc, h = _create(lib, [100], [4], softening=-1.0)
+    assert rc == native.BH_ERR_INVALID and not h.value
+    assert b"softening" in lib.bh_last_error(None)
+    rc, h = _create(lib, [100], [4], group_dim=3)
+    assert rc == native.BH_ERR_INVALID
+    rc, h = _create(lib, [-5], [4])
+    assert rc == native.BH_ERR_INVALID
+    rc, h = _create(lib, [100], [40000])
+    assert rc == native.BH_ERR_INVALID
+    rc, h = _create(lib, [100], [4], precision=7)
+    assert rc == native.BH_ERR_INVALID
+
+
+def test_workspace_size_and_unbound_calls(lib):
+    from barneshut.gb300 import native
+
+    rc, h = _create(lib, [1000, 50], [8, 2], theta=0.5, softening=1e-3, cutoff_r2=0.0)
+    assert rc == 0
+    sz = ctypes.c_size_t()
+    assert lib.bh_workspace_size(h, ctypes.byref(sz)) == 0
+    # two FP64 state buffers dominate: >= 2 * 5 * 8 bytes per particle
+    assert sz.value >= 1050 * 80
+    # phases before bh_bind fail cleanly with a workspace error (no CUDA call)
+    assert lib.bh_create_tree(h, None) == native.BH_ERR_WORKSPACE
+    assert b"bh_bind" in lib.bh_last_error(h)
+    assert lib.bh_step(h, 1, None) == native.BH_ERR_WORKSPACE
+    # too-small workspace is refused before any device access
+    assert lib.bh_bind(h, ctypes.c_void_p(256), 16, None) == native.BH_ERR_WORKSPACE
+    assert lib.bh_plan_destroy(h) == 0
+
+
+def test_missing_library_fails_loudly(monkeypatch):
+    from barneshut.gb300 import native
+
+    monkeypatch.setattr(native, "_lib", None)
+    with pytest.raises(native.NativeLibraryError):
+        native.load_library("/nonexistent/libbh_gb300.so")

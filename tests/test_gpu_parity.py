@@ -1,0 +1,303 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the
+reference's own outputs (golden vectors).
+
+Tolerances:
+  * box keys, per-box particle sets: bit-exact;
+  * flat-mode accelerations vs the reference CPU path: relative RMS <= 1e-5
+    (FP32 pair arithmetic, Kahan far field);
+  * positions after the stated steps vs the reference: max |dx| <= 1e-9
+    (unit box; dt = 1e-4, 10 steps);
+  * theta-mode accelerations vs the FP64 oracle with identical interaction
+    lists: relative RMS <= 1e-5 (FP32), 1e-10 (FP64 pairs); pair counts exact.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_cases
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def native():
+    from barneshut.gb300 import native as n
+
+    return n
+
+
+def make_plan(n, G, **kw):
+    N = native()
+    prm = N.make_params(**kw)
+    return N.Plan([n] if np.isscalar(n) else n, [G] if np.isscalar(G) else G, prm)
+
+
+def golden(name):
+    return np.load(f"{GOLDEN}/ref_{name}.npz")
+
+
+REF_KW = dict(grav_constant=1.0, tick_seconds=1e-4, softening=0.0, cutoff_r2=1e-5, theta=0.0)
+
+
+# ------------------------------------------------------------------ placement
+@pytest.mark.parametrize("name", golden_cases())
+def test_create_tree_keys_bit_exact(name):
+    z = golden(name)
+    G = int(z["s0_grid_dim"])
+    n = len(z["x0"])
+    plan = make_plan(n, G, **REF_KW)
+    plan.load(z["x0"], z["y0"], z["m"], z["vx0"], z["vy0"])
+    plan.create_tree()
+    rec = plan.store_records().cpu().numpy()
+    np.testing.assert_array_equal(rec[:, 7].astype(np.int32), z["s0_gx"])
+    np.testing.assert_array_equal(rec[:, 8].astype(np.int32), z["s0_gy"])
+    np.testing.assert_array_equal(rec[:, 9], np.arange(n))
+    info = plan.grid_info()
+    assert info["min_x"] == z["s0_min_xy"][0] and info["min_y"] == z["s0_min_xy"][1]
+    assert info["step"] == z["s0_step"]
+    assert plan.error_flags() == 0
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_summarize_coms(name):
+    z = golden(name)
+    G = int(z["s0_grid_dim"])
+    plan = make_plan(len(z["x0"]), G, **REF_KW)
+    plan.load(z["x0"], z["y0"], z["m"], z["vx0"], z["vy0"])
+    plan.create_tree()
+    plan.summarize()
+    c = plan.box_moments().cpu().numpy()
+    ref = z["s0_coms"]
+    np.testing.assert_array_equal(c[..., 2] > 0, ref[..., 2] > 0)
+    np.testing.assert_allclose(c[..., 2], ref[..., 2], rtol=1e-6)
+    # centres of mass: FP32 per-particle products, FP64 accumulation
+    step = float(z["s0_step"])
+    assert np.max(np.abs(c[..., :2] - ref[..., :2])) <= 1e-6 * step
+
+
+# ---------------------------------------------------------------- evaluation
+@pytest.mark.parametrize("name", golden_cases())
+def test_flat_forces_vs_reference(name):
+    z = golden(name)
+    G = int(z["s0_grid_dim"])
+    plan = make_plan(len(z["x0"]), G, **dict(REF_KW, grav_constant=float(z["gconst"])))
+    plan.load(z["x0"], z["y0"], z["m"], z["vx0"], z["vy0"])
+    plan.create_tree()
+    plan.summarize()
+    plan.evaluate()
+    out = plan.store()
+    ax, ay = out["ax"].cpu().numpy(), out["ay"].cpu().numpy()
+    from oracle import oracle
+
+    err = oracle.rel_rms(ax, ay, z["s0_ax"], z["s0_ay"])
+    assert err <= 1e-5, err
+
+
+def test_c1_ten_steps_positions():
+    """C1: 10 fused steps (create_tree, summarize, evaluate + tick) vs the
+    reference driven with the restated tick."""
+    z = golden("c1_uniform10k")
+    G = int(z["s0_grid_dim"])
+    plan = make_plan(len(z["x0"]), G, **REF_KW)
+    plan.load(z["x0"], z["y0"], z["m"], z["vx0"], z["vy0"])
+    plan.step(int(z["nsteps"]))
+    out = plan.store()
+    from oracle import oracle
+
+    dx = np.max(np.abs(out["x"].cpu().numpy() - z["final_x"]))
+    dy = np.max(np.abs(out["y"].cpu().numpy() - z["final_y"]))
+    assert max(dx, dy) <= 1e-9, (dx, dy)
+    err = oracle.rel_rms(out["ax"].cpu().numpy(), out["ay"].cpu().numpy(), z["s9_ax"], z["s9_ay"])
+    assert err <= 1e-5, err
+
+
+def test_unfused_phases_equal_fused():
+    from barneshut.gb300 import workloads
+
+    x, y, m, vx, vy = workloads.uniform(3000, seed=21)
+    a = make_plan(3000, 8, **REF_KW)
+    b = make_plan(3000, 8, **REF_KW)
+    a.load(x, y, m, vx, vy)
+    b.load(x, y, m, vx, vy)
+    for _ in range(3):
+        a.create_tree()
+        a.summarize()
+        a.evaluate()
+        a.timestep()
+    b.step(3)
+    oa, ob = a.store(), b.store()
+    for k in ("x", "y", "vx", "vy"):
+        np.testing.assert_allclose(oa[k].cpu().numpy(), ob[k].cpu().numpy(), rtol=1e-12, atol=1e-14)
+
+
+# ---------------------------------------------------------------- theta mode
+@pytest.mark.parametrize("theta,TG,G", [(0.3, 1, 16), (0.5, 2, 16), (0.5, 4, 19), (0.8, 2, 32)])
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_theta_vs_fp64_oracle(theta, TG, G, prec):
+    from barneshut.gb300 import workloads
+    from oracle import oracle
+
+    x, y, m, vx, vy = workloads.cluster_mixture(20000, seed=31)
+    eps = 1e-3
+    plan = make_plan(20000, G, grav_constant=1.0, tick_seconds=1e-5, softening=eps, cutoff_r2=0.0,
+                     theta=theta, group_dim=TG, precision=prec)
+    plan.load(x, y, m, vx, vy)
+    plan.create_tree()
+    plan.summarize()
+    plan.evaluate()
+    out = plan.store()
+    nn, nf = plan.pair_counts()
+    ax, ay, on, of = oracle.theta_evaluate(x, y, m, G, TG=TG, theta=theta, eps2=eps * eps, cutoff=0.0)
+    assert (nn, nf) == (on, of), "interaction lists differ from the oracle's"
+    err = oracle.rel_rms(out["ax"].cpu().numpy(), out["ay"].cpu().numpy(), ax, ay)
+    assert err <= (1e-10 if prec == 2 else 1e-5), err
+    assert plan.error_flags() == 0
+
+
+def test_theta_error_vs_direct_sum():
+    from barneshut.gb300 import workloads
+    from oracle import oracle
+
+    x, y, m, vx, vy = workloads.cluster_mixture(30000, seed=32)
+    plan = make_plan(30000, 32, grav_constant=1.0, softening=1e-3, cutoff_r2=0.0, theta=0.5)
+    plan.load(x, y, m, vx, vy)
+    plan.create_tree()
+    plan.summarize()
+    plan.evaluate()
+    out = plan.store()
+    t = np.arange(0, 30000, 7)
+    dax, day = oracle.direct(x, y, m, eps2=1e-6, cutoff=0.0, targets=t)
+    err = oracle.rel_rms(out["ax"].cpu().numpy()[t], out["ay"].cpu().numpy()[t], dax, day)
+    assert err < 5e-3, err
+
+
+# ---------------------------------------------------------------- edge cases
+@pytest.mark.parametrize("n", [1, 2, 33])
+def test_tiny_systems(n):
+    from barneshut.gb300 import workloads
+    from oracle import oracle
+
+    x, y, m, vx, vy = workloads.uniform(n, seed=40 + n)
+    plan = make_plan(n, 4 if n > 2 else 1, **REF_KW)
+    plan.load(x, y, m, vx, vy)
+    plan.create_tree()
+    plan.summarize()
+    plan.evaluate()
+    out = plan.store()
+    if n == 1:
+        assert out["ax"].item() == 0.0 and out["ay"].item() == 0.0
+    else:
+        r = oracle.reference_evaluate(x, y, m, G=4 if n > 2 else 1, gconst=1.0)
+        assert oracle.rel_rms(out["ax"].cpu().numpy(), out["ay"].cpu().numpy(), r["ax"], r["ay"]) < 1e-5
+    assert plan.error_flags() == 0
+
+
+def test_all_coincident_points():
+    n = 64
+    x = np.full(n, 0.25)
+    y = np.full(n, 0.75)
+    m = np.ones(n)
+    z = np.zeros(n)
+    plan = make_plan(n, 4, **REF_KW)
+    plan.load(x, y, m, z, z)
+    plan.step(2)
+    out = plan.store()
+    assert np.all(out["ax"].cpu().numpy() == 0.0)
+    np.testing.assert_array_equal(out["x"].cpu().numpy(), x)
+    assert plan.error_flags() == 0
+
+
+def test_nan_position_raises_flag():
+    from barneshut.gb300 import workloads
+
+    N = native()
+    x, y, m, vx, vy = workloads.uniform(1000, seed=50)
+    x[17] = np.nan
+    plan = make_plan(1000, 4, **REF_KW)
+    plan.load(x, y, m, vx, vy)
+    plan.create_tree()
+    flags = plan.error_flags(raise_on_error=False)
+    assert flags & N.BH_DEV_NAN_POSITION
+    assert plan.error_flags(raise_on_error=False) == 0  # cleared
+
+
+# ---------------------------------------------------------------- batching / graphs
+def test_batched_equals_separate():
+    from barneshut.gb300 import workloads
+
+    systems = [workloads.uniform(1500, seed=60), workloads.cluster_mixture(5000, seed=61),
+               workloads.uniform(700, seed=62)]
+    grids = [5, 9, 3]
+    kw = dict(grav_constant=1.0, tick_seconds=1e-5, softening=1e-3, cutoff_r2=0.0, theta=0.5,
+              group_dim=2)
+    plan = make_plan([len(s[0]) for s in systems], grids, **kw)
+    cat = [np.concatenate([s[k] for s in systems]) for k in range(5)]
+    plan.load(*cat)
+    plan.step(3)
+    allout = plan.store()
+    off = 0
+    for s, G in zip(systems, grids):
+        p1 = make_plan(len(s[0]), G, **kw)
+        p1.load(*s)
+        p1.step(3)
+        o1 = p1.store()
+        n = len(s[0])
+        for k in ("x", "y", "vx", "vy"):
+            np.testing.assert_allclose(allout[k][off:off + n].cpu().numpy(), o1[k].cpu().numpy(),
+                                       rtol=1e-9, atol=1e-12)
+        off += n
+
+
+def test_graph_replay_equals_eager():
+    from barneshut.gb300 import workloads
+
+    x, y, m, vx, vy = workloads.cluster_mixture(8000, seed=70)
+    kw = dict(grav_constant=1.0, tick_seconds=1e-5, softening=1e-3, cutoff_r2=0.0, theta=0.5)
+    a = make_plan(8000, 16, **kw)
+    b = make_plan(8000, 16, **kw)
+    a.load(x, y, m, vx, vy)
+    b.load(x, y, m, vx, vy)
+    a.step(4)
+    b.step_graph(2)
+    b.step_graph(2)
+    oa, ob = a.store(), b.store()
+    for k in ("x", "y", "vx", "vy"):
+        np.testing.assert_allclose(oa[k].cpu().numpy(), ob[k].cpu().numpy(), rtol=1e-9, atol=1e-12)
+
+
+# ---------------------------------------------------------------- samplers
+def test_direct_sample_matches_oracle():
+    from barneshut.gb300 import workloads
+    from oracle import oracle
+
+    x, y, m, vx, vy = workloads.uniform(4000, seed=80)
+    plan = make_plan(4000, 8, grav_constant=2.0, softening=1e-3, cutoff_r2=0.0, theta=0.5)
+    plan.load(x, y, m, vx, vy)
+    plan.step(1)  # state is box-sorted now; the sampler must map pids
+    st = plan.store()
+    xs, ys = st["x"].cpu().numpy(), st["y"].cpu().numpy()
+    t = np.array([0, 5, 999, 3999])
+    ax, ay = plan.direct_sample(t)
+    rax, ray = oracle.direct(xs, ys, m, gconst=2.0, eps2=1e-6, cutoff=-1.0, targets=t)
+    np.testing.assert_allclose(ax.cpu().numpy(), rax, rtol=1e-10)
+    np.testing.assert_allclose(ay.cpu().numpy(), ray, rtol=1e-10)
+
+
+def test_diagnostics_energy_momentum():
+    from barneshut.gb300 import workloads
+    from oracle import oracle
+
+    x, y, m, vx, vy = workloads.gen_input(1500, "normal", seed=3)
+    plan = make_plan(1500, 8, grav_constant=1.0, softening=1e-2, cutoff_r2=0.0, theta=0.5)
+    plan.load(x, y, m, vx, vy)
+    ke, px, py, pe = plan.diagnostics(potential=True)
+    assert abs(ke - 0.5 * np.sum(m * (vx ** 2 + vy ** 2))) < 1e-10 * ke
+    assert abs(px - np.sum(m * vx)) < 1e-9 * np.sum(np.abs(m * vx))
+    ref_pe = oracle.potential(x, y, m, 1.0, 1e-4)
+    assert abs(pe - ref_pe) < 1e-9 * abs(ref_pe)
