@@ -36,6 +36,7 @@ EXPORTS = (
     "bh_bind", "bh_load", "bh_load_records", "bh_store_records", "bh_store", "bh_create_tree",
     "bh_summarize", "bh_evaluate", "bh_timestep", "bh_step", "bh_step_graph", "bh_error_flags",
     "bh_pair_counts", "bh_box_moments", "bh_grid_info", "bh_direct_sample", "bh_diagnostics",
+    "bh_kernels_per_step",
 )
 
 
@@ -105,6 +106,7 @@ def load_library(path=None):
     L.bh_grid_info.argtypes = [vp, i, ctypes.POINTER(d), vp]
     L.bh_direct_sample.argtypes = [vp, i, vp, ll, vp, vp, vp]
     L.bh_diagnostics.argtypes = [vp, i, i, vp, vp]
+    L.bh_kernels_per_step.argtypes = [vp, pi]
     for name in EXPORTS:
         f = getattr(L, name)
         if name not in ("bh_last_error", "bh_grid_dim"):
@@ -257,6 +259,11 @@ class Plan:
         if raise_on_error and f.value:
             raise BHError(BH_ERR_DEVICE, f"device error flags 0x{f.value:x}")
         return f.value
+
+    def kernels_per_step(self):
+        c = ctypes.c_int()
+        self._check(self.L.bh_kernels_per_step(self.h, ctypes.byref(c)))
+        return c.value
 
     def pair_counts(self):
         a, b = ctypes.c_longlong(), ctypes.c_longlong()

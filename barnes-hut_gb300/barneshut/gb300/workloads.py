@@ -80,6 +80,24 @@ def gen_input(n, distribution="normal", seed=None, domain=500.0):
     return x, y, m, vx, vy
 
 
+def box_order(x, y, G):
+    """Permutation that sorts particles by box key (gx * G + gy) of the square
+    bounding-box grid, stable within a box (the order of the state between
+    steps of a running simulation)."""
+    mnx, mny, mxx, mxy = float(x.min()), float(y.min()), float(x.max()), float(y.max())
+    xe, ye = mxx - mnx, mxy - mny
+    if xe > ye:
+        mxy += xe - ye
+    elif ye > xe:
+        mxx += ye - xe
+    step = (mxx - mnx) / G
+    if not step > 0:
+        return np.arange(len(x))
+    kx = np.clip(np.floor((x - mnx) / step), 0, G - 1).astype(np.int64)
+    ky = np.clip(np.floor((y - mny) / step), 0, G - 1).astype(np.int64)
+    return np.argsort(kx * G + ky, kind="stable")
+
+
 def precision_subsample(n, k=16384, seed=2):
     """Seeded target subsample for force-error measurements."""
     rng = np.random.default_rng(seed + 1000)

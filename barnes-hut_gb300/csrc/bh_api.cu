@@ -28,7 +28,7 @@ struct bh_plan {
     size_t ws_bytes = 0;
     size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
-    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_tiles, o_mom, o_rec,
+    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_tiles, o_icnt, o_ioff, o_igrp, o_mom, o_rec,
         o_rec2;
     void *ws = nullptr;
     int device = -1;
@@ -140,13 +140,13 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
         if (!flat) {
             // children of cells rejected at level l+1 (edge s >= 2 boxes): a rejected cell
             // intersects the group widened by s/theta, so at most (TG/2 + 2/theta + 2)^2 of
-            // them, four children each.  Keep that within the kernel's frontier (1024).
+            // them, four children each.  Keep that within the kernel's frontier.
             double bound = 4.0 * std::pow(TG / 2.0 + 2.0 / pr.theta + 2.0, 2.0);
-            while (bound > 1024.0 && TG > 1) {
+            while (bound > (double)FRONTIER_CAP && TG > 1) {
                 TG /= 2;
                 bound = 4.0 * std::pow(TG / 2.0 + 2.0 / pr.theta + 2.0, 2.0);
             }
-            if (bound > 1024.0) return bad("theta too small for the traversal frontier (theta >= 0.15)");
+            if (bound > (double)FRONTIER_CAP) return bad("theta too small for the traversal frontier (theta >= 0.25)");
         }
         d.TG = TG;
         d.NGs = (G + TG - 1) / TG;
@@ -205,6 +205,9 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_counts = take(4 * B);
     p->o_bstart = take(4 * (B + 1));
     p->o_tiles = take(4 * (B / 4096 + 2));
+    p->o_icnt = take(4 * (size_t)p->NG_total);
+    p->o_ioff = take(4 * ((size_t)p->NG_total + 1));
+    p->o_igrp = take(4 * ((size_t)p->NG_total + N / TARGET_CHUNK + 1));
     p->o_mom = take(48 * C);
     p->o_rec = take(16 * C);
     p->o_rec2 = take(16 * C);
@@ -265,6 +268,9 @@ static void fill_dev(bh_plan *p) {
     d.counts = (int *)(w + p->o_counts);
     d.box_start = (int *)(w + p->o_bstart);
     d.tile_sums = (int *)(w + p->o_tiles);
+    d.item_cnt = (int *)(w + p->o_icnt);
+    d.item_off = (int *)(w + p->o_ioff);
+    d.item_group = (int *)(w + p->o_igrp);
     d.mom = (double *)(w + p->o_mom);
     d.rec = (float4 *)(w + p->o_rec);
     d.rec2 = (float4 *)(w + p->o_rec2);
@@ -362,6 +368,7 @@ static int enqueue_tree(bh_plan *p, cudaStream_t st) {
     CK(p, launch_place(p->dev, st), "place");
     CK(p, launch_scan(p->dev, st), "scan");
     CK(p, launch_scatter(p->dev, st), "scatter");
+    CK(p, launch_items(p->dev, st), "work items");
     return BH_OK;
 }
 
@@ -449,6 +456,15 @@ extern "C" int bh_step_graph(bh_plan *p, int nsteps, void *stream) {
     CK(p, cudaGraphLaunch(p->gexec, st), "graph launch");
     p->has_tree = true;
     p->acc_stale = true;
+    return BH_OK;
+}
+
+extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
+    if (!p || !count) return BH_ERR_INVALID;
+    // prologue, 3 box-scan phases, work items (count, 3 scan phases, fill),
+    // pyramid levels 1..Lmax-1, records; with particles also bbox, place,
+    // scatter, leaf moments, force
+    *count = 1 + 3 + 5 + (p->Lmax - 1) + 1 + (p->n_total > 0 ? 5 : 0);
     return BH_OK;
 }
 

@@ -7,12 +7,15 @@
 // kernels/gravity/cpu_numba.py:30-92) in flat mode, and this project's opening-angle rule in
 // theta mode.
 //
-// One CTA per target group (TG x TG leaf boxes).  The CTA walks the cell pyramid level by level
-// (all threads test one frontier cell each; accepted cells, rejected leaves and children are
+// Work decomposition: a target group is TG x TG leaf boxes; its nt targets are split into work
+// items of at most TARGET_CHUNK targets (built after the box scan), which CTAs pull from a device
+// queue, so dense groups spread over many SMs.  Per item the CTA walks the cell pyramid level by
+// level (every thread tests one frontier cell; accepted cells, rejected leaves and children are
 // compacted with a block scan, so list order is deterministic), stages far entries (centre of
-// mass in the group frame, mass) and near-box particles (float4, shifted into the group frame)
-// in shared memory, and every thread accumulates one target particle over a slice of the staged
-// entries.  Lists that outgrow shared memory are evaluated and emptied on the fly.
+// mass in the group frame, mass) and near-box particles (float4 shifted into the group frame) in
+// shared memory, and evaluates them: each thread owns R targets in registers and sweeps a slice of
+// the staged entries (one shared-memory load feeds R pair interactions).  Lists that outgrow
+// shared memory are evaluated and emptied on the fly; slice partials are reduced in shared memory.
 //
 // Pair arithmetic: a += m_j (x_j - x_t) * rcp(r^2 + eps^2) in FP32 (rcp.approx), far-field
 // contributions Kahan-compensated when requested; BH_PREC_FP64 runs the same lists in FP64.
@@ -21,11 +24,11 @@
 
 namespace bh {
 
-constexpr int FT = 128;        // threads per CTA
-constexpr int FAR_CAP = 1024;  // far entries per flush
+constexpr int FT = FORCE_THREADS;
+constexpr int FAR_CAP = 512;   // far entries per flush
 constexpr int NEAR_CAP = 256;  // near boxes per flush
-constexpr int SRC_CAP = 1024;  // near sources per staging pass
-constexpr int FR_CAP = 1024;   // traversal frontier (cells per level)
+constexpr int SRC_CAP = 512;   // near sources per staging pass
+constexpr int FR_CAP = FRONTIER_CAP;
 constexpr int MAX_TG = 8;
 
 template <typename R> struct Src;
@@ -45,11 +48,13 @@ template <> __device__ __forceinline__ double rinv<double>(double x) { return 1.
 __device__ __forceinline__ void src_get(const float4 &e, float &x, float &y, float &m, int &idx) {
     x = e.x; y = e.y; m = e.z; idx = __float_as_int(e.w);
 }
-__device__ __forceinline__ void src_get(const Src<double>::T &e, double &x, double &y, double &m, int &idx) {
+__device__ __forceinline__ void src_get(const Src<double>::T &e, double &x, double &y, double &m,
+                                        int &idx) {
     x = e.x; y = e.y; m = e.m; idx = e.idx;
 }
 
-__device__ __forceinline__ int block_scan_packed(int v, int *sh, int *total) {
+// Exclusive block scan of one int per thread; *total = block sum.
+__device__ __forceinline__ int block_scan(int v, int *sh, int *total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int x = v;
 #pragma unroll
@@ -59,57 +64,52 @@ __device__ __forceinline__ int block_scan_packed(int v, int *sh, int *total) {
     }
     if (lane == 31) sh[w] = x;
     __syncthreads();
-    int pre = x - v;
-    for (int k = 0; k < w; k++) pre += sh[k];
-    int tot = 0;
-    for (int k = 0; k < nw; k++) tot += sh[k];
+    int pre = x - v, tot = 0;
+    for (int k = 0; k < nw; k++) {
+        int s = sh[k];
+        if (k < w) pre += s;
+        tot += s;
+    }
     *total = tot;
     __syncthreads();
     return pre;
 }
 
-template <typename R> struct Acc {
-    R nx, ny, fx, fy, cx, cy;
-};
-
-template <typename R, bool KAHAN>
-__device__ __forceinline__ void far_add(Acc<R> &a, R tx, R ty) {
-    if (KAHAN) {
-        R yx = tx - a.cx, t = a.fx + yx;
-        a.cx = (t - a.fx) - yx;
-        a.fx = t;
-        R yy = ty - a.cy, u = a.fy + yy;
-        a.cy = (u - a.fy) - yy;
-        a.fy = u;
-    } else {
-        a.fx += tx;
-        a.fy += ty;
-    }
-}
-
-template <typename R, bool KAHAN, bool TEST, bool EXACT>
-__global__ void __launch_bounds__(FT) k_force(DevPlan d, int tick, int accumulate) {
+template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT>
+__global__ void __launch_bounds__(FT, (sizeof(R) == 4 ? 8 : 4))
+k_force(DevPlan d, int tick, int accumulate) {
     using S = typename Src<R>::T;
     extern __shared__ __align__(16) unsigned char smem[];
-    S *far = reinterpret_cast<S *>(smem);                       // FAR_CAP
-    S *src = far + FAR_CAP;                                     // SRC_CAP
-    R *red = reinterpret_cast<R *>(src + SRC_CAP);              // 4 x FT
-    float2 *nshift = reinterpret_cast<float2 *>(red + 4 * FT);  // NEAR_CAP
-    int *nbox = reinterpret_cast<int *>(nshift + NEAR_CAP);     // NEAR_CAP (first particle)
-    int *ncnt = nbox + NEAR_CAP;                                // NEAR_CAP
-    int *npre = ncnt + NEAR_CAP;                                // NEAR_CAP + 1
-    int *front0 = npre + NEAR_CAP + 4;                          // FR_CAP
-    int *front1 = front0 + FR_CAP;                              // FR_CAP
+    S *far = reinterpret_cast<S *>(smem);                     // FAR_CAP
+    S *src = far + FAR_CAP;                                   // SRC_CAP
+    R *red = reinterpret_cast<R *>(smem);                     // aliases far/src at the end
+    float2 *nshift = reinterpret_cast<float2 *>(src + SRC_CAP);  // NEAR_CAP
+    int *nbox = reinterpret_cast<int *>(nshift + NEAR_CAP);   // first particle of near box
+    int *ncnt = nbox + NEAR_CAP;
+    int *npre = ncnt + NEAR_CAP;                              // NEAR_CAP + 4
+    int *front0 = npre + NEAR_CAP + 4;                        // FR_CAP
+    int *front1 = front0 + FR_CAP;                            // FR_CAP
     __shared__ int sh_scan[32];
-    __shared__ int s_nfar, s_nnear, s_nnext, s_ovf;
+    __shared__ int s_item, s_nfar, s_nnear, s_nnext, s_ovf;
     __shared__ int s_col0[MAX_TG + 1], s_colpre[MAX_TG + 1];
     __shared__ unsigned long long s_npairs, s_fpairs;
 
     const int tid = threadIdx.x;
     const int nxt = (d.glob->epoch + 1) & 1;
     const double *Xs = d.X[nxt], *Ys = d.Y[nxt], *Ms = d.M[nxt];
+    const long long nitems = d.item_off[d.NG_total];
 
-    for (long long g = blockIdx.x; g < d.NG_total; g += gridDim.x) {
+    for (;;) {
+        if (tid == 0) {
+            s_item = (int)atomicAdd(&d.glob->item_next, 1u);
+            s_npairs = 0;
+            s_fpairs = 0;
+        }
+        __syncthreads();
+        const int item = s_item;
+        if (item >= nitems) break;
+        const long long g = d.item_group[item];
+        const int chunk = item - d.item_off[g];
         const int s = find_seg(d.goff_tab, d.nsys, g);
         const SysDesc &sd = d.sys[s];
         const SysDyn &dy = d.dyn[s];
@@ -129,129 +129,147 @@ __global__ void __launch_bounds__(FT) k_force(DevPlan d, int tick, int accumulat
         if (tid == 0) {
             s_colpre[0] = 0;
             for (int c = 1; c <= ncol; c++) s_colpre[c] += s_colpre[c - 1];
-            s_npairs = 0;
-            s_fpairs = 0;
+            s_nfar = 0;
+            s_nnear = 0;
+            s_ovf = 0;
         }
         __syncthreads();
         const int nt = s_colpre[ncol];
-        if (nt == 0) {
-            __syncthreads();
-            continue;
-        }
+        const int c0 = chunk * TARGET_CHUNK;
+        const int T = min(TARGET_CHUNK, nt - c0);
         const float step_f = __double2float_rn(dy.step);
         const float W_f = __fmul_rn((float)TG, step_f);
         const double gox = box_origin(dy.minx, gx0, dy.step), goy = box_origin(dy.miny, gy0, dy.step);
         const R eps2 = (R)(sizeof(R) == 4 ? (double)d.eps2_f : d.eps2);
         const R cut = (R)(sizeof(R) == 4 ? (double)d.cut_f : d.cutoff);
 
-        for (int c0 = 0; c0 < nt; c0 += FT) {
-            const int ntc = min(FT, nt - c0);
-            const int nslice = FT / ntc;
-            const bool active = tid < nslice * ntc;
-            const int tl = active ? tid % ntc : 0, slice = active ? tid / ntc : 0;
-            // target
-            int ti = 0;
-            R tx = 0, ty = 0;
-            double txd = 0, tyd = 0;
-            {
-                int u = c0 + tl, c = 0;
-                while (c + 1 < ncol && s_colpre[c + 1] <= u) c++;
-                ti = s_col0[c] + (u - s_colpre[c]);
-                if (sizeof(R) == 4) {
-                    float4 p = d.P[ti];
-                    int lb = d.skey[ti] - (int)sd.boff;
-                    int kx = lb / G, ky = lb - kx * G;
-                    tx = (R)__fadd_rn(__fmul_rn((float)(kx - gx0), step_f), p.x);
-                    ty = (R)__fadd_rn(__fmul_rn((float)(ky - gy0), step_f), p.y);
-                } else {
-                    tx = (R)(Xs[ti] - gox);
-                    ty = (R)(Ys[ti] - goy);
-                }
-                if (EXACT) {
-                    txd = Xs[ti];
-                    tyd = Ys[ti];
-                }
+        // ---- thread -> (slice, R targets)
+        const int nthr = (T + NR - 1) / NR;
+        const int nslice = FT / nthr;
+        const bool active = tid < nslice * nthr;
+        const int slice = active ? tid / nthr : 0, tl = active ? tid % nthr : 0;
+        int ti[NR];
+        R tx[NR], ty[NR];
+        double txd[NR], tyd[NR];
+        bool tv[NR];
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            int v = tl * NR + r;
+            tv[r] = v < T;
+            int u = c0 + (tv[r] ? v : 0), c = 0;
+            while (c + 1 < ncol && s_colpre[c + 1] <= u) c++;
+            ti[r] = s_col0[c] + (u - s_colpre[c]);
+            if (sizeof(R) == 4) {
+                float4 p = d.P[ti[r]];
+                int lb = d.skey[ti[r]] - (int)sd.boff;
+                int kx = lb / G, ky = lb - kx * G;
+                tx[r] = (R)__fadd_rn(__fmul_rn((float)(kx - gx0), step_f), p.x);
+                ty[r] = (R)__fadd_rn(__fmul_rn((float)(ky - gy0), step_f), p.y);
+            } else {
+                tx[r] = (R)(Xs[ti[r]] - gox);
+                ty[r] = (R)(Ys[ti[r]] - goy);
             }
-            Acc<R> acc = {0, 0, 0, 0, 0, 0};
+            txd[r] = EXACT ? Xs[ti[r]] : 0.0;
+            tyd[r] = EXACT ? Ys[ti[r]] : 0.0;
+        }
+        R anx[NR], any_[NR], afx[NR], afy[NR], acx[NR], acy[NR];
+#pragma unroll
+        for (int r = 0; r < NR; r++) anx[r] = any_[r] = afx[r] = afy[r] = acx[r] = acy[r] = 0;
 
-            auto flush_far = [&]() {
-                __syncthreads();
-                const int nf = s_nfar;
-                if (active) {
-                    for (int k = slice; k < nf; k += nslice) {
-                        R sx, sy, sm;
-                        int sidx;
-                        src_get(far[k], sx, sy, sm, sidx);
-                        R dx = sx - tx, dyy = sy - ty;
+        auto flush_far = [&]() {
+            __syncthreads();
+            const int nf = s_nfar;
+            if (active) {
+                for (int k = slice; k < nf; k += nslice) {
+                    R sx, sy, sm;
+                    int sidx;
+                    src_get(far[k], sx, sy, sm, sidx);
+#pragma unroll
+                    for (int r = 0; r < NR; r++) {
+                        R dx = sx - tx[r], dyy = sy - ty[r];
                         R r2 = dx * dx + dyy * dyy;
                         R inv = rinv<R>(r2 + eps2);
                         if (TEST && !(r2 > cut)) inv = 0;
                         R w = sm * inv;
-                        far_add<R, KAHAN>(acc, w * dx, w * dyy);
-                    }
-                }
-                if (tid == 0) s_fpairs += (unsigned long long)ntc * nf;
-                __syncthreads();
-                if (tid == 0) s_nfar = 0;
-                __syncthreads();
-            };
-
-            auto flush_near = [&]() {
-                __syncthreads();
-                const int nn = s_nnear;
-                {
-                    constexpr int IT = NEAR_CAP / FT;
-                    int v[IT], sum = 0;
-#pragma unroll
-                    for (int k = 0; k < IT; k++) {
-                        int e = tid * IT + k;
-                        v[k] = e < nn ? ncnt[e] : 0;
-                        sum += v[k];
-                    }
-                    int tot;
-                    int pre = block_scan_packed(sum, sh_scan, &tot);
-#pragma unroll
-                    for (int k = 0; k < IT; k++) {
-                        int e = tid * IT + k;
-                        if (e < nn) npre[e] = pre;
-                        pre += v[k];
-                    }
-                    if (tid == 0) npre[nn] = tot;
-                }
-                __syncthreads();
-                const int total = npre[nn];
-                for (int s0 = 0; s0 < total; s0 += SRC_CAP) {
-                    const int ns = min(SRC_CAP, total - s0);
-                    for (int j = tid; j < ns; j += FT) {
-                        int J = s0 + j;
-                        int lo = 0, hi = nn;  // npre[lo] <= J < npre[hi]
-                        while (hi - lo > 1) {
-                            int mid = (lo + hi) >> 1;
-                            if (npre[mid] <= J) lo = mid; else hi = mid;
-                        }
-                        int idx = nbox[lo] + (J - npre[lo]);
-                        if (sizeof(R) == 4) {
-                            float4 p = d.P[idx];
-                            float2 sh = nshift[lo];
-                            float4 q = make_float4(__fadd_rn(sh.x, p.x), __fadd_rn(sh.y, p.y), p.z, p.w);
-                            reinterpret_cast<float4 *>(src)[j] = q;
+                        R fx = w * dx, fy = w * dyy;
+                        if (KAHAN) {
+                            R yx = fx - acx[r], t1 = afx[r] + yx;
+                            acx[r] = (t1 - afx[r]) - yx;
+                            afx[r] = t1;
+                            R yy = fy - acy[r], t2 = afy[r] + yy;
+                            acy[r] = (t2 - afy[r]) - yy;
+                            afy[r] = t2;
                         } else {
-                            typename Src<double>::T q;
-                            q.x = Xs[idx] - gox;
-                            q.y = Ys[idx] - goy;
-                            q.m = Ms[idx];
-                            q.idx = idx;
-                            q.pad = 0;
-                            reinterpret_cast<typename Src<double>::T *>(src)[j] = q;
+                            afx[r] += fx;
+                            afy[r] += fy;
                         }
                     }
-                    __syncthreads();
-                    if (active) {
-                        for (int j = slice; j < ns; j += nslice) {
-                            R sx, sy, sm;
-                            int sidx;
-                            src_get(src[j], sx, sy, sm, sidx);
-                            R dx = sx - tx, dyy = sy - ty;
+                }
+            }
+            if (tid == 0) s_fpairs += (unsigned long long)T * nf;
+            __syncthreads();
+            if (tid == 0) s_nfar = 0;
+            __syncthreads();
+        };
+
+        auto flush_near = [&]() {
+            __syncthreads();
+            const int nn = s_nnear;
+            {
+                constexpr int IT = NEAR_CAP / FT;
+                int v[IT], sum = 0;
+#pragma unroll
+                for (int k = 0; k < IT; k++) {
+                    int e = tid * IT + k;
+                    v[k] = e < nn ? ncnt[e] : 0;
+                    sum += v[k];
+                }
+                int tot;
+                int pre = block_scan(sum, sh_scan, &tot);
+#pragma unroll
+                for (int k = 0; k < IT; k++) {
+                    int e = tid * IT + k;
+                    if (e < nn) npre[e] = pre;
+                    pre += v[k];
+                }
+                if (tid == 0) npre[nn] = tot;
+            }
+            __syncthreads();
+            const int total = npre[nn];
+            for (int s0 = 0; s0 < total; s0 += SRC_CAP) {
+                const int ns = min(SRC_CAP, total - s0);
+                for (int j = tid; j < ns; j += FT) {
+                    int J = s0 + j;
+                    int lo = 0, hi = nn;  // npre[lo] <= J < npre[hi]
+                    while (hi - lo > 1) {
+                        int mid = (lo + hi) >> 1;
+                        if (npre[mid] <= J) lo = mid; else hi = mid;
+                    }
+                    int idx = nbox[lo] + (J - npre[lo]);
+                    if (sizeof(R) == 4) {
+                        float4 p = d.P[idx];
+                        float2 sh = nshift[lo];
+                        reinterpret_cast<float4 *>(src)[j] =
+                            make_float4(__fadd_rn(sh.x, p.x), __fadd_rn(sh.y, p.y), p.z, p.w);
+                    } else {
+                        typename Src<double>::T q;
+                        q.x = Xs[idx] - gox;
+                        q.y = Ys[idx] - goy;
+                        q.m = Ms[idx];
+                        q.idx = idx;
+                        q.pad = 0;
+                        reinterpret_cast<typename Src<double>::T *>(src)[j] = q;
+                    }
+                }
+                __syncthreads();
+                if (active) {
+                    for (int j = slice; j < ns; j += nslice) {
+                        R sx, sy, sm;
+                        int sidx;
+                        src_get(src[j], sx, sy, sm, sidx);
+#pragma unroll
+                        for (int r = 0; r < NR; r++) {
+                            R dx = sx - tx[r], dyy = sy - ty[r];
                             R r2 = dx * dx + dyy * dyy;
                             R inv = rinv<R>(r2 + eps2);
                             if (TEST) {
@@ -260,7 +278,8 @@ __global__ void __launch_bounds__(FT) k_force(DevPlan d, int tick, int accumulat
                                     R band = cut * (R)1e-3;
                                     R diff = r2 - cut;
                                     if (diff <= band && diff >= -band) {
-                                        double ex = __dsub_rn(txd, Xs[sidx]), ey = __dsub_rn(tyd, Ys[sidx]);
+                                        double ex = __dsub_rn(txd[r], Xs[sidx]);
+                                        double ey = __dsub_rn(tyd[r], Ys[sidx]);
                                         double e2 = __dmul_rn(ex, ex);
                                         e2 = __dadd_rn(e2, __dmul_rn(ey, ey));
                                         keep = e2 > d.cutoff;
@@ -269,204 +288,199 @@ __global__ void __launch_bounds__(FT) k_force(DevPlan d, int tick, int accumulat
                                 if (!keep) inv = 0;
                             }
                             R w = sm * inv;
-                            acc.nx += w * dx;
-                            acc.ny += w * dyy;
+                            anx[r] += w * dx;
+                            any_[r] += w * dyy;
                         }
                     }
-                    if (tid == 0) s_npairs += (unsigned long long)ntc * ns;
-                    __syncthreads();
                 }
-                if (tid == 0) s_nnear = 0;
+                if (tid == 0) s_npairs += (unsigned long long)T * ns;
                 __syncthreads();
-            };
-
-            // append helper state
-            if (tid == 0) {
-                s_nfar = 0;
-                s_nnear = 0;
-                s_ovf = 0;
             }
+            if (tid == 0) s_nnear = 0;
             __syncthreads();
+        };
 
-            auto emit = [&](int kind, int cell_or_box, int l, int ci, int cj, float rx, float ry,
-                            float M, int *front_next, int gc) {
-                // kind: 0 none, 1 far, 2 near, 3 open
-                int nch = 0;
-                if (kind == 3) {
+        // kind: 0 none, 1 far, 2 near, 3 open (children into front_next)
+        auto emit = [&](int kind, int id, int l, int ci, int cj, float rx, float ry, float M,
+                        int *front_next, int gc) {
+            int nch = 0;
+            if (kind == 3) {
+                nch = (2 * ci + 1 < gc ? 2 : 1) * (2 * cj + 1 < gc ? 2 : 1);
+            }
+            int packed = (kind == 1 ? 1 : 0) | ((kind == 2 ? 1 : 0) << 10) | (nch << 20);
+            int tot;
+            int pre = block_scan(packed, sh_scan, &tot);
+            if (kind == 1) {
+                int pos = s_nfar + (pre & 1023);
+                if (sizeof(R) == 4) {
+                    reinterpret_cast<float4 *>(far)[pos] = make_float4(rx, ry, M, __int_as_float(id));
+                } else {
+                    const double *q = d.mom + 6 * (long long)id;
+                    typename Src<double>::T e;
+                    double ox = box_origin(dy.minx, ci << l, dy.step) - gox;
+                    double oy = box_origin(dy.miny, cj << l, dy.step) - goy;
+                    e.x = ox + q[1] / q[0];
+                    e.y = oy + q[2] / q[0];
+                    e.m = q[0];
+                    e.idx = id;
+                    e.pad = 0;
+                    reinterpret_cast<typename Src<double>::T *>(far)[pos] = e;
+                }
+            } else if (kind == 2) {
+                int pos = s_nnear + ((pre >> 10) & 1023);
+                int st = d.box_start[id];
+                nbox[pos] = st;
+                ncnt[pos] = d.box_start[id + 1] - st;
+                int lb = id - (int)sd.boff;
+                int kx = lb / G, ky = lb - kx * G;
+                nshift[pos] = make_float2(__fmul_rn((float)(kx - gx0), step_f),
+                                          __fmul_rn((float)(ky - gy0), step_f));
+            } else if (kind == 3) {
+                int pos = s_nnext + (pre >> 20);
+                if (pos + nch > FR_CAP) {
+                    s_ovf = 1;
+                } else {
                     for (int a = 0; a < 2; a++)
                         for (int b = 0; b < 2; b++)
-                            if (2 * ci + a < gc && 2 * cj + b < gc) nch++;
+                            if (2 * ci + a < gc && 2 * cj + b < gc)
+                                front_next[pos++] = (2 * ci + a) * gc + (2 * cj + b);
                 }
-                int packed = (kind == 1 ? 1 : 0) | ((kind == 2 ? 1 : 0) << 10) | (nch << 20);
-                int tot;
-                int pre = block_scan_packed(packed, sh_scan, &tot);
-                if (kind == 1) {
-                    int pos = s_nfar + (pre & 1023);
-                    if (sizeof(R) == 4) {
-                        reinterpret_cast<float4 *>(far)[pos] = make_float4(rx, ry, M, __int_as_float(cell_or_box));
-                    } else {
-                        // FP64 centre of mass in the group frame from the FP64 moments
-                        const double *q = d.mom + 6 * (long long)cell_or_box;
-                        typename Src<double>::T e;
-                        double ox = box_origin(dy.minx, ci << l, dy.step) - gox;
-                        double oy = box_origin(dy.miny, cj << l, dy.step) - goy;
-                        e.x = ox + q[1] / q[0];
-                        e.y = oy + q[2] / q[0];
-                        e.m = q[0];
-                        e.idx = cell_or_box;
-                        e.pad = 0;
-                        reinterpret_cast<typename Src<double>::T *>(far)[pos] = e;
-                    }
-                } else if (kind == 2) {
-                    int pos = s_nnear + ((pre >> 10) & 1023);
-                    int st = d.box_start[cell_or_box];
-                    nbox[pos] = st;
-                    ncnt[pos] = d.box_start[cell_or_box + 1] - st;
-                    int lb = cell_or_box - (int)sd.boff;
-                    int kx = lb / G, ky = lb - kx * G;
-                    nshift[pos] = make_float2(__fmul_rn((float)(kx - gx0), step_f),
-                                              __fmul_rn((float)(ky - gy0), step_f));
-                } else if (kind == 3) {
-                    int pos = s_nnext + (pre >> 20);
-                    if (pos + nch > FR_CAP) {
-                        s_ovf = 1;
-                    } else {
-                        for (int a = 0; a < 2; a++)
-                            for (int b = 0; b < 2; b++)
-                                if (2 * ci + a < gc && 2 * cj + b < gc)
-                                    front_next[pos++] = (2 * ci + a) * gc + (2 * cj + b);
-                    }
-                }
-                __syncthreads();
-                if (tid == 0) {
-                    s_nfar += tot & 1023;
-                    s_nnear += (tot >> 10) & 1023;
-                    s_nnext += tot >> 20;
-                }
-                __syncthreads();
-            };
+            }
+            __syncthreads();
+            if (tid == 0) {
+                s_nfar += tot & 1023;
+                s_nnear += (tot >> 10) & 1023;
+                s_nnext += tot >> 20;
+            }
+            __syncthreads();
+        };
 
-            if (d.flat) {
-                const long long B = (long long)G * G;
-                for (long long q0 = 0; q0 < B; q0 += FT) {
+        if (d.flat) {
+            const long long B = (long long)G * G;
+            for (long long q0 = 0; q0 < B; q0 += FT) {
+                if (s_nfar + FT > FAR_CAP) flush_far();
+                if (s_nnear + FT > NEAR_CAP) flush_near();
+                long long b = q0 + tid;
+                int kind = 0, bx = 0, byy = 0, id = 0;
+                float rx = 0, ry = 0, M = 0;
+                if (b < B) {
+                    bx = (int)(b / G);
+                    byy = (int)(b - (long long)bx * G);
+                    long long gb = sd.boff + b;
+                    if (d.box_start[gb + 1] > d.box_start[gb]) {
+                        if (abs(bx - gx0) <= 1 && abs(byy - gy0) <= 1) {
+                            kind = 2;
+                            id = (int)gb;
+                        } else {
+                            float4 rr = d.rec[sd.coff + b];
+                            rx = __fadd_rn(__fmul_rn((float)(bx - gx0), step_f), rr.x);
+                            ry = __fadd_rn(__fmul_rn((float)(byy - gy0), step_f), rr.y);
+                            M = rr.z;
+                            kind = 1;
+                            id = (int)(sd.coff + b);
+                        }
+                    }
+                }
+                emit(kind, id, 0, bx, byy, rx, ry, M, front1, 0);
+            }
+        } else {
+            int *fr = front0, *fn = front1;
+            if (tid == 0) fr[0] = 0;
+            int nfr = 1;
+            const float theta2 = d.theta2_f;
+            for (int l = sd.L - 1; l >= 0; l--) {
+                const int gl = sd.lvg[l];
+                const int gc = l > 0 ? sd.lvg[l - 1] : 0;
+                if (tid == 0) s_nnext = 0;
+                __syncthreads();
+                for (int q0 = 0; q0 < nfr; q0 += FT) {
                     if (s_nfar + FT > FAR_CAP) flush_far();
                     if (s_nnear + FT > NEAR_CAP) flush_near();
-                    long long b = q0 + tid;
-                    int kind = 0, bx = 0, byy = 0;
+                    int q = q0 + tid;
+                    int kind = 0, ci = 0, cj = 0, id = 0;
                     float rx = 0, ry = 0, M = 0;
-                    if (b < B) {
-                        bx = (int)(b / G);
-                        byy = (int)(b - (long long)bx * G);
-                        long long gb = sd.boff + b;
-                        if (d.box_start[gb + 1] > d.box_start[gb]) {
-                            if (abs(bx - gx0) <= 1 && abs(byy - gy0) <= 1) {
-                                kind = 2;
-                            } else {
-                                float4 r = d.rec[sd.coff + b];
-                                rx = __fadd_rn(__fmul_rn((float)(bx - gx0), step_f), r.x);
-                                ry = __fadd_rn(__fmul_rn((float)(byy - gy0), step_f), r.y);
-                                M = r.z;
+                    if (q < nfr) {
+                        int loc = fr[q];
+                        ci = loc / gl;
+                        cj = loc - ci * gl;
+                        long long cell = sd.coff + sd.lvoff[l] + loc;
+                        float4 rr = d.rec[cell];
+                        if (rr.z > 0.f) {
+                            int lo_x = ci << l, hi_x = (ci + 1) << l;
+                            int lo_y = cj << l, hi_y = (cj + 1) << l;
+                            bool overlap = lo_x < gx1 && hi_x > gx0 && lo_y < gy1 && hi_y > gy0;
+                            bool accept = false;
+                            if (!overlap) {
+                                rx = __fadd_rn(__fmul_rn((float)(lo_x - gx0), step_f), rr.x);
+                                ry = __fadd_rn(__fmul_rn((float)(lo_y - gy0), step_f), rr.y);
+                                float dxo = fmaxf(0.f, fmaxf(-rx, __fsub_rn(rx, W_f)));
+                                float dyo = fmaxf(0.f, fmaxf(-ry, __fsub_rn(ry, W_f)));
+                                float d2 = __fadd_rn(__fmul_rn(dxo, dxo), __fmul_rn(dyo, dyo));
+                                float s_f = ldexpf(step_f, l);
+                                accept = __fmul_rn(s_f, s_f) < __fmul_rn(theta2, d2);
+                            }
+                            M = rr.z;
+                            if (accept) {
                                 kind = 1;
+                                id = (int)cell;
+                            } else if (l == 0) {
+                                kind = 2;
+                                id = (int)(sd.boff + loc);
+                            } else {
+                                kind = 3;
                             }
                         }
                     }
-                    int id = kind == 2 ? (int)(sd.boff + b) : (int)(sd.coff + b);
-                    emit(kind, id, 0, bx, byy, rx, ry, M, front1, 0);
+                    emit(kind, id, l, ci, cj, rx, ry, M, fn, gc);
                 }
-            } else {
-                int *fr = front0, *fn = front1;
-                if (tid == 0) fr[0] = 0;
-                int nfr = 1;
-                const float theta2 = d.theta2_f;
-                for (int l = sd.L - 1; l >= 0; l--) {
-                    const int gl = sd.lvg[l];
-                    const int gc = l > 0 ? sd.lvg[l - 1] : 0;
-                    if (tid == 0) s_nnext = 0;
-                    __syncthreads();
-                    for (int q0 = 0; q0 < nfr; q0 += FT) {
-                        if (s_nfar + FT > FAR_CAP) flush_far();
-                        if (s_nnear + FT > NEAR_CAP) flush_near();
-                        int q = q0 + tid;
-                        int kind = 0, ci = 0, cj = 0, id = 0;
-                        float rx = 0, ry = 0, M = 0;
-                        if (q < nfr) {
-                            int loc = fr[q];
-                            ci = loc / gl;
-                            cj = loc - ci * gl;
-                            long long cell = sd.coff + sd.lvoff[l] + loc;
-                            float4 r = d.rec[cell];
-                            if (r.z > 0.f) {
-                                int lo_x = ci << l, hi_x = (ci + 1) << l;
-                                int lo_y = cj << l, hi_y = (cj + 1) << l;
-                                bool overlap = lo_x < gx1 && hi_x > gx0 && lo_y < gy1 && hi_y > gy0;
-                                bool accept = false;
-                                if (!overlap) {
-                                    rx = __fadd_rn(__fmul_rn((float)(lo_x - gx0), step_f), r.x);
-                                    ry = __fadd_rn(__fmul_rn((float)(lo_y - gy0), step_f), r.y);
-                                    float dxo = fmaxf(0.f, fmaxf(-rx, __fsub_rn(rx, W_f)));
-                                    float dyo = fmaxf(0.f, fmaxf(-ry, __fsub_rn(ry, W_f)));
-                                    float d2 = __fadd_rn(__fmul_rn(dxo, dxo), __fmul_rn(dyo, dyo));
-                                    float s_f = ldexpf(step_f, l);
-                                    accept = __fmul_rn(s_f, s_f) < __fmul_rn(theta2, d2);
-                                }
-                                M = r.z;
-                                if (accept) {
-                                    kind = 1;
-                                    id = (int)cell;
-                                } else if (l == 0) {
-                                    kind = 2;
-                                    id = (int)(sd.boff + loc);
-                                } else {
-                                    kind = 3;
-                                }
-                            }
-                        }
-                        emit(kind, id, l, ci, cj, rx, ry, M, fn, gc);
-                    }
-                    int *t = fr;
-                    fr = fn;
-                    fn = t;
-                    // an overflowed frontier may hold unwritten slots: abandon the walk
-                    // (flagged; the host bounds theta and group size so this cannot happen)
-                    nfr = s_ovf ? 0 : min(s_nnext, FR_CAP);
-                    if (s_ovf && tid == 0) raise_err(d.glob, 2u /*BH_DEV_LIST_OVERFLOW*/);
-                }
+                int *t = fr;
+                fr = fn;
+                fn = t;
+                // an overflowed frontier may hold unwritten slots: abandon the walk
+                // (flagged; the host bounds theta and group size so this cannot happen)
+                nfr = s_ovf ? 0 : min(s_nnext, FR_CAP);
+                if (s_ovf && tid == 0) raise_err(d.glob, 2u /*BH_DEV_LIST_OVERFLOW*/);
             }
-            flush_far();
-            flush_near();
+        }
+        flush_far();
+        flush_near();
 
-            // reduce slices and write
-            R farx = acc.fx - acc.cx, fary = acc.fy - acc.cy;
-            if (active) {
-                red[4 * tid + 0] = acc.nx;
-                red[4 * tid + 1] = acc.ny;
-                red[4 * tid + 2] = farx;
-                red[4 * tid + 3] = fary;
+        // ---- reduce slice partials (red aliases the staging buffers) and write
+        if (active) {
+#pragma unroll
+            for (int r = 0; r < NR; r++) {
+                R *o = red + 2 * ((slice * nthr + tl) * NR + r);
+                o[0] = anx[r] + (afx[r] - acx[r]);
+                o[1] = any_[r] + (afy[r] - acy[r]);
             }
-            __syncthreads();
-            if (active && slice == 0) {
+        }
+        __syncthreads();
+        if (active && slice == 0) {
+#pragma unroll
+            for (int r = 0; r < NR; r++) {
+                if (!tv[r]) continue;
                 R sx = 0, sy = 0;
                 for (int k = 0; k < nslice; k++) {
-                    const R *r = red + 4 * (tl + k * ntc);
-                    sx += r[0] + r[2];
-                    sy += r[1] + r[3];
+                    const R *o = red + 2 * ((k * nthr + tl) * NR + r);
+                    sx += o[0];
+                    sy += o[1];
                 }
+                const int t = ti[r];
                 double ax = d.gconst * (double)sx, ay = d.gconst * (double)sy;
                 if (accumulate) {
-                    ax += (double)d.AX[ti];
-                    ay += (double)d.AY[ti];
+                    ax += d.AX[t];
+                    ay += d.AY[t];
                 }
-                d.AX[ti] = ax;
-                d.AY[ti] = ay;
+                d.AX[t] = ax;
+                d.AY[t] = ay;
                 if (tick) {
-                    double vx = d.VX[nxt][ti] + ax * d.dt, vy = d.VY[nxt][ti] + ay * d.dt;
-                    d.VX[nxt][ti] = vx;
-                    d.VY[nxt][ti] = vy;
-                    d.X[nxt][ti] = Xs[ti] + vx * d.dt;
-                    d.Y[nxt][ti] = Ys[ti] + vy * d.dt;
+                    double vx = d.VX[nxt][t] + ax * d.dt, vy = d.VY[nxt][t] + ay * d.dt;
+                    d.VX[nxt][t] = vx;
+                    d.VY[nxt][t] = vy;
+                    d.X[nxt][t] = Xs[t] + vx * d.dt;
+                    d.Y[nxt][t] = Ys[t] + vy * d.dt;
                 }
             }
-            __syncthreads();
         }
         if (tid == 0) {
             atomicAdd(&d.glob->near_pairs, s_npairs);
@@ -479,24 +493,29 @@ __global__ void __launch_bounds__(FT) k_force(DevPlan d, int tick, int accumulat
 template <typename R>
 static size_t force_smem() {
     using S = typename Src<R>::T;
-    return sizeof(S) * (FAR_CAP + SRC_CAP) + sizeof(R) * 4 * FT + sizeof(float2) * NEAR_CAP +
+    return sizeof(S) * (FAR_CAP + SRC_CAP) + sizeof(float2) * NEAR_CAP +
            sizeof(int) * (3 * NEAR_CAP + 4) + sizeof(int) * 2 * FR_CAP;
 }
 
-template <typename R, bool KAHAN, bool TEST, bool EXACT>
+template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT>
 static cudaError_t launch_force_t(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
-    auto k = k_force<R, KAHAN, TEST, EXACT>;
+    static_assert(sizeof(R) * 2 * FT * NR <= sizeof(typename Src<R>::T) * (FAR_CAP + SRC_CAP),
+                  "reduction buffer must fit in the staging buffers");
+    auto k = k_force<R, NR, KAHAN, TEST, EXACT>;
     size_t sm = force_smem<R>();
-    long long grid = d.NG_total;
-    if (grid > (1LL << 30)) grid = 1LL << 30;
+    long long items_max = d.NG_total + d.n_total / TARGET_CHUNK + 1;
+    long long grid = 152LL * (sizeof(R) == 4 ? 8 : 4);
+    if (grid > items_max) grid = items_max;
     if (grid < 1) grid = 1;
+    cudaError_t e = cudaMemsetAsync(&d.glob->item_next, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
     k<<<(unsigned)grid, FT, sm, st>>>(d, tick ? 1 : 0, accumulate ? 1 : 0);
     return cudaGetLastError();
 }
 
-template <typename R, bool KAHAN, bool TEST, bool EXACT>
+template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT>
 static cudaError_t init_force_t() {
-    return cudaFuncSetAttribute(k_force<R, KAHAN, TEST, EXACT>,
+    return cudaFuncSetAttribute(k_force<R, NR, KAHAN, TEST, EXACT>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)force_smem<R>());
 }
 
@@ -504,14 +523,14 @@ static cudaError_t init_force_t() {
 // any stream capture).
 cudaError_t force_init() {
     cudaError_t e;
-    if ((e = init_force_t<double, false, true, false>()) != cudaSuccess) return e;
-    if ((e = init_force_t<double, false, false, false>()) != cudaSuccess) return e;
-    if ((e = init_force_t<float, true, true, true>()) != cudaSuccess) return e;
-    if ((e = init_force_t<float, true, true, false>()) != cudaSuccess) return e;
-    if ((e = init_force_t<float, true, false, false>()) != cudaSuccess) return e;
-    if ((e = init_force_t<float, false, true, true>()) != cudaSuccess) return e;
-    if ((e = init_force_t<float, false, true, false>()) != cudaSuccess) return e;
-    return init_force_t<float, false, false, false>();
+    if ((e = init_force_t<double, 2, false, true, false>()) != cudaSuccess) return e;
+    if ((e = init_force_t<double, 2, false, false, false>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, FORCE_R, true, true, true>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, FORCE_R, true, true, false>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, FORCE_R, true, false, false>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, FORCE_R, false, true, true>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, FORCE_R, false, true, false>()) != cudaSuccess) return e;
+    return init_force_t<float, FORCE_R, false, false, false>();
 }
 
 cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
@@ -519,17 +538,17 @@ cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStrea
     const bool test = d.cutoff > 0.0 || d.eps2 == 0.0;
     const bool exact = d.cutoff > 0.0;
     if (d.prec == 2) {
-        if (test) return launch_force_t<double, false, true, false>(d, tick, accumulate, st);
-        return launch_force_t<double, false, false, false>(d, tick, accumulate, st);
+        if (test) return launch_force_t<double, 2, false, true, false>(d, tick, accumulate, st);
+        return launch_force_t<double, 2, false, false, false>(d, tick, accumulate, st);
     }
     if (d.prec == 1) {
-        if (exact) return launch_force_t<float, true, true, true>(d, tick, accumulate, st);
-        if (test) return launch_force_t<float, true, true, false>(d, tick, accumulate, st);
-        return launch_force_t<float, true, false, false>(d, tick, accumulate, st);
+        if (exact) return launch_force_t<float, FORCE_R, true, true, true>(d, tick, accumulate, st);
+        if (test) return launch_force_t<float, FORCE_R, true, true, false>(d, tick, accumulate, st);
+        return launch_force_t<float, FORCE_R, true, false, false>(d, tick, accumulate, st);
     }
-    if (exact) return launch_force_t<float, false, true, true>(d, tick, accumulate, st);
-    if (test) return launch_force_t<float, false, true, false>(d, tick, accumulate, st);
-    return launch_force_t<float, false, false, false>(d, tick, accumulate, st);
+    if (exact) return launch_force_t<float, FORCE_R, false, true, true>(d, tick, accumulate, st);
+    if (test) return launch_force_t<float, FORCE_R, false, true, false>(d, tick, accumulate, st);
+    return launch_force_t<float, FORCE_R, false, false, false>(d, tick, accumulate, st);
 }
 
 }  // namespace bh

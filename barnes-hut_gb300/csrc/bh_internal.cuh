@@ -28,6 +28,10 @@
 namespace bh {
 
 constexpr int MAX_LEVELS = 16;  // G <= 32768
+constexpr int FORCE_THREADS = 128;
+constexpr int FORCE_R = 4;                                   // targets per thread (FP32)
+constexpr int TARGET_CHUNK = FORCE_THREADS * FORCE_R;        // targets per work item
+constexpr int FRONTIER_CAP = 512;                            // traversal frontier per level
 
 struct SysDesc {
     long long n, poff;  // particle count, first particle (concatenated)
@@ -49,6 +53,8 @@ struct Globals {
     unsigned int epoch;
     unsigned int err;
     unsigned long long near_pairs, far_pairs;
+    unsigned int item_next;  // force work queue head (zeroed before each force launch)
+    unsigned int pad;
 };
 
 struct MlpDev;  // learned correction weights (bh_mlp.cu)
@@ -70,6 +76,7 @@ struct DevPlan {
     float4 *P;
     int *key, *slot, *skey;
     int *counts, *box_start, *tile_sums;
+    int *item_cnt, *item_off, *item_group;  // force work items (group, target chunk)
     double *mom;
     float4 *rec, *rec2;
     // parameters
@@ -136,6 +143,7 @@ cudaError_t launch_prologue(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_bbox(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_place(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_scan(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_items(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st);

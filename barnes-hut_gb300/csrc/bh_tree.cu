@@ -174,49 +174,89 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh, int *total) {
     return pre;
 }
 
-__global__ void __launch_bounds__(TPB) k_scan_tiles(DevPlan d) {
+// Generic over (in, out, n): out[i] = sum(in[0..i)), out[n] = total.
+__global__ void __launch_bounds__(TPB) k_scan_tiles(const int *in, long long n, int *tiles) {
     __shared__ int sh[32];
     long long t0 = (long long)blockIdx.x * SCAN_TILE;
     int s = 0;
     for (int k = threadIdx.x; k < SCAN_TILE; k += TPB) {
         long long b = t0 + k;
-        if (b < d.B_total) s += d.counts[b];
+        if (b < n) s += in[b];
     }
     int tot;
     block_excl_scan(s, sh, &tot);
-    if (threadIdx.x == 0) d.tile_sums[blockIdx.x] = tot;
+    if (threadIdx.x == 0) tiles[blockIdx.x] = tot;
 }
 
-__global__ void __launch_bounds__(1024) k_scan_sums(DevPlan d, int ntiles) {
+__global__ void __launch_bounds__(1024) k_scan_sums(int *tiles, int ntiles, int *out, long long n) {
     __shared__ int sh[32];
     int carry = 0;
     for (int t0 = 0; t0 < ntiles; t0 += 1024) {
         int t = t0 + threadIdx.x;
-        int v = t < ntiles ? d.tile_sums[t] : 0;
+        int v = t < ntiles ? tiles[t] : 0;
         int tot;
         int p = block_excl_scan(v, sh, &tot);
-        if (t < ntiles) d.tile_sums[t] = carry + p;
+        if (t < ntiles) tiles[t] = carry + p;
         carry += tot;
     }
-    if (threadIdx.x == 0) d.box_start[d.B_total] = carry;
+    if (threadIdx.x == 0) out[n] = carry;
 }
 
-__global__ void __launch_bounds__(TPB) k_scan_apply(DevPlan d) {
+__global__ void __launch_bounds__(TPB) k_scan_apply(const int *in, long long n, const int *tiles,
+                                                   int *out) {
     __shared__ int sh[32];
     long long t0 = (long long)blockIdx.x * SCAN_TILE;
-    // each thread owns 16 consecutive counts
+    // each thread owns 16 consecutive entries
     long long b0 = t0 + (long long)threadIdx.x * 16;
     int v[16], s = 0;
 #pragma unroll
     for (int k = 0; k < 16; k++) {
-        v[k] = (b0 + k < d.B_total) ? d.counts[b0 + k] : 0;
+        v[k] = (b0 + k < n) ? in[b0 + k] : 0;
         s += v[k];
     }
-    int pre = block_excl_scan(s, sh, nullptr) + d.tile_sums[blockIdx.x];
+    int pre = block_excl_scan(s, sh, nullptr) + tiles[blockIdx.x];
 #pragma unroll
     for (int k = 0; k < 16; k++) {
-        if (b0 + k < d.B_total) d.box_start[b0 + k] = pre;
+        if (b0 + k < n) out[b0 + k] = pre;
         pre += v[k];
+    }
+}
+
+static cudaError_t scan_excl(const int *in, int *out, long long n, int *tiles, cudaStream_t st) {
+    int ntiles = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
+    if (ntiles < 1) ntiles = 1;
+    k_scan_tiles<<<ntiles, TPB, 0, st>>>(in, n, tiles);
+    k_scan_sums<<<1, 1024, 0, st>>>(tiles, ntiles, out, n);
+    k_scan_apply<<<ntiles, TPB, 0, st>>>(in, n, tiles, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- work items
+// Force work items: a target group with nt targets is split into
+// ceil(nt / TARGET_CHUNK) items so that dense groups spread over many CTAs.
+__global__ void __launch_bounds__(TPB) k_group_items(DevPlan d) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < d.NG_total; g += stride) {
+        int s = find_seg(d.goff_tab, d.nsys, g);
+        const SysDesc &sd = d.sys[s];
+        long long lg = g - sd.goff;
+        int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
+        int gx0 = gi * sd.TG, gy0 = gj * sd.TG;
+        int gx1 = min(sd.G, gx0 + sd.TG), gy1 = min(sd.G, gy0 + sd.TG);
+        int nt = 0;
+        for (int c = gx0; c < gx1; c++) {
+            long long b0 = sd.boff + (long long)c * sd.G + gy0;
+            nt += d.box_start[b0 + (gy1 - gy0)] - d.box_start[b0];
+        }
+        d.item_cnt[g] = (nt + TARGET_CHUNK - 1) / TARGET_CHUNK;
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_fill_items(DevPlan d) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < d.NG_total; g += stride) {
+        int o = d.item_off[g], c = d.item_cnt[g];
+        for (int k = 0; k < c; k++) d.item_group[o + k] = (int)g;
     }
 }
 
@@ -373,11 +413,14 @@ cudaError_t launch_place(const DevPlan &d, cudaStream_t st) {
     return cudaGetLastError();
 }
 cudaError_t launch_scan(const DevPlan &d, cudaStream_t st) {
-    int ntiles = (int)((d.B_total + SCAN_TILE - 1) / SCAN_TILE);
-    if (ntiles < 1) ntiles = 1;
-    k_scan_tiles<<<ntiles, TPB, 0, st>>>(d);
-    k_scan_sums<<<1, 1024, 0, st>>>(d, ntiles);
-    k_scan_apply<<<ntiles, TPB, 0, st>>>(d);
+    return scan_excl(d.counts, d.box_start, d.B_total, d.tile_sums, st);
+}
+cudaError_t launch_items(const DevPlan &d, cudaStream_t st) {
+    unsigned g = grid_for(d.NG_total, TPB, 152LL * 8);
+    k_group_items<<<g, TPB, 0, st>>>(d);
+    cudaError_t e = scan_excl(d.item_cnt, d.item_off, d.NG_total, d.tile_sums, st);
+    if (e != cudaSuccess) return e;
+    k_fill_items<<<g, TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {

@@ -150,6 +150,11 @@ int bh_step(bh_plan *plan, int nsteps, void *stream);
 /* bh_step captured once into a CUDA graph (per nsteps value) and replayed. */
 int bh_step_graph(bh_plan *plan, int nsteps, void *stream);
 
+/* Number of kernels one bh_step round launches (host only; no reference
+ * counterpart: the reference launches 6 Numba kernels per round,
+ * singlegpu.py:41-99). */
+int bh_kernels_per_step(const bh_plan *plan, int *count);
+
 /* Synchronise the stream and read (then clear) the device error flags. */
 int bh_error_flags(bh_plan *plan, unsigned *flags, void *stream);
 

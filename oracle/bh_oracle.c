@@ -308,6 +308,136 @@ int oref_reference_evaluate(long long n, const double *x, const double *y, const
     return G;
 }
 
+/*
+ * Timed, bounded sample of one reference CPU step on a large system (the CPU
+ * baseline).  Runs the O(N) phases in full (bounding box, keys, the sort by
+ * (gx, gy, px, ...), per-box COM) and the com_concat_dedup evaluation for
+ * `nsample` non-empty target boxes drawn with a fixed stride, with OpenMP over
+ * the sampled boxes.  Each sampled box does the reference's work: build its
+ * COM list over all boxes, the far field against it, the four dedup
+ * neighbours with mutual update, and the self interaction.
+ * out[0] = seconds of the O(N) phases, out[1] = seconds of the sampled
+ * evaluation, out[2] = non-empty boxes, out[3] = boxes sampled,
+ * out[4] = estimated seconds per step = out[0] + out[1] * out[2] / out[3].
+ */
+static double wall_seconds(void)
+{
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return (double)clock() / CLOCKS_PER_SEC;
+#endif
+}
+
+void oref_reference_sample_time(long long n, const double *x, const double *y, const double *m,
+                                int G, long long nsample, int nthreads, double *out)
+{
+    double t0 = wall_seconds();
+    double bb[5];
+    oref_bbox(n, x, y, G, bb);
+    rrec *r = (rrec *)malloc(sizeof(rrec) * (size_t)n);
+    for (long long i = 0; i < n; i++) {
+        r[i].gx = (double)ref_key1(x[i], bb[0], bb[4], G);
+        r[i].gy = (double)ref_key1(y[i], bb[1], bb[4], G);
+        r[i].px = x[i];
+        r[i].py = y[i];
+        r[i].m = m[i];
+        r[i].vx = r[i].vy = r[i].ax = r[i].ay = 0.0;
+        r[i].pid = (double)i;
+    }
+    qsort(r, (size_t)n, sizeof(rrec), cmp_rrec);
+    long long B = (long long)G * G;
+    long long *start = (long long *)calloc((size_t)B + 1, sizeof(long long));
+    for (long long i = 0; i < n; i++) start[(long long)r[i].gx * G + (long long)r[i].gy + 1]++;
+    for (long long b = 0; b < B; b++) start[b + 1] += start[b];
+    double *coms = (double *)calloc(3 * (size_t)B, sizeof(double));
+    long long nonempty = 0;
+    for (long long b = 0; b < B; b++) {
+        if (start[b + 1] == start[b]) continue;
+        nonempty++;
+        double M = 0.0, sx = 0.0, sy = 0.0;
+        for (long long i = start[b]; i < start[b + 1]; i++) {
+            sx += r[i].px * r[i].m;
+            sy += r[i].py * r[i].m;
+            M += r[i].m;
+        }
+        coms[3 * b] = sx / M;
+        coms[3 * b + 1] = sy / M;
+        coms[3 * b + 2] = M;
+    }
+    long long *ne = (long long *)malloc(sizeof(long long) * (size_t)(nonempty ? nonempty : 1));
+    long long k = 0;
+    for (long long b = 0; b < B; b++)
+        if (start[b + 1] > start[b]) ne[k++] = b;
+    double t1 = wall_seconds();
+    if (nsample > nonempty) nsample = nonempty;
+    long long strd = nsample ? nonempty / nsample : 1;
+    double sink = 0.0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : sink)
+#endif
+    for (long long q = 0; q < nsample; q++) {
+        long long b = ne[q * strd];
+        int bx = (int)(b / G), by = (int)(b % G);
+        long long s0 = start[b], na = start[b + 1] - s0;
+        double *f1 = (double *)calloc(2 * (size_t)na, sizeof(double));
+        long long *coml = (long long *)malloc(sizeof(long long) * (size_t)B);
+        long long ncom = 0;
+        for (int i = 0; i < G; i++)
+            for (int j = 0; j < G; j++) {
+                long long c = (long long)i * G + j;
+                if (start[c + 1] == start[c] || c == b) continue;
+                if (abs(i - bx) <= 1 && abs(j - by) <= 1) continue;
+                coml[ncom++] = c;
+            }
+        for (long long ii = 0; ii < ncom; ii++) {
+            const double *c = coms + 3 * coml[ii];
+            for (long long j = 0; j < na; j++) {
+                double fa, fb;
+                ref_pair_fk(r[s0 + j].px - c[0], r[s0 + j].py - c[1], 1.0, &fa, &fb);
+                f1[2 * j] -= fa * c[2];
+                f1[2 * j + 1] -= fb * c[2];
+            }
+        }
+        const int nbx[4] = {1, -1, 0, 1}, nby[4] = {0, 1, 1, 1};
+        for (int t = 0; t < 4; t++) {
+            int i2 = bx + nbx[t], j2 = by + nby[t];
+            if (i2 < 0 || i2 >= G || j2 < 0 || j2 >= G) continue;
+            long long c = (long long)i2 * G + j2, t0 = start[c], nbb = start[c + 1] - t0;
+            for (long long i = 0; i < nbb; i++)
+                for (long long j = 0; j < na; j++) {
+                    double fa, fb;
+                    ref_pair_fk(r[s0 + j].px - r[t0 + i].px, r[s0 + j].py - r[t0 + i].py, 1.0, &fa, &fb);
+                    f1[2 * j] -= fa * r[t0 + i].m;
+                    f1[2 * j + 1] -= fb * r[t0 + i].m;
+                    sink += fa * r[s0 + j].m + fb;
+                }
+        }
+        for (long long i = 0; i < na; i++)
+            for (long long j = i + 1; j < na; j++) {
+                double fa, fb;
+                ref_pair_fk(r[s0 + j].px - r[s0 + i].px, r[s0 + j].py - r[s0 + i].py, 1.0, &fa, &fb);
+                f1[2 * i] += fa * r[s0 + j].m;
+                f1[2 * j] -= fa * r[s0 + i].m;
+            }
+        for (long long j = 0; j < na; j++) sink += f1[2 * j] + f1[2 * j + 1];
+        free(f1);
+        free(coml);
+    }
+    double t2 = wall_seconds();
+    out[0] = t1 - t0;
+    out[1] = t2 - t1;
+    out[2] = (double)nonempty;
+    out[3] = (double)nsample;
+    out[4] = out[0] + (nsample ? out[1] * (double)nonempty / (double)nsample : 0.0);
+    out[5] = sink;
+    free(r);
+    free(start);
+    free(coms);
+    free(ne);
+}
+
 /* ------------------------------------------------------------------ 5 -- */
 void oref_tick(long long n, double *x, double *y, double *vx, double *vy, const double *ax,
                const double *ay, double dt)

@@ -68,6 +68,7 @@ def lib():
         L.oref_moments.argtypes = [ll, pd, pd, pd, i, pd, pi, pi, pd, pf]
         L.oref_theta_evaluate.argtypes = [ll, pd, pd, pd, i, i, d, d, d, d, pd, pd, pll, i]
         L.oref_theta_evaluate.restype = i
+        L.oref_reference_sample_time.argtypes = [ll, pd, pd, pd, i, ll, i, pd]
         _lib = L
     return _lib
 
@@ -186,6 +187,17 @@ def theta_evaluate(x, y, m, G, TG=1, theta=0.5, eps2=0.0, cutoff=0.0, gconst=1.0
                               float(eps2), float(cutoff), float(gconst), _p(ax), _p(ay),
                               _p(cnt, ctypes.c_longlong), int(nthreads))
     return ax, ay, int(cnt[0]), int(cnt[1])
+
+
+def reference_sample_time(x, y, m, G, nsample, nthreads=0):
+    """Time a bounded sample of one reference CPU step (see bh_oracle.c).
+    Returns dict(setup_s, sample_s, nonempty, sampled, step_s)."""
+    x, y, m = _d(x), _d(y), _d(m)
+    out = np.zeros(6)
+    lib().oref_reference_sample_time(len(x), _p(x), _p(y), _p(m), int(G), int(nsample),
+                                     int(nthreads), _p(out))
+    return dict(setup_s=out[0], sample_s=out[1], nonempty=int(out[2]), sampled=int(out[3]),
+                step_s=out[4])
 
 
 def tick(x, y, vx, vy, ax, ay, dt):
