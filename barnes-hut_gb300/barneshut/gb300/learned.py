@@ -1,0 +1,165 @@
+"""Learned far-field correction: parameters, tensor-core training and inference.
+
+A 6 -> 64 -> 64 -> 64 -> 2 GELU MLP (BF16 weights and activations, FP32
+accumulation, tcgen05 kernels in libbh_gb300.so) maps the features of a
+(target particle, far cell) pair to the dimensionless correction of the
+monopole acceleration:
+
+  features  u = dx / s, v = dy / s          (target -> cell centre of mass, cell edge s)
+            qxx, qxy, qyy = I / (M s^2)     (second moments about the centre of mass)
+            w = 1 / sqrt(u^2 + v^2)
+  output    c such that  a_cell ~= a_monopole + G M / s * c
+
+The box mass M enters as the exact linear scale of the correction.  Training
+data are (target, cell) pairs produced by the method itself: the exact sum over
+the cell's particles minus its monopole (see bh_learned_pairs).
+"""
+import ctypes
+
+import numpy as np
+
+from . import native
+
+N_FEAT = 6
+
+
+def _lib():
+    L = native.load_library()
+    if not getattr(L, "_mlp_typed", False):
+        vp, ll, i, f = ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int, ctypes.c_float
+        L.bh_mlp_param_count.restype = i
+        L.bh_mlp_image_bytes.restype = i
+        L.bh_mlp_pack.argtypes = [vp, vp, vp]
+        L.bh_mlp_pack.restype = i
+        L.bh_mlp_forward.argtypes = [vp, i, ll, vp, vp, vp, vp, vp]
+        L.bh_mlp_forward.restype = i
+        L.bh_mlp_train_batch.argtypes = [vp, i, vp, ll, vp, vp, vp, vp, vp, vp]
+        L.bh_mlp_train_batch.restype = i
+        L.bh_mlp_adam.argtypes = [vp, vp, vp, vp, i, f, vp]
+        L.bh_mlp_adam.restype = i
+        L._mlp_typed = True
+    return L
+
+
+def init_params(seed=0):
+    """Seeded initialisation (scaled uniform, zero biases) in the flat layout."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(10448, dtype=np.float32)
+
+    def block(off, fan_in, shape, rows=None, cols=None):
+        a = rng.uniform(-1, 1, size=shape) * np.sqrt(3.0 / fan_in)
+        if rows is not None:
+            a[rows:] = 0
+        if cols is not None:
+            a[:, cols:] = 0
+        p[off:off + a.size] = a.reshape(-1)
+
+    block(0, 6, (16, 64), rows=6)
+    block(1088, 64, (64, 64))
+    block(5248, 64, (64, 64))
+    block(9408, 64, (64, 16), cols=2)
+    return p
+
+
+class LearnedCorrection:
+    """Device-resident MLP parameters with tensor-core forward and training."""
+
+    def __init__(self, params=None, device="cuda", seed=0):
+        import torch
+
+        self.torch = torch
+        self.L = _lib()
+        self.device = torch.device(device)
+        assert self.L.bh_mlp_param_count() == 10448
+        p = init_params(seed) if params is None else np.asarray(params, dtype=np.float32)
+        self.params = torch.tensor(p, device=self.device)
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.grad = torch.zeros_like(self.params)
+        self.image = torch.zeros(self.L.bh_mlp_image_bytes() + 256, dtype=torch.uint8, device=self.device)
+        self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.loss = torch.zeros(1, dtype=torch.float32, device=self.device)
+        self.step_count = 0
+        self.target_scale = 1.0
+        self.pack()
+
+    def _st(self):
+        return ctypes.c_void_p(self.torch.cuda.current_stream(self.device).cuda_stream)
+
+    def _img(self):
+        off = (-self.image.data_ptr()) % 256
+        return ctypes.c_void_p(self.image.data_ptr() + off)
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise native.BHError(rc, what)
+
+    def pack(self):
+        self._check(self.L.bh_mlp_pack(ctypes.c_void_p(self.params.data_ptr()), self._img(),
+                                       self._st()), "bh_mlp_pack")
+
+    def check_errors(self):
+        e = int(self.err.item())
+        if e:
+            self.err.zero_()
+            raise native.BHError(native.BH_ERR_DEVICE, f"mlp device error flags 0x{e:x}")
+
+    def forward(self, feats):
+        """feats: (P, >=6) float32 device tensor -> (P, 2) float32."""
+        torch = self.torch
+        f = feats.to(self.device, torch.float32).contiguous()
+        out = torch.empty((f.shape[0], 2), dtype=torch.float32, device=self.device)
+        self._check(self.L.bh_mlp_forward(ctypes.c_void_p(f.data_ptr()), f.shape[1], f.shape[0],
+                                          self._img(), ctypes.c_void_p(self.params.data_ptr()),
+                                          ctypes.c_void_p(out.data_ptr()),
+                                          ctypes.c_void_p(self.err.data_ptr()), self._st()),
+                    "bh_mlp_forward")
+        return out
+
+    def grad_batch(self, feats, targets):
+        """Accumulate the gradient of mean((y - t)^2) over the batch; returns the loss."""
+        torch = self.torch
+        f = feats.to(self.device, torch.float32).contiguous()
+        t = targets.to(self.device, torch.float32).contiguous()
+        self.loss.zero_()
+        self._check(self.L.bh_mlp_train_batch(
+            ctypes.c_void_p(f.data_ptr()), f.shape[1], ctypes.c_void_p(t.data_ptr()), f.shape[0],
+            self._img(), ctypes.c_void_p(self.params.data_ptr()),
+            ctypes.c_void_p(self.grad.data_ptr()), ctypes.c_void_p(self.loss.data_ptr()),
+            ctypes.c_void_p(self.err.data_ptr()), self._st()), "bh_mlp_train_batch")
+        return self.loss
+
+    def adam_step(self, lr):
+        self.step_count += 1
+        self._check(self.L.bh_mlp_adam(ctypes.c_void_p(self.params.data_ptr()),
+                                       ctypes.c_void_p(self.m.data_ptr()),
+                                       ctypes.c_void_p(self.v.data_ptr()),
+                                       ctypes.c_void_p(self.grad.data_ptr()), self.step_count,
+                                       float(lr), self._st()), "bh_mlp_adam")
+        self.pack()
+
+    def train(self, feats, targets, epochs=4, batch=65536, lr=2e-3, seed=0, log=None):
+        """Mini-batch Adam on device tensors; returns the per-epoch mean loss."""
+        torch = self.torch
+        n = feats.shape[0]
+        gen = torch.Generator(device="cpu").manual_seed(seed)
+        hist = []
+        for ep in range(epochs):
+            perm = torch.randperm(n, generator=gen).to(self.device)
+            tot = 0.0
+            nb = 0
+            lr_ep = lr * (0.5 ** ep)
+            for s in range(0, n - batch + 1, batch):
+                idx = perm[s:s + batch]
+                loss = self.grad_batch(feats[idx], targets[idx])
+                self.adam_step(lr_ep)
+                tot += float(loss.item()) / (batch * 2)
+                nb += 1
+            hist.append(tot / max(nb, 1))
+            if log:
+                log(f"epoch {ep}: loss {hist[-1]:.4e}")
+        self.check_errors()
+        return hist
+
+    def state(self):
+        return {"params": self.params.cpu().numpy(), "target_scale": self.target_scale}

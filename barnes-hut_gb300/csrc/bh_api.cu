@@ -536,3 +536,48 @@ extern "C" int bh_diagnostics(bh_plan *p, int sys, int want_potential, double *o
     CK(p, launch_diag(p->dev, sys, want_potential, out, (cudaStream_t)stream), "diagnostics");
     return BH_OK;
 }
+
+// ------------------------------------------------------------ learned correction
+static int mlp_ready() {
+    static int state = 0;  // 0 unknown, 1 ready, 2 failed (idempotent attribute setting)
+    if (state == 0) state = mlp_init() == cudaSuccess ? 1 : 2;
+    return state == 1;
+}
+
+extern "C" int bh_mlp_param_count(void) { return MLP_PARAMS; }
+extern "C" int bh_mlp_image_bytes(void) { return MLP_IMAGE_BYTES; }
+
+extern "C" int bh_mlp_pack(const float *params, void *image, void *stream) {
+    if (!params || !image) return BH_ERR_INVALID;
+    if (((uintptr_t)image) & 15) return BH_ERR_INVALID;
+    return mlp_pack(params, (uint8_t *)image, (cudaStream_t)stream) == cudaSuccess ? BH_OK : BH_ERR_CUDA;
+}
+
+extern "C" int bh_mlp_forward(const float *feats, int fs, long long rows, const void *image,
+                              const float *params, float *out, unsigned *err, void *stream) {
+    if (rows < 0 || fs < 6 || (rows > 0 && (!feats || !image || !params || !out || !err)))
+        return BH_ERR_INVALID;
+    if (((uintptr_t)image) & 15) return BH_ERR_INVALID;
+    if (!mlp_ready()) return BH_ERR_CUDA;
+    return mlp_infer(feats, fs, rows, (const uint8_t *)image, params, out, err,
+                     (cudaStream_t)stream) == cudaSuccess ? BH_OK : BH_ERR_CUDA;
+}
+
+extern "C" int bh_mlp_train_batch(const float *feats, int fs, const float *targets, long long rows,
+                                  const void *image, const float *params, float *grad, float *loss,
+                                  unsigned *err, void *stream) {
+    if (rows < 0 || fs < 6 ||
+        (rows > 0 && (!feats || !targets || !image || !params || !grad || !loss || !err)))
+        return BH_ERR_INVALID;
+    if (((uintptr_t)image) & 15) return BH_ERR_INVALID;
+    if (!mlp_ready()) return BH_ERR_CUDA;
+    return mlp_train(feats, fs, targets, rows, (const uint8_t *)image, params, grad, loss, err,
+                     (cudaStream_t)stream) == cudaSuccess ? BH_OK : BH_ERR_CUDA;
+}
+
+extern "C" int bh_mlp_adam(float *params, float *m, float *v, float *grad, int step, float lr,
+                           void *stream) {
+    if (!params || !m || !v || !grad || step < 1) return BH_ERR_INVALID;
+    return mlp_adam(params, m, v, grad, step, lr, (cudaStream_t)stream) == cudaSuccess ? BH_OK
+                                                                                     : BH_ERR_CUDA;
+}

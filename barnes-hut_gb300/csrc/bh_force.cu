@@ -399,8 +399,10 @@ k_force(DevPlan d, int tick, int accumulate) {
                     int q = q0 + tid;
                     int kind = 0, ci = 0, cj = 0, id = 0;
                     float rx = 0, ry = 0, M = 0;
-                    if (q < nfr) {
-                        int loc = fr[q];
+                    int loc = q < nfr ? fr[q] : 0;
+                    if (q < nfr && (unsigned)loc >= (unsigned)(gl * gl)) {
+                        raise_err(d.glob, 4u /*BH_DEV_BAD_KEY*/);  // never expected: skip the cell
+                    } else if (q < nfr) {
                         ci = loc / gl;
                         cj = loc - ci * gl;
                         long long cell = sd.coff + sd.lvoff[l] + loc;
@@ -439,7 +441,10 @@ k_force(DevPlan d, int tick, int accumulate) {
                 // an overflowed frontier may hold unwritten slots: abandon the walk
                 // (flagged; the host bounds theta and group size so this cannot happen)
                 nfr = s_ovf ? 0 : min(s_nnext, FR_CAP);
-                if (s_ovf && tid == 0) raise_err(d.glob, 2u /*BH_DEV_LIST_OVERFLOW*/);
+                const bool ovf = s_ovf != 0;
+                // every thread must have read s_nnext before the next level resets it
+                __syncthreads();
+                if (ovf && tid == 0) raise_err(d.glob, 2u /*BH_DEV_LIST_OVERFLOW*/);
             }
         }
         flush_far();
@@ -501,6 +506,7 @@ template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT>
 static cudaError_t launch_force_t(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
     static_assert(sizeof(R) * 2 * FT * NR <= sizeof(typename Src<R>::T) * (FAR_CAP + SRC_CAP),
                   "reduction buffer must fit in the staging buffers");
+    static_assert(FT * NR >= TARGET_CHUNK, "a CTA must cover every target of a work item");
     auto k = k_force<R, NR, KAHAN, TEST, EXACT>;
     size_t sm = force_smem<R>();
     long long items_max = d.NG_total + d.n_total / TARGET_CHUNK + 1;
@@ -523,8 +529,8 @@ static cudaError_t init_force_t() {
 // any stream capture).
 cudaError_t force_init() {
     cudaError_t e;
-    if ((e = init_force_t<double, 2, false, true, false>()) != cudaSuccess) return e;
-    if ((e = init_force_t<double, 2, false, false, false>()) != cudaSuccess) return e;
+    if ((e = init_force_t<double, FORCE_R, false, true, false>()) != cudaSuccess) return e;
+    if ((e = init_force_t<double, FORCE_R, false, false, false>()) != cudaSuccess) return e;
     if ((e = init_force_t<float, FORCE_R, true, true, true>()) != cudaSuccess) return e;
     if ((e = init_force_t<float, FORCE_R, true, true, false>()) != cudaSuccess) return e;
     if ((e = init_force_t<float, FORCE_R, true, false, false>()) != cudaSuccess) return e;
@@ -538,8 +544,8 @@ cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStrea
     const bool test = d.cutoff > 0.0 || d.eps2 == 0.0;
     const bool exact = d.cutoff > 0.0;
     if (d.prec == 2) {
-        if (test) return launch_force_t<double, 2, false, true, false>(d, tick, accumulate, st);
-        return launch_force_t<double, 2, false, false, false>(d, tick, accumulate, st);
+        if (test) return launch_force_t<double, FORCE_R, false, true, false>(d, tick, accumulate, st);
+        return launch_force_t<double, FORCE_R, false, false, false>(d, tick, accumulate, st);
     }
     if (d.prec == 1) {
         if (exact) return launch_force_t<float, FORCE_R, true, true, true>(d, tick, accumulate, st);

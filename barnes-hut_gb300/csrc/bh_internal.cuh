@@ -158,4 +158,15 @@ cudaError_t launch_direct(const DevPlan &d, int sys, const long long *targets, l
                           double *ax, double *ay, cudaStream_t st);
 cudaError_t launch_diag(const DevPlan &d, int sys, int want_pot, double *out, cudaStream_t st);
 cudaError_t launch_box_com(const DevPlan &d, int sys, double *out, cudaStream_t st);
+// learned correction (bh_mlp.cu)
+constexpr int MLP_PARAMS = 10448;
+constexpr int MLP_IMAGE_BYTES = 38912;
+cudaError_t mlp_init();
+cudaError_t mlp_pack(const float *params, uint8_t *img, cudaStream_t st);
+cudaError_t mlp_infer(const float *feats, int fs, long long P, const uint8_t *img,
+                      const float *params, float *out, unsigned *err, cudaStream_t st);
+cudaError_t mlp_train(const float *feats, int fs, const float *targets, long long P,
+                      const uint8_t *img, const float *params, float *grad, float *loss,
+                      unsigned *err, cudaStream_t st);
+cudaError_t mlp_adam(float *p, float *m, float *v, float *g, int step, float lr, cudaStream_t st);
 }  // namespace bh

@@ -189,6 +189,30 @@ int bh_direct_sample(bh_plan *plan, int sys, const long long *targets, long long
  * counterpart (the reference reports no energies). */
 int bh_diagnostics(bh_plan *plan, int sys, int want_potential, double *out, void *stream);
 
+/* ---- learned far-field correction (no reference counterpart: python-bh has
+ * no learned component).  A 6 -> 64 -> 64 -> 64 -> 2 GELU MLP with BF16
+ * weights and activations and FP32 accumulation on the 5th-generation tensor
+ * cores.  Parameters are FP32 "master" values in global memory
+ * (bh_mlp_param_count floats); bh_mlp_pack converts them to the BF16 operand
+ * images (bh_mlp_image_bytes bytes) the kernels stage into shared memory.
+ * Feature rows are 6 floats at a stride of feat_stride floats; outputs and
+ * targets are 2 floats per row.  err points at a device unsigned that
+ * receives BH_DEV_WAIT_TIMEOUT if a bounded tensor-core wait gave up. */
+int bh_mlp_param_count(void);
+int bh_mlp_image_bytes(void);
+int bh_mlp_pack(const float *params, void *image, void *stream);
+int bh_mlp_forward(const float *feats, int feat_stride, long long rows, const void *image,
+                   const float *params, float *out, unsigned *err, void *stream);
+/* Accumulate d(loss)/d(params) of loss = mean((y - target)^2) over the rows
+ * into grad (FP32, device, zeroed by bh_mlp_adam) and the summed squared
+ * error into *loss (device float). */
+int bh_mlp_train_batch(const float *feats, int feat_stride, const float *targets,
+                       long long rows, const void *image, const float *params, float *grad,
+                       float *loss, unsigned *err, void *stream);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on params with moments m, v;
+ * zeroes grad.  step counts from 1. */
+int bh_mlp_adam(float *params, float *m, float *v, float *grad, int step, float lr, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
