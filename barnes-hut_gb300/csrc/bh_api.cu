@@ -462,9 +462,9 @@ extern "C" int bh_step_graph(bh_plan *p, int nsteps, void *stream) {
 extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     if (!p || !count) return BH_ERR_INVALID;
     // prologue, 3 box-scan phases, work items (count, 3 scan phases, fill),
-    // pyramid levels 1..Lmax-1, records; with particles also bbox, place,
-    // scatter, leaf moments, force
-    *count = 1 + 3 + 5 + (p->Lmax - 1) + 1 + (p->n_total > 0 ? 5 : 0);
+    // pyramid levels 1..Lmax-1, records; with particles also bbox, bbox
+    // finalize, place, scatter, leaf moments, force
+    *count = 1 + 3 + 5 + (p->Lmax - 1) + 1 + (p->n_total > 0 ? 6 : 0);
     return BH_OK;
 }
 

@@ -90,21 +90,17 @@ k_force(DevPlan d, int tick, int accumulate) {
     int *front0 = npre + NEAR_CAP + 4;                        // FR_CAP
     int *front1 = front0 + FR_CAP;                            // FR_CAP
     __shared__ int sh_scan[32];
-    __shared__ int s_item, s_nfar, s_nnear, s_nnext, s_ovf;
+    __shared__ int s_item;
     __shared__ int s_col0[MAX_TG + 1], s_colpre[MAX_TG + 1];
-    __shared__ unsigned long long s_npairs, s_fpairs;
 
     const int tid = threadIdx.x;
     const int nxt = (d.glob->epoch + 1) & 1;
     const double *Xs = d.X[nxt], *Ys = d.Y[nxt], *Ms = d.M[nxt];
     const long long nitems = d.item_off[d.NG_total];
+    unsigned long long npairs = 0, fpairs = 0;  // counted by thread 0
 
     for (;;) {
-        if (tid == 0) {
-            s_item = (int)atomicAdd(&d.glob->item_next, 1u);
-            s_npairs = 0;
-            s_fpairs = 0;
-        }
+        if (tid == 0) s_item = (int)atomicAdd(&d.glob->item_next, 1u);
         __syncthreads();
         const int item = s_item;
         if (item >= nitems) break;
@@ -129,11 +125,12 @@ k_force(DevPlan d, int tick, int accumulate) {
         if (tid == 0) {
             s_colpre[0] = 0;
             for (int c = 1; c <= ncol; c++) s_colpre[c] += s_colpre[c - 1];
-            s_nfar = 0;
-            s_nnear = 0;
-            s_ovf = 0;
         }
         __syncthreads();
+        // list counters: block-uniform registers, advanced by every thread from the
+        // block scan's totals (no shared counter, no extra barrier)
+        int nfar = 0, nnear = 0, nnext = 0;
+        bool ovf = false;
         const int nt = s_colpre[ncol];
         const int c0 = chunk * TARGET_CHUNK;
         const int T = min(TARGET_CHUNK, nt - c0);
@@ -143,7 +140,7 @@ k_force(DevPlan d, int tick, int accumulate) {
         const R eps2 = (R)(sizeof(R) == 4 ? (double)d.eps2_f : d.eps2);
         const R cut = (R)(sizeof(R) == 4 ? (double)d.cut_f : d.cutoff);
 
-        // ---- thread -> (slice, R targets)
+        // ---- thread -> (slice, NR targets)
         const int nthr = (T + NR - 1) / NR;
         const int nslice = FT / nthr;
         const bool active = tid < nslice * nthr;
@@ -176,9 +173,30 @@ k_force(DevPlan d, int tick, int accumulate) {
 #pragma unroll
         for (int r = 0; r < NR; r++) anx[r] = any_[r] = afx[r] = afy[r] = acx[r] = acy[r] = 0;
 
+        // 1 / (r^2 + eps^2) with the cutoff predicate on the unsoftened r^2
+        auto pair_inv = [&](R dx, R dyy, int r, int sidx) -> R {
+            if (!TEST) return rinv<R>(dx * dx + (dyy * dyy + eps2));
+            R r2 = dx * dx + dyy * dyy;
+            R inv = rinv<R>(r2 + eps2);
+            bool keep = r2 > cut;
+            if (EXACT && sidx >= 0) {
+                R band = cut * (R)1e-3;
+                R diff = r2 - cut;
+                if (diff <= band && diff >= -band) {
+                    double ex = __dsub_rn(txd[r], Xs[sidx]), ey = __dsub_rn(tyd[r], Ys[sidx]);
+                    double e2 = __dmul_rn(ex, ex);
+                    e2 = __dadd_rn(e2, __dmul_rn(ey, ey));
+                    keep = e2 > d.cutoff;
+                }
+            }
+            return keep ? inv : (R)0;
+        };
+
+        // evaluate and empty the far list (entries were written before the last barrier of
+        // the block scan that appended them; the next append's scan barriers order the reuse)
         auto flush_far = [&]() {
             __syncthreads();
-            const int nf = s_nfar;
+            const int nf = nfar;
             if (active) {
                 for (int k = slice; k < nf; k += nslice) {
                     R sx, sy, sm;
@@ -187,10 +205,7 @@ k_force(DevPlan d, int tick, int accumulate) {
 #pragma unroll
                     for (int r = 0; r < NR; r++) {
                         R dx = sx - tx[r], dyy = sy - ty[r];
-                        R r2 = dx * dx + dyy * dyy;
-                        R inv = rinv<R>(r2 + eps2);
-                        if (TEST && !(r2 > cut)) inv = 0;
-                        R w = sm * inv;
+                        R w = sm * pair_inv(dx, dyy, r, -1);
                         R fx = w * dx, fy = w * dyy;
                         if (KAHAN) {
                             R yx = fx - acx[r], t1 = afx[r] + yx;
@@ -206,15 +221,14 @@ k_force(DevPlan d, int tick, int accumulate) {
                     }
                 }
             }
-            if (tid == 0) s_fpairs += (unsigned long long)T * nf;
-            __syncthreads();
-            if (tid == 0) s_nfar = 0;
-            __syncthreads();
+            fpairs += (unsigned long long)T * nf;
+            nfar = 0;
         };
 
         auto flush_near = [&]() {
             __syncthreads();
-            const int nn = s_nnear;
+            const int nn = nnear;
+            int total;
             {
                 constexpr int IT = NEAR_CAP / FT;
                 int v[IT], sum = 0;
@@ -224,18 +238,16 @@ k_force(DevPlan d, int tick, int accumulate) {
                     v[k] = e < nn ? ncnt[e] : 0;
                     sum += v[k];
                 }
-                int tot;
-                int pre = block_scan(sum, sh_scan, &tot);
+                int pre = block_scan(sum, sh_scan, &total);
 #pragma unroll
                 for (int k = 0; k < IT; k++) {
                     int e = tid * IT + k;
                     if (e < nn) npre[e] = pre;
                     pre += v[k];
                 }
-                if (tid == 0) npre[nn] = tot;
+                if (tid == 0) npre[nn] = total;
             }
             __syncthreads();
-            const int total = npre[nn];
             for (int s0 = 0; s0 < total; s0 += SRC_CAP) {
                 const int ns = min(SRC_CAP, total - s0);
                 for (int j = tid; j < ns; j += FT) {
@@ -270,48 +282,29 @@ k_force(DevPlan d, int tick, int accumulate) {
 #pragma unroll
                         for (int r = 0; r < NR; r++) {
                             R dx = sx - tx[r], dyy = sy - ty[r];
-                            R r2 = dx * dx + dyy * dyy;
-                            R inv = rinv<R>(r2 + eps2);
-                            if (TEST) {
-                                bool keep = r2 > cut;
-                                if (EXACT) {
-                                    R band = cut * (R)1e-3;
-                                    R diff = r2 - cut;
-                                    if (diff <= band && diff >= -band) {
-                                        double ex = __dsub_rn(txd[r], Xs[sidx]);
-                                        double ey = __dsub_rn(tyd[r], Ys[sidx]);
-                                        double e2 = __dmul_rn(ex, ex);
-                                        e2 = __dadd_rn(e2, __dmul_rn(ey, ey));
-                                        keep = e2 > d.cutoff;
-                                    }
-                                }
-                                if (!keep) inv = 0;
-                            }
-                            R w = sm * inv;
+                            R w = sm * pair_inv(dx, dyy, r, sidx);
                             anx[r] += w * dx;
                             any_[r] += w * dyy;
                         }
                     }
                 }
-                if (tid == 0) s_npairs += (unsigned long long)T * ns;
-                __syncthreads();
+                npairs += (unsigned long long)T * ns;
+                __syncthreads();  // src is restaged by the next pass
             }
-            if (tid == 0) s_nnear = 0;
-            __syncthreads();
+            nnear = 0;
         };
 
-        // kind: 0 none, 1 far, 2 near, 3 open (children into front_next)
+        // kind: 0 none, 1 far, 2 near, 3 open (children into front_next).  One block scan
+        // places every thread's entries; all threads advance the counters from its total.
         auto emit = [&](int kind, int id, int l, int ci, int cj, float rx, float ry, float M,
                         int *front_next, int gc) {
             int nch = 0;
-            if (kind == 3) {
-                nch = (2 * ci + 1 < gc ? 2 : 1) * (2 * cj + 1 < gc ? 2 : 1);
-            }
+            if (kind == 3) nch = (2 * ci + 1 < gc ? 2 : 1) * (2 * cj + 1 < gc ? 2 : 1);
             int packed = (kind == 1 ? 1 : 0) | ((kind == 2 ? 1 : 0) << 10) | (nch << 20);
             int tot;
             int pre = block_scan(packed, sh_scan, &tot);
             if (kind == 1) {
-                int pos = s_nfar + (pre & 1023);
+                int pos = nfar + (pre & 1023);
                 if (sizeof(R) == 4) {
                     reinterpret_cast<float4 *>(far)[pos] = make_float4(rx, ry, M, __int_as_float(id));
                 } else {
@@ -327,7 +320,7 @@ k_force(DevPlan d, int tick, int accumulate) {
                     reinterpret_cast<typename Src<double>::T *>(far)[pos] = e;
                 }
             } else if (kind == 2) {
-                int pos = s_nnear + ((pre >> 10) & 1023);
+                int pos = nnear + ((pre >> 10) & 1023);
                 int st = d.box_start[id];
                 nbox[pos] = st;
                 ncnt[pos] = d.box_start[id + 1] - st;
@@ -336,30 +329,25 @@ k_force(DevPlan d, int tick, int accumulate) {
                 nshift[pos] = make_float2(__fmul_rn((float)(kx - gx0), step_f),
                                           __fmul_rn((float)(ky - gy0), step_f));
             } else if (kind == 3) {
-                int pos = s_nnext + (pre >> 20);
-                if (pos + nch > FR_CAP) {
-                    s_ovf = 1;
-                } else {
+                int pos = nnext + (pre >> 20);
+                if (pos + nch <= FR_CAP) {
                     for (int a = 0; a < 2; a++)
                         for (int b = 0; b < 2; b++)
                             if (2 * ci + a < gc && 2 * cj + b < gc)
                                 front_next[pos++] = (2 * ci + a) * gc + (2 * cj + b);
                 }
             }
-            __syncthreads();
-            if (tid == 0) {
-                s_nfar += tot & 1023;
-                s_nnear += (tot >> 10) & 1023;
-                s_nnext += tot >> 20;
-            }
-            __syncthreads();
+            nfar += tot & 1023;
+            nnear += (tot >> 10) & 1023;
+            if (nnext + (tot >> 20) > FR_CAP) ovf = true;
+            nnext += tot >> 20;
         };
 
         if (d.flat) {
             const long long B = (long long)G * G;
             for (long long q0 = 0; q0 < B; q0 += FT) {
-                if (s_nfar + FT > FAR_CAP) flush_far();
-                if (s_nnear + FT > NEAR_CAP) flush_near();
+                if (nfar + FT > FAR_CAP) flush_far();
+                if (nnear + FT > NEAR_CAP) flush_near();
                 long long b = q0 + tid;
                 int kind = 0, bx = 0, byy = 0, id = 0;
                 float rx = 0, ry = 0, M = 0;
@@ -388,14 +376,14 @@ k_force(DevPlan d, int tick, int accumulate) {
             if (tid == 0) fr[0] = 0;
             int nfr = 1;
             const float theta2 = d.theta2_f;
-            for (int l = sd.L - 1; l >= 0; l--) {
+            for (int l = sd.L - 1; l >= 0 && nfr > 0; l--) {
                 const int gl = sd.lvg[l];
                 const int gc = l > 0 ? sd.lvg[l - 1] : 0;
-                if (tid == 0) s_nnext = 0;
-                __syncthreads();
+                nnext = 0;
+                __syncthreads();  // frontier entries of the previous level are visible
                 for (int q0 = 0; q0 < nfr; q0 += FT) {
-                    if (s_nfar + FT > FAR_CAP) flush_far();
-                    if (s_nnear + FT > NEAR_CAP) flush_near();
+                    if (nfar + FT > FAR_CAP) flush_far();
+                    if (nnear + FT > NEAR_CAP) flush_near();
                     int q = q0 + tid;
                     int kind = 0, ci = 0, cj = 0, id = 0;
                     float rx = 0, ry = 0, M = 0;
@@ -440,17 +428,15 @@ k_force(DevPlan d, int tick, int accumulate) {
                 fn = t;
                 // an overflowed frontier may hold unwritten slots: abandon the walk
                 // (flagged; the host bounds theta and group size so this cannot happen)
-                nfr = s_ovf ? 0 : min(s_nnext, FR_CAP);
-                const bool ovf = s_ovf != 0;
-                // every thread must have read s_nnext before the next level resets it
-                __syncthreads();
+                nfr = ovf ? 0 : nnext;
                 if (ovf && tid == 0) raise_err(d.glob, 2u /*BH_DEV_LIST_OVERFLOW*/);
             }
         }
         flush_far();
         flush_near();
+        __syncthreads();  // the reduction below reuses the staging buffers
 
-        // ---- reduce slice partials (red aliases the staging buffers) and write
+        // ---- reduce slice partials and write
         if (active) {
 #pragma unroll
             for (int r = 0; r < NR; r++) {
@@ -487,11 +473,11 @@ k_force(DevPlan d, int tick, int accumulate) {
                 }
             }
         }
-        if (tid == 0) {
-            atomicAdd(&d.glob->near_pairs, s_npairs);
-            atomicAdd(&d.glob->far_pairs, s_fpairs);
-        }
-        __syncthreads();
+        __syncthreads();  // red and s_item are reused by the next item
+    }
+    if (tid == 0) {
+        atomicAdd(&d.glob->near_pairs, npairs);
+        atomicAdd(&d.glob->far_pairs, fpairs);
     }
 }
 

@@ -47,6 +47,7 @@ struct SysDyn {
     unsigned long long bbmin[2];  // ordered bits of min x, min y (atomicMin)
     unsigned long long bbmax[2];  // ordered bits of max x, max y (atomicMax)
     double minx, miny, step;      // square bounding box origin and box edge
+    double inv_step;              // 1 / step (0 when step is not positive)
 };
 
 struct Globals {
@@ -122,6 +123,20 @@ __device__ __forceinline__ void square_bbox(double mnx, double mny, double mxx, 
 __device__ __forceinline__ int box_key1(double p, double mn, double step, int G) {
     if (!(step > 0.0)) return 0;
     double k = floor(__ddiv_rn(__dsub_rn(p, mn), step));
+    k = fmin(fmax(k, 0.0), (double)(G - 1));
+    return (int)k;
+}
+
+// Same key, computed as floor((p - mn) * inv_step).  The product differs from the correctly
+// rounded quotient by at most ~3 ulp, so the floors can differ only when the quotient lies
+// within ~3 ulp of an integer (< 1e-10 for G <= 32768); only then is the IEEE division taken.
+__device__ __forceinline__ int box_key1_fast(double p, double mn, double step, double inv, int G) {
+    if (!(step > 0.0)) return 0;
+    double d = __dsub_rn(p, mn);
+    double q = __dmul_rn(d, inv);
+    double k = floor(q);
+    double fr = q - k;
+    if (fr < 1e-10 || fr > 1.0 - 1e-10) k = floor(__ddiv_rn(d, step));
     k = fmin(fmax(k, 0.0), (double)(G - 1));
     return (int)k;
 }

@@ -105,6 +105,23 @@ __global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
     }
 }
 
+// One thread per system: the square bounding box (helpers/grid.py:10-26), its
+// box edge step = edge / G (base.py:233) and 1 / step, once per step.
+__global__ void k_bbox_finalize(DevPlan d) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.nsys) return;
+    SysDyn &dy = d.dyn[s];
+    if (d.sys[s].n == 0) return;
+    double mnx = unord_bits(dy.bbmin[0]), mny = unord_bits(dy.bbmin[1]);
+    double mxx = unord_bits(dy.bbmax[0]), mxy = unord_bits(dy.bbmax[1]);
+    double step;
+    square_bbox(mnx, mny, mxx, mxy, d.sys[s].G, &step);
+    dy.minx = mnx;
+    dy.miny = mny;
+    dy.step = step;
+    dy.inv_step = step > 0.0 ? 1.0 / step : 0.0;
+}
+
 // -------------------------------------------------------------------- place
 // FP64 box keys (bit-exact with the reference), warp-aggregated histogram:
 // lanes with the same key elect one leader that adds the group's size; each
@@ -121,15 +138,11 @@ __global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
         if (i < d.n_total) {
             int s = find_seg(d.poff_tab, d.nsys, i);
             const SysDesc &sd = d.sys[s];
-            SysDyn &dy = d.dyn[s];
-            double mnx = unord_bits(dy.bbmin[0]), mny = unord_bits(dy.bbmin[1]);
-            double mxx = unord_bits(dy.bbmax[0]), mxy = unord_bits(dy.bbmax[1]);
-            double step;
-            square_bbox(mnx, mny, mxx, mxy, sd.G, &step);
-            if (i == sd.poff) { dy.minx = mnx; dy.miny = mny; dy.step = step; }
+            const SysDyn &dy = d.dyn[s];
             double x = X[i], y = Y[i];
             if (!(isfinite(x) && isfinite(y))) raise_err(d.glob, 1u /*BH_DEV_NAN_POSITION*/);
-            int kx = box_key1(x, mnx, step, sd.G), ky = box_key1(y, mny, step, sd.G);
+            int kx = box_key1_fast(x, dy.minx, dy.step, dy.inv_step, sd.G);
+            int ky = box_key1_fast(y, dy.miny, dy.step, dy.inv_step, sd.G);
             key = (int)(sd.boff + (long long)kx * sd.G + ky);
         }
         unsigned peers = __match_any_sync(0xffffffffu, key);
@@ -409,6 +422,7 @@ cudaError_t launch_bbox(const DevPlan &d, cudaStream_t st) {
 }
 cudaError_t launch_place(const DevPlan &d, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
+    k_bbox_finalize<<<(d.nsys + 127) / 128, 128, 0, st>>>(d);
     k_place<<<grid_for(d.n_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }

@@ -46,7 +46,7 @@ WORKLOAD = "cluster-mixture N=4,194,304, 512x512 boxes, theta=0.5, eps=1e-4, dt=
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_PART, help=argparse.SUPPRESS)
