@@ -163,3 +163,63 @@ class LearnedCorrection:
 
     def state(self):
         return {"params": self.params.cpu().numpy(), "target_scale": self.target_scale}
+
+
+def generate_pairs(systems, grid, theta_hi, theta_lo, n_pairs, max_level=5, targets_per_item=8,
+                   softening=1e-4, device="cuda", seed=0):
+    """Training rows made by the method: for each (x, y, m, vx, vy) system, build the tree and
+    collect (target, band cell) rows until n_pairs rows exist.  Returns device tensors
+    feats (n, 8) and targets (n, 2)."""
+    import torch
+
+    feats = torch.zeros((n_pairs, 8), dtype=torch.float32, device=device)
+    targs = torch.zeros((n_pairs, 2), dtype=torch.float32, device=device)
+    counter = torch.zeros(1, dtype=torch.int32, device=device)
+    per_sys = max(1, n_pairs // max(1, len(systems)))
+    for k, s in enumerate(systems):
+        prm = native.make_params(1.0, 1e-5, softening, 0.0, theta_hi, 0, native.BH_PREC_FP32_KAHAN)
+        plan = native.Plan([len(s[0])], [grid], prm, device=device)
+        plan.load(*s)
+        plan.create_tree()
+        plan.summarize()
+        goal = min(n_pairs, (k + 1) * per_sys if k + 1 < len(systems) else n_pairs)
+        offset, stride = (seed + k) % 7, 7
+        rounds = 0
+        while int(counter.item()) < goal and rounds < 7:
+            plan.learned_pairs(theta_hi, theta_lo, goal, max_level=max_level,
+                               item_offset=(offset + rounds) % stride, item_stride=stride,
+                               targets_per_item=targets_per_item, feats=feats, targets=targs,
+                               counter=counter)
+            rounds += 1
+        plan.error_flags()
+        plan.close()
+    n = min(int(counter.item()), n_pairs)
+    return feats[:n], targs[:n]
+
+
+def fold_output_scale(mlp, scale):
+    """Multiply the network output by `scale` (last layer weights and bias)."""
+    p = mlp.params
+    p[9408:10432] *= scale
+    p[10432:10448] *= scale
+    mlp.pack()
+
+
+def train_correction(systems, grid, theta_hi=0.8, theta_lo=0.5, n_pairs=1 << 20, epochs=4,
+                     batch=16384, lr=3e-3, seed=0, device="cuda", log=None):
+    """Generate pairs, train the MLP on normalised targets, fold the scale back."""
+    import torch
+
+    feats, targs = generate_pairs(systems, grid, theta_hi, theta_lo, n_pairs, seed=seed,
+                                  device=device)
+    scale = float(targs.abs().mean()) * 2.0 + 1e-30
+    mlp = LearnedCorrection(device=device, seed=seed)
+    hist = mlp.train(feats, targs / scale, epochs=epochs, batch=min(batch, feats.shape[0]),
+                     lr=lr, seed=seed, log=log)
+    fold_output_scale(mlp, scale)
+    mlp.target_scale = scale
+    with torch.no_grad():
+        pred = mlp.forward(feats)
+        resid = float(((pred - targs) ** 2).mean() / (targs ** 2).mean())
+    return mlp, {"pairs": int(feats.shape[0]), "loss_history": hist, "scale": scale,
+                 "relative_mse": resid}

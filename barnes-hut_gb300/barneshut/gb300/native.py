@@ -36,7 +36,8 @@ EXPORTS = (
     "bh_bind", "bh_load", "bh_load_records", "bh_store_records", "bh_store", "bh_create_tree",
     "bh_summarize", "bh_evaluate", "bh_timestep", "bh_step", "bh_step_graph", "bh_error_flags",
     "bh_pair_counts", "bh_box_moments", "bh_grid_info", "bh_direct_sample", "bh_diagnostics",
-    "bh_kernels_per_step",
+    "bh_kernels_per_step", "bh_mlp_param_count", "bh_mlp_image_bytes", "bh_mlp_pack",
+    "bh_mlp_forward", "bh_mlp_train_batch", "bh_mlp_adam", "bh_set_correction", "bh_learned_pairs",
 )
 
 
@@ -60,7 +61,8 @@ class Params(ctypes.Structure):
         ("group_dim", ctypes.c_int),
         ("precision", ctypes.c_int),
         ("flags", ctypes.c_int),
-        ("reserved", ctypes.c_int),
+        ("tune", ctypes.c_int),
+        ("correction_theta", ctypes.c_double),
     ]
 
 
@@ -107,9 +109,11 @@ def load_library(path=None):
     L.bh_direct_sample.argtypes = [vp, i, vp, ll, vp, vp, vp]
     L.bh_diagnostics.argtypes = [vp, i, i, vp, vp]
     L.bh_kernels_per_step.argtypes = [vp, pi]
+    L.bh_set_correction.argtypes = [vp, vp, vp]
+    L.bh_learned_pairs.argtypes = [vp, d, d, i, ll, ll, i, vp, vp, vp, ll, vp]
     for name in EXPORTS:
         f = getattr(L, name)
-        if name not in ("bh_last_error", "bh_grid_dim"):
+        if name not in ("bh_last_error",):
             f.restype = i
     _lib = L
     return L
@@ -120,9 +124,11 @@ def grid_dim(n, max_particles_per_box):
 
 
 def make_params(grav_constant=1.0, tick_seconds=0.005, softening=0.0, cutoff_r2=1e-5,
-                theta=0.0, group_dim=0, precision=BH_PREC_FP32_KAHAN, flags=0):
+                theta=0.0, group_dim=0, precision=BH_PREC_FP32_KAHAN, flags=0, tune=0,
+                correction_theta=0.0):
     return Params(float(grav_constant), float(tick_seconds), float(softening), float(cutoff_r2),
-                  float(theta), int(group_dim), int(precision), int(flags), 0)
+                  float(theta), int(group_dim), int(precision), int(flags), int(tune),
+                  float(correction_theta))
 
 
 def _ptr(t):
@@ -259,6 +265,28 @@ class Plan:
         if raise_on_error and f.value:
             raise BHError(BH_ERR_DEVICE, f"device error flags 0x{f.value:x}")
         return f.value
+
+    def set_correction(self, mlp):
+        """Bind a LearnedCorrection (barneshut.gb300.learned) used when the plan's
+        params carry BH_FLAG_LEARNED."""
+        self._mlp = mlp
+        self._check(self.L.bh_set_correction(self.h, mlp._img(),
+                                             ctypes.c_void_p(mlp.params.data_ptr())))
+
+    def learned_pairs(self, theta_hi, theta_lo, capacity, max_level=5, item_offset=0,
+                      item_stride=16, targets_per_item=8, feats=None, targets=None, counter=None):
+        """Training rows from the current tree (after create_tree + summarize).
+        Returns (feats (cap, 8), targets (cap, 2), counter tensor)."""
+        torch = self._torch
+        if feats is None:
+            feats = torch.zeros((capacity, 8), dtype=torch.float32, device=self.device)
+            targets = torch.zeros((capacity, 2), dtype=torch.float32, device=self.device)
+            counter = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._check(self.L.bh_learned_pairs(
+            self.h, float(theta_hi), float(theta_lo), int(max_level), int(item_offset),
+            int(item_stride), int(targets_per_item), _ptr(feats), _ptr(targets), _ptr(counter),
+            int(capacity), self._st()))
+        return feats, targets, counter
 
     def kernels_per_step(self):
         c = ctypes.c_int()

@@ -39,6 +39,9 @@ struct bh_plan {
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 0;
     cudaStream_t gstream = nullptr;
+    // learned correction (caller-owned device buffers)
+    const uint8_t *mlp_img = nullptr;
+    const float *mlp_params = nullptr;
     char err[512];
 };
 
@@ -285,7 +288,8 @@ static void fill_dev(bh_plan *p) {
     d.flat = pr.theta > 0.0 ? 0 : 1;
     d.prec = pr.precision;
     d.learned = (pr.flags & BH_FLAG_LEARNED) ? 1 : 0;
-    d.mlp = nullptr;
+    d.tune = pr.tune;
+    d.correction_theta = pr.correction_theta;
 }
 
 extern "C" int bh_bind(bh_plan *p, void *workspace, size_t bytes, void *stream) {
@@ -296,6 +300,7 @@ extern "C" int bh_bind(bh_plan *p, void *workspace, size_t bytes, void *stream) 
     cudaStream_t st = (cudaStream_t)stream;
     CK(p, cudaGetDevice(&p->device), "cudaGetDevice");
     CK(p, force_init(), "force kernel attributes");
+    CK(p, learned_init(), "learned kernel attributes");
     p->ws = workspace;
     fill_dev(p);
     char *w = (char *)workspace;
@@ -394,7 +399,11 @@ extern "C" int bh_evaluate(bh_plan *p, void *stream) {
     int r = need_bound(p);
     if (r) return r;
     if (!p->has_tree) return fail(p, BH_ERR_INVALID, "evaluate before create_tree");
+    if (p->dev.learned && !p->mlp_img) return fail(p, BH_ERR_INVALID, "BH_FLAG_LEARNED without bh_set_correction");
     CK(p, launch_force(p->dev, false, !p->acc_stale, (cudaStream_t)stream), "evaluate");
+    if (p->dev.learned)
+        CK(p, launch_learned_correct(p->dev, p->params.correction_theta, p->mlp_img, p->mlp_params,
+                                     false, (cudaStream_t)stream), "learned correction");
     p->acc_stale = false;
     return BH_OK;
 }
@@ -412,7 +421,14 @@ static int enqueue_steps(bh_plan *p, int nsteps, cudaStream_t st) {
         int r = enqueue_tree(p, st);
         if (r) return r;
         CK(p, launch_summarize(p->dev, st), "summarize");
-        CK(p, launch_force(p->dev, true, false, st), "force+tick");
+        if (p->dev.learned) {
+            if (!p->mlp_img) return fail(p, BH_ERR_INVALID, "BH_FLAG_LEARNED without bh_set_correction");
+            CK(p, launch_force(p->dev, false, false, st), "force");
+            CK(p, launch_learned_correct(p->dev, p->params.correction_theta, p->mlp_img,
+                                         p->mlp_params, true, st), "learned correction+tick");
+        } else {
+            CK(p, launch_force(p->dev, true, false, st), "force+tick");
+        }
     }
     return BH_OK;
 }
@@ -580,4 +596,33 @@ extern "C" int bh_mlp_adam(float *params, float *m, float *v, float *grad, int s
     if (!params || !m || !v || !grad || step < 1) return BH_ERR_INVALID;
     return mlp_adam(params, m, v, grad, step, lr, (cudaStream_t)stream) == cudaSuccess ? BH_OK
                                                                                      : BH_ERR_CUDA;
+}
+
+extern "C" int bh_set_correction(bh_plan *p, const void *image, const float *params) {
+    if (!p) return BH_ERR_INVALID;
+    if (!image || !params || (((uintptr_t)image) & 15)) return fail(p, BH_ERR_INVALID, "bad MLP buffers");
+    p->mlp_img = (const uint8_t *)image;
+    p->mlp_params = params;
+    if (p->gexec) {  // a captured step must pick up the new buffers
+        cudaGraphExecDestroy(p->gexec);
+        p->gexec = nullptr;
+        p->gsteps = 0;
+    }
+    return BH_OK;
+}
+
+extern "C" int bh_learned_pairs(bh_plan *p, double theta_hi, double theta_lo, int max_level,
+                                long long item_offset, long long item_stride, int tpi, float *feats,
+                                float *targets, unsigned *counter, long long capacity,
+                                void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (!p->has_tree) return fail(p, BH_ERR_INVALID, "learned_pairs before create_tree/summarize");
+    if (!(theta_hi > theta_lo) || !(theta_lo > 0.0) || item_stride < 1 || item_offset < 0 ||
+        tpi < 1 || capacity < 0 || !feats || !targets || !counter)
+        return fail(p, BH_ERR_INVALID, "bad learned_pairs arguments");
+    CK(p, launch_learned_pairs(p->dev, theta_hi, theta_lo, max_level, item_offset, item_stride, tpi,
+                               feats, targets, counter, capacity, (cudaStream_t)stream),
+       "learned pairs");
+    return BH_OK;
 }

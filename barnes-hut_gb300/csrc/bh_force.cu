@@ -25,7 +25,7 @@
 namespace bh {
 
 constexpr int FT = FORCE_THREADS;
-constexpr int FAR_CAP = 512;   // far entries per flush
+constexpr int FAR_CAP = 384;   // far entries per flush
 constexpr int NEAR_CAP = 256;  // near boxes per flush
 constexpr int SRC_CAP = 512;   // near sources per staging pass
 constexpr int FR_CAP = FRONTIER_CAP;
@@ -44,6 +44,40 @@ __device__ __forceinline__ float rcp_approx(float x) {
 template <typename R> __device__ __forceinline__ R rinv(R x);
 template <> __device__ __forceinline__ float rinv<float>(float x) { return rcp_approx(x); }
 template <> __device__ __forceinline__ double rinv<double>(double x) { return 1.0 / x; }
+
+// Packed FP32 pairs (sm_100-family f32x2 instructions): two lanes of work per instruction.
+typedef unsigned long long f2_t;
+__device__ __forceinline__ f2_t f2_pack(float a, float b) {
+    f2_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2_t v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b) {
+    f2_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
+    f2_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
+    f2_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ f2_t f2_rcp(f2_t a) {
+    f2_t r;
+    asm("{\n.reg .f32 a0, a1, r0, r1;\nmov.b64 {a0, a1}, %1;\nrcp.approx.ftz.f32 r0, a0;\n"
+        "rcp.approx.ftz.f32 r1, a1;\nmov.b64 %0, {r0, r1};\n}"
+        : "=l"(r)
+        : "l"(a));
+    return r;
+}
 
 __device__ __forceinline__ void src_get(const float4 &e, float &x, float &y, float &m, int &idx) {
     x = e.x; y = e.y; m = e.z; idx = __float_as_int(e.w);
@@ -75,15 +109,24 @@ __device__ __forceinline__ int block_scan(int v, int *sh, int *total) {
     return pre;
 }
 
-template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT>
-__global__ void __launch_bounds__(FT, (sizeof(R) == 4 ? 8 : 4))
+// bytes per staged near source: the record, or (x, x, y, y) + (m, m) for the packed path
+template <typename R> __host__ __device__ constexpr int src_bytes() {
+    return sizeof(typename Src<R>::T) > 24 ? (int)sizeof(typename Src<R>::T) : 24;
+}
+
+template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT, int MINB>
+__global__ void __launch_bounds__(FT, MINB)
 k_force(DevPlan d, int tick, int accumulate) {
     using S = typename Src<R>::T;
+    // packed FP32 near field (no cutoff test): sources staged as (x, x, y, y) + (m, m)
+    constexpr bool PACKED = sizeof(R) == 4 && !TEST && NR % 2 == 0;
     extern __shared__ __align__(16) unsigned char smem[];
     S *far = reinterpret_cast<S *>(smem);                     // FAR_CAP
-    S *src = far + FAR_CAP;                                   // SRC_CAP
+    S *src = far + FAR_CAP;                                   // SRC_CAP x src_bytes<R>()
+    float2 *srcm = reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(src) + SRC_CAP);
     R *red = reinterpret_cast<R *>(smem);                     // aliases far/src at the end
-    float2 *nshift = reinterpret_cast<float2 *>(src + SRC_CAP);  // NEAR_CAP
+    float2 *nshift = reinterpret_cast<float2 *>(reinterpret_cast<unsigned char *>(src) +
+                                                SRC_CAP * src_bytes<R>());  // NEAR_CAP
     int *nbox = reinterpret_cast<int *>(nshift + NEAR_CAP);   // first particle of near box
     int *ncnt = nbox + NEAR_CAP;
     int *npre = ncnt + NEAR_CAP;                              // NEAR_CAP + 4
@@ -172,6 +215,17 @@ k_force(DevPlan d, int tick, int accumulate) {
         R anx[NR], any_[NR], afx[NR], afy[NR], acx[NR], acy[NR];
 #pragma unroll
         for (int r = 0; r < NR; r++) anx[r] = any_[r] = afx[r] = afy[r] = acx[r] = acy[r] = 0;
+        // packed near-field state: negated target coordinates and accumulators, pairs of targets
+        f2_t ntx2[NR / 2], nty2[NR / 2], nax2[NR / 2], nay2[NR / 2];
+        const f2_t eps2x2 = f2_pack((float)eps2, (float)eps2);
+        if (PACKED) {
+#pragma unroll
+            for (int k = 0; k < NR / 2; k++) {
+                ntx2[k] = f2_pack(-(float)tx[2 * k], -(float)tx[2 * k + 1]);
+                nty2[k] = f2_pack(-(float)ty[2 * k], -(float)ty[2 * k + 1]);
+                nax2[k] = nay2[k] = f2_pack(0.f, 0.f);
+            }
+        }
 
         // 1 / (r^2 + eps^2) with the cutoff predicate on the unsoftened r^2
         auto pair_inv = [&](R dx, R dyy, int r, int sidx) -> R {
@@ -258,7 +312,13 @@ k_force(DevPlan d, int tick, int accumulate) {
                         if (npre[mid] <= J) lo = mid; else hi = mid;
                     }
                     int idx = nbox[lo] + (J - npre[lo]);
-                    if (sizeof(R) == 4) {
+                    if (PACKED) {
+                        float4 p = d.P[idx];
+                        float2 sh = nshift[lo];
+                        float sx = __fadd_rn(sh.x, p.x), sy = __fadd_rn(sh.y, p.y);
+                        reinterpret_cast<float4 *>(src)[j] = make_float4(sx, sx, sy, sy);
+                        srcm[j] = make_float2(p.z, p.z);
+                    } else if (sizeof(R) == 4) {
                         float4 p = d.P[idx];
                         float2 sh = nshift[lo];
                         reinterpret_cast<float4 *>(src)[j] =
@@ -274,7 +334,23 @@ k_force(DevPlan d, int tick, int accumulate) {
                     }
                 }
                 __syncthreads();
-                if (active) {
+                if (active && PACKED) {
+                    const ulonglong2 *s4 = reinterpret_cast<const ulonglong2 *>(src);
+                    const f2_t *sm2 = reinterpret_cast<const f2_t *>(srcm);
+#pragma unroll 2
+                    for (int j = slice; j < ns; j += nslice) {
+                        const ulonglong2 sxy = s4[j];  // (sx, sx), (sy, sy)
+                        const f2_t mm = sm2[j];        // (m, m)
+#pragma unroll
+                        for (int k = 0; k < NR / 2; k++) {
+                            f2_t dx = f2_add(sxy.x, ntx2[k]), dyy = f2_add(sxy.y, nty2[k]);
+                            f2_t r2 = f2_fma(dx, dx, f2_fma(dyy, dyy, eps2x2));
+                            f2_t w = f2_mul(mm, f2_rcp(r2));
+                            nax2[k] = f2_fma(w, dx, nax2[k]);
+                            nay2[k] = f2_fma(w, dyy, nay2[k]);
+                        }
+                    }
+                } else if (active) {
                     for (int j = slice; j < ns; j += nslice) {
                         R sx, sy, sm;
                         int sidx;
@@ -437,6 +513,18 @@ k_force(DevPlan d, int tick, int accumulate) {
         __syncthreads();  // the reduction below reuses the staging buffers
 
         // ---- reduce slice partials and write
+        if (PACKED) {
+#pragma unroll
+            for (int k = 0; k < NR / 2; k++) {
+                float a0, a1, b0, b1;
+                f2_unpack(nax2[k], a0, a1);
+                f2_unpack(nay2[k], b0, b1);
+                anx[2 * k] = (R)a0;
+                anx[2 * k + 1] = (R)a1;
+                any_[2 * k] = (R)b0;
+                any_[2 * k + 1] = (R)b1;
+            }
+        }
         if (active) {
 #pragma unroll
             for (int r = 0; r < NR; r++) {
@@ -484,19 +572,20 @@ k_force(DevPlan d, int tick, int accumulate) {
 template <typename R>
 static size_t force_smem() {
     using S = typename Src<R>::T;
-    return sizeof(S) * (FAR_CAP + SRC_CAP) + sizeof(float2) * NEAR_CAP +
+    return sizeof(S) * FAR_CAP + (size_t)src_bytes<R>() * SRC_CAP + sizeof(float2) * NEAR_CAP +
            sizeof(int) * (3 * NEAR_CAP + 4) + sizeof(int) * 2 * FR_CAP;
 }
 
-template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT>
+template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT,
+          int MINB = (sizeof(R) == 4 ? 8 : 4)>
 static cudaError_t launch_force_t(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
     static_assert(sizeof(R) * 2 * FT * NR <= sizeof(typename Src<R>::T) * (FAR_CAP + SRC_CAP),
                   "reduction buffer must fit in the staging buffers");
     static_assert(FT * NR >= TARGET_CHUNK, "a CTA must cover every target of a work item");
-    auto k = k_force<R, NR, KAHAN, TEST, EXACT>;
+    auto k = k_force<R, NR, KAHAN, TEST, EXACT, MINB>;
     size_t sm = force_smem<R>();
     long long items_max = d.NG_total + d.n_total / TARGET_CHUNK + 1;
-    long long grid = 152LL * (sizeof(R) == 4 ? 8 : 4);
+    long long grid = 152LL * MINB;
     if (grid > items_max) grid = items_max;
     if (grid < 1) grid = 1;
     cudaError_t e = cudaMemsetAsync(&d.glob->item_next, 0, sizeof(unsigned), st);
@@ -505,9 +594,10 @@ static cudaError_t launch_force_t(const DevPlan &d, bool tick, bool accumulate, 
     return cudaGetLastError();
 }
 
-template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT>
+template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT,
+          int MINB = (sizeof(R) == 4 ? 8 : 4)>
 static cudaError_t init_force_t() {
-    return cudaFuncSetAttribute(k_force<R, NR, KAHAN, TEST, EXACT>,
+    return cudaFuncSetAttribute(k_force<R, NR, KAHAN, TEST, EXACT, MINB>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)force_smem<R>());
 }
 
@@ -522,6 +612,8 @@ cudaError_t force_init() {
     if ((e = init_force_t<float, FORCE_R, true, false, false>()) != cudaSuccess) return e;
     if ((e = init_force_t<float, FORCE_R, false, true, true>()) != cudaSuccess) return e;
     if ((e = init_force_t<float, FORCE_R, false, true, false>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, FORCE_R, true, false, false, 6>()) != cudaSuccess) return e;
+    if ((e = init_force_t<float, FORCE_R, false, false, false, 6>()) != cudaSuccess) return e;
     return init_force_t<float, FORCE_R, false, false, false>();
 }
 
@@ -536,10 +628,12 @@ cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStrea
     if (d.prec == 1) {
         if (exact) return launch_force_t<float, FORCE_R, true, true, true>(d, tick, accumulate, st);
         if (test) return launch_force_t<float, FORCE_R, true, true, false>(d, tick, accumulate, st);
+        if (d.tune == 1) return launch_force_t<float, FORCE_R, true, false, false, 6>(d, tick, accumulate, st);
         return launch_force_t<float, FORCE_R, true, false, false>(d, tick, accumulate, st);
     }
     if (exact) return launch_force_t<float, FORCE_R, false, true, true>(d, tick, accumulate, st);
     if (test) return launch_force_t<float, FORCE_R, false, true, false>(d, tick, accumulate, st);
+    if (d.tune == 1) return launch_force_t<float, FORCE_R, false, false, false, 6>(d, tick, accumulate, st);
     return launch_force_t<float, FORCE_R, false, false, false>(d, tick, accumulate, st);
 }
 

@@ -54,11 +54,9 @@ struct Globals {
     unsigned int epoch;
     unsigned int err;
     unsigned long long near_pairs, far_pairs;
-    unsigned int item_next;  // force work queue head (zeroed before each force launch)
-    unsigned int pad;
+    unsigned int item_next;   // force work queue head (zeroed before each force launch)
+    unsigned int item_next2;  // learned-correction work queue head
 };
-
-struct MlpDev;  // learned correction weights (bh_mlp.cu)
 
 struct DevPlan {
     int nsys, Lmax;
@@ -83,8 +81,8 @@ struct DevPlan {
     // parameters
     double gconst, dt, eps2, cutoff;
     float theta2_f, eps2_f, cut_f;
-    int flat, prec, learned;
-    const MlpDev *mlp;
+    int flat, prec, learned, tune;
+    double correction_theta;
 };
 
 // ---------------------------------------------------------------- helpers
@@ -184,4 +182,11 @@ cudaError_t mlp_train(const float *feats, int fs, const float *targets, long lon
                       const uint8_t *img, const float *params, float *grad, float *loss,
                       unsigned *err, cudaStream_t st);
 cudaError_t mlp_adam(float *p, float *m, float *v, float *g, int step, float lr, cudaStream_t st);
+cudaError_t learned_init();
+cudaError_t launch_learned_correct(const DevPlan &d, double theta_lo, const uint8_t *img,
+                                   const float *params, bool tick, cudaStream_t st);
+cudaError_t launch_learned_pairs(const DevPlan &d, double theta_hi, double theta_lo, int max_level,
+                                 long long item_offset, long long item_stride, int tpi,
+                                 float *feats, float *targets, unsigned *counter, long long capacity,
+                                 cudaStream_t st);
 }  // namespace bh

@@ -14,25 +14,11 @@
 // so the rows are the MMA's K dimension and the layer widths (16 or 64) its M dimension; two
 // layers share one M = 128 MMA by stacking: [a1^T; a2^T] x [dh2^T; dh3^T]^T holds dW2 and dW3
 // as diagonal blocks, [a0^T; a3^T; 0] x [dh1^T; dh4^T]^T holds dW1 and dW4.
-#include <cuda_bf16.h>
-
-#include "bh_internal.cuh"
-#include "bh_tc.cuh"
+#include "bh_mlp.cuh"
 
 namespace bh {
 
-constexpr int MLP_IN = 6, MLP_K0 = 16, MLP_H = 64, MLP_NO = 16, MLP_OUT = 2;
-constexpr int P_W1 = 0, P_B1 = 1024, P_W2 = 1088, P_B2 = 5184, P_W3 = 5248, P_B3 = 9344,
-              P_W4 = 9408, P_B4 = 10432, P_TOTAL = 10448;
-// image byte offsets
-constexpr int I_B1 = 0, I_B2 = 2048, I_B3 = 10240, I_B4 = 18432, I_FWD = 20480;
-constexpr int I_B2T = 20480, I_B3T = 28672, I_B4T = 36864, I_TOTAL = 38912;
 constexpr int MT = 128;  // rows per tile = threads per CTA
-
-__device__ __forceinline__ uint16_t bf16_bits(float v) {
-    __nv_bfloat16 b = __float2bfloat16_rn(v);
-    return *reinterpret_cast<uint16_t *>(&b);
-}
 
 // ------------------------------------------------------------------ packing
 __global__ void k_mlp_pack(const float *p, uint8_t *img) {
@@ -76,62 +62,11 @@ struct MlpSmemInfer {
     static constexpr int TOTAL = BIAS + 208 * 4;
 };
 
-__device__ __forceinline__ void copy_bytes(uint8_t *dst, const uint8_t *src, int bytes) {
-    for (int i = threadIdx.x * 16; i < bytes; i += blockDim.x * 16)
-        *reinterpret_cast<uint4 *>(dst + i) = *reinterpret_cast<const uint4 *>(src + i);
-}
-
-// write the 64 BF16 values of row r of a K-major 128 x 64 tile (8 core columns)
-__device__ __forceinline__ void store_row64(uint8_t *tile, int r, const float *v) {
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-        uint32_t w[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-            w[q] = (uint32_t)bf16_bits(v[8 * c + 2 * q]) | ((uint32_t)bf16_bits(v[8 * c + 2 * q + 1]) << 16);
-        *reinterpret_cast<uint4 *>(tile + tc::kmajor_off(r, 8 * c, 8)) = make_uint4(w[0], w[1], w[2], w[3]);
-    }
-}
-__device__ __forceinline__ void store_row16(uint8_t *tile, int r, const float *v) {
-#pragma unroll
-    for (int c = 0; c < 2; c++) {
-        uint32_t w[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-            w[q] = (uint32_t)bf16_bits(v[8 * c + 2 * q]) | ((uint32_t)bf16_bits(v[8 * c + 2 * q + 1]) << 16);
-        *reinterpret_cast<uint4 *>(tile + tc::kmajor_off(r, 8 * c, 2)) = make_uint4(w[0], w[1], w[2], w[3]);
-    }
-}
 // transposed store: value v[j] of row r goes to element (row0 + j, r) of a K-major tile with
 // 16 core columns (K = 128 rows of the batch tile)
 __device__ __forceinline__ void store_colT(uint8_t *tile, int row0, int r, const float *v, int n) {
     for (int j = 0; j < n; j++)
         *reinterpret_cast<uint16_t *>(tile + tc::kmajor_off(row0 + j, r, 16)) = bf16_bits(v[j]);
-}
-
-// load 64 accumulator columns of this thread's lane starting at column col
-__device__ __forceinline__ void ld64(uint32_t tbase, int col, float *v) {
-    const uint32_t lane = (uint32_t)(threadIdx.x & ~31) << 16;
-#pragma unroll
-    for (int c = 0; c < 4; c++) tc::ld16(tbase + lane + col + 16 * c, v + 16 * c);
-    tc::ld_wait();
-}
-
-// one MMA round: issue (thread 0), commit, wait (all threads).  Returns false on timeout.
-template <typename F>
-__device__ __forceinline__ bool mma_round(uint64_t *mbar, uint32_t &phase, F issue) {
-    tc::fence_async_smem();
-    tc::fence_before();
-    __syncthreads();
-    tc::fence_after();
-    if (threadIdx.x == 0) {
-        issue();
-        tc::commit(mbar);
-    }
-    bool ok = tc::mbar_wait(mbar, phase);
-    phase ^= 1u;
-    tc::fence_after();
-    return __syncthreads_and(ok ? 1 : 0) != 0;
 }
 
 // ---------------------------------------------------------------- inference
@@ -164,7 +99,7 @@ __global__ void __launch_bounds__(MT) k_mlp_infer(const float *feats, int fs, lo
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = tslot;
-    const uint32_t sW = tc::smem_u32(W), sA0 = tc::smem_u32(A0), sACT = tc::smem_u32(ACT);
+    const uint32_t sW = tc::smem_u32(W), sA0 = tc::smem_u32(A0);
     uint32_t phase = 0;
     bool ok = true;
     const long long ntiles = (P + MT - 1) / MT;
@@ -178,40 +113,12 @@ __global__ void __launch_bounds__(MT) k_mlp_infer(const float *feats, int fs, lo
             for (int k = 0; k < MLP_IN; k++) v[k] = feats[row * fs + k];
         }
         store_row16(A0, tid, v);
-        ok = mma_round(&mbar, phase, [&] {
-            tc::mma(tmem, tc::kdesc(sA0, 2, 0), tc::kdesc(sW + I_B1, 2, 0), tc::idesc_bf16(128, 64), 0);
-        });
+        float y[2];
+        ok = mlp_tile_forward(sW, sA0, ACT, bias, tmem, &mbar, phase, y);
         if (!ok) break;
-        for (int layer = 0; layer < 2; layer++) {
-            ld64(tmem, 0, v);
-#pragma unroll
-            for (int j = 0; j < 64; j++) v[j] = tc::gelu(v[j] + bias[64 * layer + j]);
-            store_row64(ACT, tid, v);
-            const uint32_t wimg = sW + (layer == 0 ? I_B2 : I_B3);
-            ok = mma_round(&mbar, phase, [&] {
-                for (int j = 0; j < 4; j++)
-                    tc::mma(tmem, tc::kdesc(sACT, 8, j), tc::kdesc(wimg, 8, j), tc::idesc_bf16(128, 64), j);
-            });
-            if (!ok) break;
-        }
-        if (!ok) break;
-        ld64(tmem, 0, v);
-#pragma unroll
-        for (int j = 0; j < 64; j++) v[j] = tc::gelu(v[j] + bias[128 + j]);
-        store_row64(ACT, tid, v);
-        ok = mma_round(&mbar, phase, [&] {
-            for (int j = 0; j < 4; j++)
-                tc::mma(tmem, tc::kdesc(sACT, 8, j), tc::kdesc(sW + I_B4, 8, j), tc::idesc_bf16(128, 16), j);
-        });
-        if (!ok) break;
-        {
-            const uint32_t lane = (uint32_t)(tid & ~31) << 16;
-            tc::ld16(tmem + lane, v);
-            tc::ld_wait();
-        }
         if (row < P) {
-            out[row * 2 + 0] = v[0] + bias[192];
-            out[row * 2 + 1] = v[1] + bias[193];
+            out[row * 2 + 0] = y[0];
+            out[row * 2 + 1] = y[1];
         }
     }
     if (!ok && tid == 0) atomicOr(err, 8u /*BH_DEV_WAIT_TIMEOUT*/);

@@ -65,7 +65,10 @@ typedef struct bh_params {
                              0 = automatic); forced to 1 in flat mode */
     int precision;        /* BH_PREC_* */
     int flags;            /* BH_FLAG_* */
-    int reserved;
+    int tune;             /* force-kernel variant (0: 8 CTAs per SM, 1: 6 CTAs per
+                             SM with more registers), picked by the autotuner */
+    double correction_theta; /* with BH_FLAG_LEARNED: cells accepted at theta but
+                                not at correction_theta get the learned correction */
 } bh_params;
 
 typedef struct bh_plan bh_plan;
@@ -212,6 +215,24 @@ int bh_mlp_train_batch(const float *feats, int feat_stride, const float *targets
 /* One Adam step (beta 0.9 / 0.999, eps 1e-8) on params with moments m, v;
  * zeroes grad.  step counts from 1. */
 int bh_mlp_adam(float *params, float *m, float *v, float *grad, int step, float lr, void *stream);
+
+/* Bind the MLP (image from bh_mlp_pack, FP32 parameters; the caller keeps
+ * both alive) that bh_evaluate and bh_step apply when params.flags has
+ * BH_FLAG_LEARNED: the cells accepted at params.theta but not at
+ * params.correction_theta get a += G M / s * MLP(features) per target. */
+int bh_set_correction(bh_plan *plan, const void *image, const float *params);
+
+/* Training pairs made by the method on the current state (after
+ * bh_create_tree and bh_summarize): for work items item_offset + k *
+ * item_stride, the cells accepted at theta_hi but not at theta_lo up to
+ * pyramid level max_level, and targets_per_item targets of each item, one
+ * row per (target, cell): 8 features (u, v, qxx, qxy, qyy, w, level, 0) and 2
+ * targets ((exact sum over the cell's particles - monopole) * s / M, FP64
+ * sums), appended at rows atomicAdd(counter) < capacity. */
+int bh_learned_pairs(bh_plan *plan, double theta_hi, double theta_lo, int max_level,
+                     long long item_offset, long long item_stride, int targets_per_item,
+                     float *feats, float *targets, unsigned *counter, long long capacity,
+                     void *stream);
 
 #ifdef __cplusplus
 }
