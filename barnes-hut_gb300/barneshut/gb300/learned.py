@@ -205,21 +205,58 @@ def fold_output_scale(mlp, scale):
     mlp.pack()
 
 
+def fold_input_standardisation(mlp, mu, sigma):
+    """The network was trained on (x - mu) / sigma; fold that into W1 and b1 so the
+    kernels take raw features: W1' = W1 / sigma, b1' = b1 - (mu / sigma) W1."""
+    import torch
+
+    p = mlp.params
+    W1 = p[0:1024].view(16, 64)
+    mu_t = torch.zeros(16, device=p.device)
+    sg_t = torch.ones(16, device=p.device)
+    mu_t[:N_FEAT] = torch.as_tensor(mu, dtype=torch.float32, device=p.device)
+    sg_t[:N_FEAT] = torch.as_tensor(sigma, dtype=torch.float32, device=p.device)
+    b1 = p[1024:1088]
+    b1 -= (mu_t / sg_t) @ W1
+    W1 /= sg_t[:, None]
+    mlp.pack()
+
+
+def quadrupole_prediction(feats):
+    """Analytic 2D quadrupole term of the (target, cell) correction in the same units:
+    (exact - monopole) * s / M ~= Re, Im of (qxx - qyy - 2i qxy) / (u - i v)^3."""
+    import torch
+
+    u, v = feats[:, 0].double(), feats[:, 1].double()
+    a, b = (feats[:, 2] - feats[:, 4]).double(), (-2.0 * feats[:, 3]).double()
+    z = torch.complex(u, -v)
+    c = torch.complex(a, b) / z ** 3
+    return torch.stack([c.real, c.imag], dim=1).float()
+
+
 def train_correction(systems, grid, theta_hi=0.8, theta_lo=0.5, n_pairs=1 << 20, epochs=4,
-                     batch=16384, lr=3e-3, seed=0, device="cuda", log=None):
-    """Generate pairs, train the MLP on normalised targets, fold the scale back."""
+                     batch=4096, lr=3e-3, seed=0, device="cuda", log=None):
+    """Generate pairs, train the MLP on standardised features and normalised targets, fold
+    both normalisations into the weights."""
     import torch
 
     feats, targs = generate_pairs(systems, grid, theta_hi, theta_lo, n_pairs, seed=seed,
                                   device=device)
-    scale = float(targs.abs().mean()) * 2.0 + 1e-30
+    mu = feats[:, :N_FEAT].mean(0)
+    sigma = feats[:, :N_FEAT].std(0) + 1e-12
+    fstd = feats.clone()
+    fstd[:, :N_FEAT] = (feats[:, :N_FEAT] - mu) / sigma
+    scale = float(targs.std()) + 1e-30
     mlp = LearnedCorrection(device=device, seed=seed)
-    hist = mlp.train(feats, targs / scale, epochs=epochs, batch=min(batch, feats.shape[0]),
+    hist = mlp.train(fstd, targs / scale, epochs=epochs, batch=min(batch, feats.shape[0]),
                      lr=lr, seed=seed, log=log)
+    fold_input_standardisation(mlp, mu.cpu().numpy(), sigma.cpu().numpy())
     fold_output_scale(mlp, scale)
     mlp.target_scale = scale
     with torch.no_grad():
+        den = float((targs ** 2).mean())
         pred = mlp.forward(feats)
-        resid = float(((pred - targs) ** 2).mean() / (targs ** 2).mean())
+        resid = float(((pred - targs) ** 2).mean()) / den
+        quad = float(((quadrupole_prediction(feats) - targs) ** 2).mean()) / den
     return mlp, {"pairs": int(feats.shape[0]), "loss_history": hist, "scale": scale,
-                 "relative_mse": resid}
+                 "relative_mse": resid, "quadrupole_relative_mse": quad}

@@ -25,7 +25,7 @@
 namespace bh {
 
 constexpr int FT = FORCE_THREADS;
-constexpr int FAR_CAP = 384;   // far entries per flush
+constexpr int FAR_CAP = 256;   // far entries per flush
 constexpr int NEAR_CAP = 256;  // near boxes per flush
 constexpr int SRC_CAP = 512;   // near sources per staging pass
 constexpr int FR_CAP = FRONTIER_CAP;
@@ -121,8 +121,9 @@ k_force(DevPlan d, int tick, int accumulate) {
     // packed FP32 near field (no cutoff test): sources staged as (x, x, y, y) + (m, m)
     constexpr bool PACKED = sizeof(R) == 4 && !TEST && NR % 2 == 0;
     extern __shared__ __align__(16) unsigned char smem[];
-    S *far = reinterpret_cast<S *>(smem);                     // FAR_CAP
-    S *src = far + FAR_CAP;                                   // SRC_CAP x src_bytes<R>()
+    S *far = reinterpret_cast<S *>(smem);                     // FAR_CAP x src_bytes<R>()
+    float2 *farm = reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(far) + FAR_CAP);
+    S *src = reinterpret_cast<S *>(smem + FAR_CAP * src_bytes<R>());  // SRC_CAP x src_bytes<R>()
     float2 *srcm = reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(src) + SRC_CAP);
     R *red = reinterpret_cast<R *>(smem);                     // aliases far/src at the end
     float2 *nshift = reinterpret_cast<float2 *>(reinterpret_cast<unsigned char *>(src) +
@@ -217,13 +218,17 @@ k_force(DevPlan d, int tick, int accumulate) {
         for (int r = 0; r < NR; r++) anx[r] = any_[r] = afx[r] = afy[r] = acx[r] = acy[r] = 0;
         // packed near-field state: negated target coordinates and accumulators, pairs of targets
         f2_t ntx2[NR / 2], nty2[NR / 2], nax2[NR / 2], nay2[NR / 2];
+        // packed far-field sums and Kahan compensations
+        f2_t fsx2[NR / 2], fsy2[NR / 2], fcx2[NR / 2], fcy2[NR / 2];
         const f2_t eps2x2 = f2_pack((float)eps2, (float)eps2);
+        const f2_t m1x2 = f2_pack(-1.f, -1.f);
         if (PACKED) {
 #pragma unroll
             for (int k = 0; k < NR / 2; k++) {
                 ntx2[k] = f2_pack(-(float)tx[2 * k], -(float)tx[2 * k + 1]);
                 nty2[k] = f2_pack(-(float)ty[2 * k], -(float)ty[2 * k + 1]);
                 nax2[k] = nay2[k] = f2_pack(0.f, 0.f);
+                fsx2[k] = fsy2[k] = fcx2[k] = fcy2[k] = f2_pack(0.f, 0.f);
             }
         }
 
@@ -251,7 +256,31 @@ k_force(DevPlan d, int tick, int accumulate) {
         auto flush_far = [&]() {
             __syncthreads();
             const int nf = nfar;
-            if (active) {
+            if (active && PACKED) {
+                const ulonglong2 *fp = reinterpret_cast<const ulonglong2 *>(far);
+                const f2_t *fm = reinterpret_cast<const f2_t *>(farm);
+                for (int k = slice; k < nf; k += nslice) {
+                    const ulonglong2 rxy = fp[k];  // (rx, rx), (ry, ry)
+                    const f2_t mm = fm[k];         // (M, M)
+#pragma unroll
+                    for (int kk = 0; kk < NR / 2; kk++) {
+                        f2_t dx = f2_add(rxy.x, ntx2[kk]), dyy = f2_add(rxy.y, nty2[kk]);
+                        f2_t w = f2_mul(mm, f2_rcp(f2_fma(dx, dx, f2_fma(dyy, dyy, eps2x2))));
+                        f2_t fx = f2_mul(w, dx), fy = f2_mul(w, dyy);
+                        if (KAHAN) {  // y = f - c; t = s + y; c = (t - s) - y; s = t
+                            f2_t yx = f2_fma(fcx2[kk], m1x2, fx), t1 = f2_add(fsx2[kk], yx);
+                            fcx2[kk] = f2_fma(yx, m1x2, f2_fma(fsx2[kk], m1x2, t1));
+                            fsx2[kk] = t1;
+                            f2_t yy = f2_fma(fcy2[kk], m1x2, fy), t2 = f2_add(fsy2[kk], yy);
+                            fcy2[kk] = f2_fma(yy, m1x2, f2_fma(fsy2[kk], m1x2, t2));
+                            fsy2[kk] = t2;
+                        } else {
+                            fsx2[kk] = f2_add(fsx2[kk], fx);
+                            fsy2[kk] = f2_add(fsy2[kk], fy);
+                        }
+                    }
+                }
+            } else if (active) {
                 for (int k = slice; k < nf; k += nslice) {
                     R sx, sy, sm;
                     int sidx;
@@ -382,7 +411,12 @@ k_force(DevPlan d, int tick, int accumulate) {
             if (kind == 1) {
                 int pos = nfar + (pre & 1023);
                 if (sizeof(R) == 4) {
-                    reinterpret_cast<float4 *>(far)[pos] = make_float4(rx, ry, M, __int_as_float(id));
+                    if (PACKED) {
+                        reinterpret_cast<float4 *>(far)[pos] = make_float4(rx, rx, ry, ry);
+                        farm[pos] = make_float2(M, M);
+                    } else {
+                        reinterpret_cast<float4 *>(far)[pos] = make_float4(rx, ry, M, __int_as_float(id));
+                    }
                 } else {
                     const double *q = d.mom + 6 * (long long)id;
                     typename Src<double>::T e;
@@ -523,6 +557,18 @@ k_force(DevPlan d, int tick, int accumulate) {
                 anx[2 * k + 1] = (R)a1;
                 any_[2 * k] = (R)b0;
                 any_[2 * k + 1] = (R)b1;
+                f2_unpack(fsx2[k], a0, a1);
+                f2_unpack(fsy2[k], b0, b1);
+                afx[2 * k] = (R)a0;
+                afx[2 * k + 1] = (R)a1;
+                afy[2 * k] = (R)b0;
+                afy[2 * k + 1] = (R)b1;
+                f2_unpack(fcx2[k], a0, a1);
+                f2_unpack(fcy2[k], b0, b1);
+                acx[2 * k] = (R)a0;
+                acx[2 * k + 1] = (R)a1;
+                acy[2 * k] = (R)b0;
+                acy[2 * k + 1] = (R)b1;
             }
         }
         if (active) {
@@ -572,7 +618,7 @@ k_force(DevPlan d, int tick, int accumulate) {
 template <typename R>
 static size_t force_smem() {
     using S = typename Src<R>::T;
-    return sizeof(S) * FAR_CAP + (size_t)src_bytes<R>() * SRC_CAP + sizeof(float2) * NEAR_CAP +
+    return (size_t)src_bytes<R>() * (FAR_CAP + SRC_CAP) + sizeof(float2) * NEAR_CAP +
            sizeof(int) * (3 * NEAR_CAP + 4) + sizeof(int) * 2 * FR_CAP;
 }
 

@@ -113,8 +113,10 @@ __device__ int band_walk(const DevPlan &d, const ItemGeom &ig, float th2_hi, flo
             int isband = 0, nch = 0;
             int ci = 0, cj = 0;
             BandCell bc;
-            if (q < nfr) {
-                int loc = fr[q];
+            int loc = q < nfr ? fr[q] : 0;
+            if (q < nfr && (unsigned)loc >= (unsigned)(gl * gl)) {
+                raise_err(d.glob, 4u /*BH_DEV_BAD_KEY*/);  // never expected: skip the cell
+            } else if (q < nfr) {
                 ci = loc / gl;
                 cj = loc - ci * gl;
                 long long cell = sd.coff + sd.lvoff[l] + loc;
@@ -175,8 +177,10 @@ __device__ int band_walk(const DevPlan &d, const ItemGeom &ig, float th2_hi, flo
             for (int q0 = 0; q0 < nfr; q0 += LT) {
                 int q = q0 + tid, isband = 0;
                 BandCell bc;
-                if (q < nfr) {
-                    int loc = fr[q];
+                int loc = q < nfr ? fr[q] : 0;
+                if (q < nfr && (unsigned)loc >= (unsigned)(gc * gc)) {
+                    raise_err(d.glob, 4u /*BH_DEV_BAD_KEY*/);
+                } else if (q < nfr) {
                     int ci0 = loc / gc, cj0 = loc - ci0 * gc;
                     long long cell = sd.coff + loc;
                     float4 rr = d.rec[cell];
@@ -367,9 +371,15 @@ __global__ void __launch_bounds__(LT) k_learned_pairs(DevPlan d, float th2_hi, f
     const int nxt = (d.glob->epoch + 1) & 1;
     const double *X = d.X[nxt], *Y = d.Y[nxt], *Mm = d.M[nxt];
     const long long nitems = d.item_off[d.NG_total];
+    __shared__ int s_stop;
     for (long long it = item_offset + (long long)blockIdx.x * item_stride; it < nitems;
          it += (long long)gridDim.x * item_stride) {
-        if (*(volatile unsigned *)counter >= capacity) break;
+        // one thread decides for the whole block (every thread must take the same branch)
+        if (tid == 0) s_stop = *(volatile unsigned *)counter >= capacity;
+        __syncthreads();
+        const bool stop = s_stop != 0;
+        __syncthreads();
+        if (stop) break;
         const long long g = d.item_group[it];
         ItemGeom ig;
         item_geom(d, g, (int)(it - d.item_off[g]), s_col0, s_colpre, ig);

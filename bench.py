@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--grid", type=int, default=GRID, help=argparse.SUPPRESS)
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 accuracy sample")
     ap.add_argument("--ref-sample-boxes", type=int, default=1024)
+    ap.add_argument("--quick", action="store_true",
+                    help="skip the autotuner and the batched / learned side measurements")
     return ap.parse_args()
 
 
@@ -162,6 +164,97 @@ def cpu_baseline(args, x, y, m, G):
             "step_seconds": r["step_s"]}
 
 
+def batched_benchmark(torch, dev, nsys=512, steps=50, warmup=3):
+    """512 independent systems (log-uniform N in [1024, 262144], uniform or 4-cluster,
+    ~64 particles per box, theta 0.5, FP32) stepped together: every phase is one launch
+    over all systems (the force kernel a persistent work queue), the step one CUDA graph."""
+    import numpy as np
+
+    from barneshut.gb300 import autotune, native, workloads
+
+    systems, grids = workloads.batched_systems(nsys, seed=4)
+    n = [len(s[0]) for s in systems]
+    tile, _ = autotune.tune(systems, grids, 1.0, 1e-6, 1e-4, 0.5, device=dev)
+    prm = native.make_params(1.0, 1e-6, 1e-4, 0.0, 0.5, tile["group_dim"],
+                             native.BH_PREC_FP32_KAHAN, 0, tile["tune"])
+    plan = native.Plan(n, grids, prm, device=dev)
+    plan.load(*[np.concatenate([s[k] for s in systems]) for k in range(5)])
+    for _ in range(warmup):
+        plan.step_graph(1)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    plan.step_graph(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    flags = plan.error_flags(raise_on_error=False)
+    out = {"metric": "particle-steps/s, 512 batched systems", "value": sum(n) * steps / t,
+           "systems": nsys, "particles": int(sum(n)), "steps": steps, "ms_per_step": 1e3 * t / steps,
+           "theta": 0.5, "dt": 1e-6, "tile": tile, "graph": f"{steps} steps in one CUDA graph",
+           "kernels_per_step": plan.kernels_per_step(), "device_error_flags": flags}
+    plan.close()
+    return out
+
+
+def learned_benchmark(torch, dev, batch, plain_step_s, plain_acc, steps=20):
+    """Learned far-field correction: network trained on (target, cell) pairs generated by the
+    method on two seeded cluster-mixture systems (N = 1,048,576, 256 x 256 boxes), applied at
+    theta 0.8 on the bench's N = 4,194,304 batch; compared with plain theta 0.5 (the headline)
+    and plain theta 0.8 in step time and in relative RMS force error against the FP64 direct
+    sum on the same 16,384 targets."""
+    import time as _t
+
+    from barneshut.gb300 import learned, native, workloads
+
+    t0 = _t.time()
+    train = [workloads.cluster_mixture(1 << 20, seed=11), workloads.cluster_mixture(1 << 20, seed=12)]
+    mlp, info = learned.train_correction(train, 256, 0.8, 0.5, n_pairs=1 << 21, epochs=4)
+    train_s = _t.time() - t0
+    n = batch[0].numel()
+    tgt = workloads.precision_subsample(n, 16384, seed=SEED)
+    idx = torch.as_tensor(tgt, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    res = {}
+    for name, theta, flags in (("plain_0.8", 0.8, 0), ("learned_0.8", 0.8, native.BH_FLAG_LEARNED)):
+        prm = native.make_params(1.0, DT, SOFTENING, 0.0, theta, 0, native.BH_PREC_FP32_KAHAN,
+                                 flags, 0, 0.5)
+        plan = native.Plan([n], [GRID], prm, device=dev)
+        if flags:
+            plan.set_correction(mlp)
+        for _ in range(3):
+            plan.load(*batch)
+            plan.step_graph(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            plan.load(*batch)
+            plan.step_graph(1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        plan.load(*batch)
+        plan.create_tree()
+        plan.summarize()
+        plan.evaluate()
+        o = plan.store()
+        dax, day = plan.direct_sample(tgt)
+        ax, ay = o["ax"][idx], o["ay"][idx]
+        err = float(torch.sqrt(((ax - dax) ** 2 + (ay - day) ** 2).sum() / (dax ** 2 + day ** 2).sum()))
+        res[name] = {"ms_per_step": ms, "particle_steps_per_s": n / (ms / 1e3),
+                     "rel_rms_vs_fp64_direct": err,
+                     "device_error_flags": plan.error_flags(raise_on_error=False)}
+        plan.close()
+    res["plain_0.5"] = {"ms_per_step": 1e3 * plain_step_s, "particle_steps_per_s": n / plain_step_s,
+                        "rel_rms_vs_fp64_direct": plain_acc["rel_rms_vs_fp64_direct"] if plain_acc else None}
+    res["training"] = {"pairs": info["pairs"], "relative_mse": info["relative_mse"],
+                       "quadrupole_only_relative_mse": info["quadrupole_relative_mse"],
+                       "loss_history": info["loss_history"], "seconds": train_s}
+    return res
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -210,7 +303,16 @@ def main():
     # batch in box order (the state's order between steps of a running simulation)
     order = workloads.box_order(x, y, args.grid)
     x, y, m, vx, vy = (a[order].copy() for a in (x, y, m, vx, vy))
-    prm = native.make_params(1.0, DT, SOFTENING, 0.0, THETA, 0, native.BH_PREC_FP32_KAHAN)
+    tile = {"group_dim": 0, "tune": 0}
+    tune_ms = None
+    if not args.quick:
+        from barneshut.gb300 import autotune
+
+        tile, tt = autotune.tune([(x, y, m, vx, vy)], [args.grid], 1.0, DT, SOFTENING, THETA,
+                                 device=dev)
+        tune_ms = {k: round(1e3 * v, 3) for k, v in tt.items()}
+    prm = native.make_params(1.0, DT, SOFTENING, 0.0, THETA, tile["group_dim"],
+                             native.BH_PREC_FP32_KAHAN, 0, tile["tune"])
     plan = native.Plan([args.n], [args.grid], prm, device=dev)
     stream = torch.cuda.current_stream(dev)
     batch = [torch.from_numpy(a).to(dev) for a in (x, y, m, vx, vy)]
@@ -324,6 +426,11 @@ def main():
         acc = {"rel_rms_vs_fp64_direct": float(torch.sqrt(num / den)),
                "rel_max_vs_fp64_direct": float(rel.max()), "targets": int(len(t))}
 
+    side = {}
+    if not args.quick and rank == 0:
+        side["batched"] = batched_benchmark(torch, dev)
+        side["learned"] = learned_benchmark(torch, dev, batch, t_dev / K, acc)
+
     cpu = None
     if rank == 0:
         cpu = cpu_baseline(args, x, y, m, args.grid)
@@ -352,6 +459,8 @@ def main():
             "accuracy": acc,
             "pairs_per_step": {"near": near2, "far": far2},
             "phases_ms": phases_ms,
+            "tile": {"chosen": tile, "autotune_force_ms": tune_ms},
+            **side,
             "device_error_flags": flags,
             "reference_recorded": {"value": 10_000_000 / 166.837, "unit": "particle-steps/s",
                                    "note": "python-bh singlegpu, N=10M, flat far field, FP64, "
