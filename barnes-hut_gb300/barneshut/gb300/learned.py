@@ -191,6 +191,9 @@ def generate_pairs(systems, grid, theta_hi, theta_lo, n_pairs, max_level=5, targ
                                targets_per_item=targets_per_item, feats=feats, targets=targs,
                                counter=counter)
             rounds += 1
+        # rows past the capacity were counted but not written: the next system appends
+        # right after the last written row
+        counter.clamp_(max=goal)
         plan.error_flags()
         plan.close()
     n = min(int(counter.item()), n_pairs)
