@@ -38,7 +38,9 @@ EXPORTS = (
     "bh_pair_counts", "bh_box_moments", "bh_grid_info", "bh_direct_sample", "bh_diagnostics",
     "bh_kernels_per_step", "bh_mlp_param_count", "bh_mlp_image_bytes", "bh_mlp_pack",
     "bh_mlp_forward", "bh_mlp_train_batch", "bh_mlp_adam", "bh_set_correction", "bh_learned_pairs",
+    "bh_direct_sum_noalloc",
 )
+BH_NOALLOC_MAX_TARGETS = 4096
 
 
 class NativeLibraryError(RuntimeError):
@@ -110,6 +112,7 @@ def load_library(path=None):
     L.bh_diagnostics.argtypes = [vp, i, i, vp, vp]
     L.bh_kernels_per_step.argtypes = [vp, pi]
     L.bh_set_correction.argtypes = [vp, vp, vp]
+    L.bh_direct_sum_noalloc.argtypes = [vp, vp, vp, ll, vp, ll, d, d, vp, vp, vp]
     L.bh_learned_pairs.argtypes = [vp, d, d, i, ll, ll, i, vp, vp, vp, ll, vp]
     for name in EXPORTS:
         f = getattr(L, name)

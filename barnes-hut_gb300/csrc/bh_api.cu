@@ -69,6 +69,11 @@ static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 static thread_local char g_create_err[256] = "";
 
+int bh::bh_set_thread_error(int code, const char *msg) {
+    snprintf(g_create_err, sizeof(g_create_err), "%s", msg);
+    return code;
+}
+
 extern "C" int bh_grid_dim(long long n, int ppb) {
     // base.py:223-231 with helpers/grid.py:5-8 (next_perfect_square)
     if (n <= 0) return 0;

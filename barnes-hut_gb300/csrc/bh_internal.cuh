@@ -171,6 +171,8 @@ cudaError_t launch_direct(const DevPlan &d, int sys, const long long *targets, l
                           double *ax, double *ay, cudaStream_t st);
 cudaError_t launch_diag(const DevPlan &d, int sys, int want_pot, double *out, cudaStream_t st);
 cudaError_t launch_box_com(const DevPlan &d, int sys, double *out, cudaStream_t st);
+// record a failure of a call without a plan (read by bh_last_error(NULL)); returns code
+int bh_set_thread_error(int code, const char *msg);
 // learned correction (bh_mlp.cu)
 constexpr int MLP_PARAMS = 10448;
 constexpr int MLP_IMAGE_BYTES = 38912;

@@ -185,6 +185,29 @@ int bh_grid_info(bh_plan *plan, int sys, double *out, void *stream);
 int bh_direct_sample(bh_plan *plan, int sys, const long long *targets, long long nt,
                      double *ax, double *ay, void *stream);
 
+/* Direct-sum sampler that allocates nothing.  No counterpart in the reference:
+ * it is the FP64 direct sum of bh_direct_sample for callers that cannot
+ * allocate device memory (and so cannot bind a plan workspace) -- e.g. code
+ * inside another framework that has reserved the whole device for its own
+ * memory pool.  Inputs are plain device arrays: positions x, y and masses m
+ * of n particles (any order), nt target indices into them (device
+ * long longs); outputs ax, ay (device, nt doubles):
+ *   a_t = grav_constant * sum_{j != t} m_j (x_j - x_t) / (r^2 + softening^2).
+ * Scratch (the per-chunk partial sums of every target) lives in a static
+ * device array of BH_NOALLOC_MAX_TARGETS x BH_NOALLOC_CHUNKS x 2 doubles (4 MiB)
+ * that every GPU loading the library holds until the process exits; more
+ * than BH_NOALLOC_MAX_TARGETS targets is rejected with BH_ERR_INVALID.  The
+ * first call on a device looks up that array's device address (once, with
+ * the device current); make that first call before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU (e.g. on two streams)
+ * race and must be ordered by the caller.  bh_last_error(NULL) describes a
+ * failure. */
+#define BH_NOALLOC_MAX_TARGETS 4096
+#define BH_NOALLOC_CHUNKS 64
+int bh_direct_sum_noalloc(const double *x, const double *y, const double *m, long long n,
+                          const long long *targets, long long nt, double grav_constant,
+                          double softening, double *ax, double *ay, void *stream);
+
 /* FP64 diagnostics of system `sys` into out[4] (device doubles):
  * kinetic energy, momentum x, momentum y, and the potential energy
  * sum_{i<j} G m_i m_j ln(sqrt(r^2 + eps^2)) by an FP64 direct sum (O(n^2):
