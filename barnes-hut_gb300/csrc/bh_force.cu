@@ -21,13 +21,14 @@
 // contributions Kahan-compensated when requested; BH_PREC_FP64 runs the same lists in FP64.
 // Positions are box-relative offsets rounded once from FP64, so dx keeps ~1e-7 of a box edge.
 #include "bh_internal.cuh"
+#include "bh_tc.cuh"
 
 namespace bh {
 
 constexpr int FT = FORCE_THREADS;
 constexpr int FAR_CAP = 256;   // far entries per flush
 constexpr int NEAR_CAP = 256;  // near boxes per flush
-constexpr int SRC_CAP = 512;   // near sources per staging pass
+constexpr int SRC_CAP = 384;   // near sources per staging pass
 constexpr int FR_CAP = FRONTIER_CAP;
 constexpr int MAX_TG = 8;
 
@@ -109,9 +110,13 @@ __device__ __forceinline__ int block_scan(int v, int *sh, int *total) {
     return pre;
 }
 
-// bytes per staged near source: the record, or (x, x, y, y) + (m, m) for the packed path
-template <typename R> __host__ __device__ constexpr int src_bytes() {
+// bytes per staged far entry: the record, or (x, x, y, y) + (M, M) for the packed path
+template <typename R> __host__ __device__ constexpr int far_bytes() {
     return sizeof(typename Src<R>::T) > 24 ? (int)sizeof(typename Src<R>::T) : 24;
+}
+// bytes per staged near source: the record, or the 32-byte PD record (x, x, y, y), (m, m, i, 0)
+template <typename R> __host__ __device__ constexpr int src_bytes() {
+    return sizeof(typename Src<R>::T) > 32 ? (int)sizeof(typename Src<R>::T) : 32;
 }
 
 template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT, int MINB>
@@ -121,10 +126,10 @@ k_force(DevPlan d, int tick, int accumulate) {
     // packed FP32 near field (no cutoff test): sources staged as (x, x, y, y) + (m, m)
     constexpr bool PACKED = sizeof(R) == 4 && !TEST && NR % 2 == 0;
     extern __shared__ __align__(16) unsigned char smem[];
-    S *far = reinterpret_cast<S *>(smem);                     // FAR_CAP x src_bytes<R>()
+    S *far = reinterpret_cast<S *>(smem);                     // FAR_CAP x far_bytes<R>()
     float2 *farm = reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(far) + FAR_CAP);
-    S *src = reinterpret_cast<S *>(smem + FAR_CAP * src_bytes<R>());  // SRC_CAP x src_bytes<R>()
-    float2 *srcm = reinterpret_cast<float2 *>(reinterpret_cast<float4 *>(src) + SRC_CAP);
+    S *src = reinterpret_cast<S *>(smem + FAR_CAP * far_bytes<R>());  // SRC_CAP x src_bytes<R>()
+    __shared__ uint64_t s_mbar;  // bulk-copy completion of the near-source staging
     R *red = reinterpret_cast<R *>(smem);                     // aliases far/src at the end
     float2 *nshift = reinterpret_cast<float2 *>(reinterpret_cast<unsigned char *>(src) +
                                                 SRC_CAP * src_bytes<R>());  // NEAR_CAP
@@ -142,6 +147,15 @@ k_force(DevPlan d, int tick, int accumulate) {
     const double *Xs = d.X[nxt], *Ys = d.Y[nxt], *Ms = d.M[nxt];
     const long long nitems = d.item_off[d.NG_total];
     unsigned long long npairs = 0, fpairs = 0;  // counted by thread 0
+    uint32_t tphase = 0;                        // parity of s_mbar's current phase
+    bool tma_ok = true;  // block-uniform; cleared (and flagged) when a staging wait times out
+    if (PACKED) {
+        if (tid == 0) {
+            tc::mbar_init(&s_mbar, 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+    }
 
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(&d.glob->item_next, 1u);
@@ -331,8 +345,76 @@ k_force(DevPlan d, int tick, int accumulate) {
                 if (tid == 0) npre[nn] = total;
             }
             __syncthreads();
-            for (int s0 = 0; s0 < total; s0 += SRC_CAP) {
+            for (int s0 = 0; s0 < total && tma_ok; s0 += SRC_CAP) {
                 const int ns = min(SRC_CAP, total - s0);
+                if (PACKED) {
+                    // Bulk copies (TMA) of the 32-byte PD records of every near-box piece
+                    // that falls into [s0, s0 + ns), all completing on one mbarrier phase.
+                    if (tid == 0) tc::mbar_expect_tx(&s_mbar, (uint32_t)ns * 32u);
+                    tc::fence_async_smem();
+                    unsigned char *sbase = reinterpret_cast<unsigned char *>(src);
+                    for (int k = tid; k < nn; k += FT) {
+                        const int lo = max(npre[k], s0), hi = min(npre[k] + ncnt[k], s0 + ns);
+                        if (lo < hi)
+                            tc::bulk_g2s(sbase + 32 * (lo - s0), d.PD + 2 * (long long)(nbox[k] + (lo - npre[k])),
+                                         (uint32_t)(hi - lo) * 32u, &s_mbar);
+                    }
+                    const bool ok = tc::mbar_wait(&s_mbar, tphase);
+                    tphase ^= 1u;
+                    if (!__syncthreads_and(ok ? 1 : 0)) {
+                        // flagged; give the copies in flight a second bounded wait, then stage
+                        // nothing more in this launch (the barrier phase is no longer known)
+                        if (tid == 0) raise_err(d.glob, 8u /*BH_DEV_WAIT_TIMEOUT*/);
+                        tc::mbar_wait(&s_mbar, tphase ^ 1u);
+                        tma_ok = false;
+                        __syncthreads();
+                        break;
+                    }
+                    // a slice takes an equal contiguous range [j0, j1) of the staged sources and
+                    // walks the boxes it overlaps; each box's shift is folded into the targets
+                    const int per = (ns + nslice - 1) / nslice;
+                    const int j0 = min(ns, slice * per), j1 = min(ns, j0 + per);
+                    if (active && j0 < j1) {
+                        const float4 *s4 = reinterpret_cast<const float4 *>(src);
+                        int k = 0;
+                        {
+                            int hi = nn;  // npre[k] <= s0 + j0 < npre[hi]
+                            while (hi - k > 1) {
+                                const int mid = (k + hi) >> 1;
+                                if (npre[mid] <= s0 + j0) k = mid; else hi = mid;
+                            }
+                        }
+                        for (int lo = j0; lo < j1 && k < nn; k++) {
+                            const int hi = min(npre[k] + ncnt[k] - s0, j1);
+                            if (lo >= hi) continue;
+                            const float2 sh = nshift[k];
+                            const f2_t shx = f2_pack(sh.x, sh.x), shy = f2_pack(sh.y, sh.y);
+                            f2_t bx[NR / 2], by[NR / 2];
+#pragma unroll
+                            for (int kk = 0; kk < NR / 2; kk++) {
+                                bx[kk] = f2_add(ntx2[kk], shx);
+                                by[kk] = f2_add(nty2[kk], shy);
+                            }
+#pragma unroll 2
+                            for (int j = lo; j < hi; j++) {
+                                const ulonglong2 sxy = *reinterpret_cast<const ulonglong2 *>(s4 + 2 * j);
+                                const f2_t mm = *reinterpret_cast<const f2_t *>(s4 + 2 * j + 1);
+#pragma unroll
+                                for (int kk = 0; kk < NR / 2; kk++) {
+                                    f2_t dx = f2_add(sxy.x, bx[kk]), dyy = f2_add(sxy.y, by[kk]);
+                                    f2_t r2 = f2_fma(dx, dx, f2_fma(dyy, dyy, eps2x2));
+                                    f2_t w = f2_mul(mm, f2_rcp(r2));
+                                    nax2[kk] = f2_fma(w, dx, nax2[kk]);
+                                    nay2[kk] = f2_fma(w, dyy, nay2[kk]);
+                                }
+                            }
+                            lo = hi;
+                        }
+                    }
+                    npairs += (unsigned long long)T * ns;
+                    __syncthreads();  // the staging buffer is refilled by the next pass
+                    continue;
+                }
                 for (int j = tid; j < ns; j += FT) {
                     int J = s0 + j;
                     int lo = 0, hi = nn;  // npre[lo] <= J < npre[hi]
@@ -341,13 +423,7 @@ k_force(DevPlan d, int tick, int accumulate) {
                         if (npre[mid] <= J) lo = mid; else hi = mid;
                     }
                     int idx = nbox[lo] + (J - npre[lo]);
-                    if (PACKED) {
-                        float4 p = d.P[idx];
-                        float2 sh = nshift[lo];
-                        float sx = __fadd_rn(sh.x, p.x), sy = __fadd_rn(sh.y, p.y);
-                        reinterpret_cast<float4 *>(src)[j] = make_float4(sx, sx, sy, sy);
-                        srcm[j] = make_float2(p.z, p.z);
-                    } else if (sizeof(R) == 4) {
+                    if (sizeof(R) == 4) {
                         float4 p = d.P[idx];
                         float2 sh = nshift[lo];
                         reinterpret_cast<float4 *>(src)[j] =
@@ -363,23 +439,7 @@ k_force(DevPlan d, int tick, int accumulate) {
                     }
                 }
                 __syncthreads();
-                if (active && PACKED) {
-                    const ulonglong2 *s4 = reinterpret_cast<const ulonglong2 *>(src);
-                    const f2_t *sm2 = reinterpret_cast<const f2_t *>(srcm);
-#pragma unroll 2
-                    for (int j = slice; j < ns; j += nslice) {
-                        const ulonglong2 sxy = s4[j];  // (sx, sx), (sy, sy)
-                        const f2_t mm = sm2[j];        // (m, m)
-#pragma unroll
-                        for (int k = 0; k < NR / 2; k++) {
-                            f2_t dx = f2_add(sxy.x, ntx2[k]), dyy = f2_add(sxy.y, nty2[k]);
-                            f2_t r2 = f2_fma(dx, dx, f2_fma(dyy, dyy, eps2x2));
-                            f2_t w = f2_mul(mm, f2_rcp(r2));
-                            nax2[k] = f2_fma(w, dx, nax2[k]);
-                            nay2[k] = f2_fma(w, dyy, nay2[k]);
-                        }
-                    }
-                } else if (active) {
+                if (active) {
                     for (int j = slice; j < ns; j += nslice) {
                         R sx, sy, sm;
                         int sidx;
@@ -618,14 +678,14 @@ k_force(DevPlan d, int tick, int accumulate) {
 template <typename R>
 static size_t force_smem() {
     using S = typename Src<R>::T;
-    return (size_t)src_bytes<R>() * (FAR_CAP + SRC_CAP) + sizeof(float2) * NEAR_CAP +
+    return (size_t)far_bytes<R>() * FAR_CAP + (size_t)src_bytes<R>() * SRC_CAP + sizeof(float2) * NEAR_CAP +
            sizeof(int) * (3 * NEAR_CAP + 4) + sizeof(int) * 2 * FR_CAP;
 }
 
 template <typename R, int NR, bool KAHAN, bool TEST, bool EXACT,
           int MINB = (sizeof(R) == 4 ? 8 : 4)>
 static cudaError_t launch_force_t(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
-    static_assert(sizeof(R) * 2 * FT * NR <= sizeof(typename Src<R>::T) * (FAR_CAP + SRC_CAP),
+    static_assert(sizeof(R) * 2 * FT * NR <= (size_t)far_bytes<R>() * FAR_CAP + (size_t)src_bytes<R>() * SRC_CAP,
                   "reduction buffer must fit in the staging buffers");
     static_assert(FT * NR >= TARGET_CHUNK, "a CTA must cover every target of a work item");
     auto k = k_force<R, NR, KAHAN, TEST, EXACT, MINB>;

@@ -73,6 +73,8 @@ struct DevPlan {
     int *PID[2];
     double *AX, *AY;  // accelerations, box-sorted order
     float4 *P;
+    float4 *PD;  // per box-sorted particle: (x, x, y, y), (m, m, index, 0) -- the packed
+                 // near-field record, staged into shared memory by bulk copies
     int *key, *slot, *skey;
     int *counts, *box_start, *tile_sums;
     int *item_cnt, *item_off, *item_group;  // force work items (group, target chunk)

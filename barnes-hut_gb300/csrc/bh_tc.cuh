@@ -106,6 +106,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *m, uint32_t phase, int limit
     return false;
 }
 
+// One arrival on mbar that also announces `bytes` of bulk-copy data to wait for.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *m, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes)
+                 : "memory");
+}
+// Bulk copy (TMA, untiled) global -> shared; completes `bytes` on mbar.  dst, src and bytes
+// must be multiples of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *m) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(m))
+        : "memory");
+}
+
 // 32 lanes x 16 consecutive FP32 columns: thread t of the warp gets lane (lane_base + t)
 __device__ __forceinline__ void ld16(uint32_t taddr, float *v) {
     uint32_t r[16];

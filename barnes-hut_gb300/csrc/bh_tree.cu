@@ -298,7 +298,10 @@ __global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
         d.PID[nxt][dst] = d.PID[cur][i];
         float ox = __double2float_rn(__dsub_rn(x, box_origin(dy.minx, kx, dy.step)));
         float oy = __double2float_rn(__dsub_rn(y, box_origin(dy.miny, ky, dy.step)));
-        d.P[dst] = make_float4(ox, oy, __double2float_rn(m), __int_as_float(dst));
+        const float mf = __double2float_rn(m);
+        d.P[dst] = make_float4(ox, oy, mf, __int_as_float(dst));
+        d.PD[2 * (long long)dst] = make_float4(ox, ox, oy, oy);
+        d.PD[2 * (long long)dst + 1] = make_float4(mf, mf, __int_as_float(dst), 0.f);
         d.skey[dst] = key;
     }
 }

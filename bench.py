@@ -65,6 +65,23 @@ def dist_setup():
     return ws, rank, local
 
 
+def replica_seed(rank):
+    """Seed of the batch a replica steps: every rank draws its own system."""
+    return SEED + rank
+
+
+def max_over_ranks(seconds, ws, device):
+    """The slowest rank's time (the job finishes when it does); ws == 1 returns it as is.
+    Works with any process-group backend whose all_reduce accepts tensors on `device`."""
+    if ws <= 1:
+        return float(seconds)
+    import torch
+
+    t = torch.tensor([float(seconds)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
 
@@ -255,6 +272,99 @@ def learned_benchmark(torch, dev, batch, plain_step_s, plain_acc, steps=20):
     return res
 
 
+def precision_study(torch, dev, batch, thetas=(0.3, 0.5, 0.7), reps=3):
+    """Force error of FP32 naive, FP32 with Kahan far field and FP64 pair arithmetic against
+    the FP64 direct sum on 16,384 seeded targets of the bench's N = 4,194,304 batch (512 x 512
+    boxes), at each opening angle, with the evaluate time (median of `reps` launches)."""
+    from barneshut.gb300 import native, workloads
+
+    n = batch[0].numel()
+    tgt = workloads.precision_subsample(n, 16384, seed=SEED)
+    idx = torch.as_tensor(tgt, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ref = None
+    out = {"targets": len(tgt), "n": n, "grid": GRID}
+    for theta in thetas:
+        row = {}
+        for name, prec in (("fp32", native.BH_PREC_FP32), ("fp32_kahan", native.BH_PREC_FP32_KAHAN),
+                           ("fp64", native.BH_PREC_FP64)):
+            prm = native.make_params(1.0, DT, SOFTENING, 0.0, theta, 0, prec, 0, 0)
+            plan = native.Plan([n], [GRID], prm, device=dev)
+            plan.load(*batch)
+            plan.create_tree()
+            plan.summarize()
+            ms = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                plan.evaluate()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            # evaluate accumulates into a: one clean pass for the error and the pair counts
+            plan.load(*batch)
+            plan.create_tree()
+            plan.summarize()
+            plan.evaluate()
+            o = plan.store()
+            if ref is None:
+                ref = plan.direct_sample(tgt)
+            dax, day = ref
+            ax, ay = o["ax"][idx], o["ay"][idx]
+            num = ((ax - dax) ** 2 + (ay - day) ** 2).sum()
+            mag = torch.sqrt(dax ** 2 + day ** 2)
+            rel = torch.sqrt((ax - dax) ** 2 + (ay - day) ** 2) / mag
+            near, far = plan.pair_counts()
+            row[name] = {"rel_rms": float(torch.sqrt(num / (mag ** 2).sum())),
+                         "rel_max": float(rel.max()), "evaluate_ms": sorted(ms)[len(ms) // 2],
+                         "pairs_near": near, "pairs_far": far,
+                         "device_error_flags": plan.error_flags(raise_on_error=False)}
+            plan.close()
+        out[f"theta_{theta}"] = row
+    return out
+
+
+def free_run(torch, dev, steps=100):
+    """N = 1,048,576 cluster mixture (seed 1), 256 x 256 boxes, theta 0.5, softening 1e-4,
+    dt 1e-5, FP32 + Kahan: `steps` free-running steps in one CUDA graph, with FP64 kinetic
+    energy and momentum before and after (the ln-potential diagnostic is O(N^2) and is left
+    out at this size)."""
+    import numpy as np
+
+    from barneshut.gb300 import native, workloads
+
+    x, y, m, vx, vy = workloads.cluster_mixture(1 << 20, seed=1)
+    n = len(x)
+    prm = native.make_params(1.0, 1e-5, 1e-4, 0.0, 0.5, 0, native.BH_PREC_FP32_KAHAN, 0, 0)
+    plan = native.Plan([n], [256], prm, device=dev)
+    plan.load(x, y, m, vx, vy)
+    plan.step_graph(3)  # graph capture and warm-up
+    plan.load(x, y, m, vx, vy)
+    torch.cuda.synchronize()
+    ke0, px0, py0, _ = plan.diagnostics()
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    plan.step_graph(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    ke1, px1, py1, _ = plan.diagnostics()
+    o = plan.store()
+    msum = float(np.sum(m))
+    speed = torch.sqrt(o["vx"] ** 2 + o["vy"] ** 2)
+    mv = float((torch.as_tensor(m, device=dev) * speed).sum())
+    res = {"metric": "particle-steps/s, N=1M free-running", "value": n * steps / t,
+           "ms_per_step": 1e3 * t / steps, "steps": steps, "n": n, "grid": 256,
+           "graph": f"{steps} steps in one CUDA graph",
+           "kinetic_energy": [ke0, ke1],
+           "momentum_drift_over_sum_m_abs_v": float(np.hypot(px1 - px0, py1 - py0) / mv) if mv > 0 else None,
+           "total_mass": msum,
+           "device_error_flags": plan.error_flags(raise_on_error=False)}
+    plan.close()
+    return res
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -299,7 +409,7 @@ def main():
         dist.init_process_group("nccl", device_id=dev)
     from barneshut.gb300 import native, workloads
 
-    x, y, m, vx, vy = workloads.cluster_mixture(args.n, seed=SEED + rank)
+    x, y, m, vx, vy = workloads.cluster_mixture(args.n, seed=replica_seed(rank))
     # batch in box order (the state's order between steps of a running simulation)
     order = workloads.box_order(x, y, args.grid)
     x, y, m, vx, vy = (a[order].copy() for a in (x, y, m, vx, vy))
@@ -345,11 +455,7 @@ def main():
     if ws > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    t_dev = e0.elapsed_time(e1) / 1e3
-    if ws > 1:
-        t = torch.tensor([t_dev], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
+    t_dev = max_over_ranks(e0.elapsed_time(e1) / 1e3, ws, dev)
     value = ws * args.n * K / t_dev
     flags = plan.error_flags(raise_on_error=False)
     kernels_per_step = plan.kernels_per_step()
@@ -402,9 +508,11 @@ def main():
             h.copy_(outs[k], non_blocking=True)
     g1.record(stream)
     torch.cuda.synchronize()
-    t_e2e = g0.elapsed_time(g1) / 1e3 / e2e_steps
-    e2e = {"value": args.n / t_e2e, "unit": "particle-steps/s",
-           "h2d_bytes_per_step": 5 * 8 * args.n, "d2h_bytes_per_step": 6 * 8 * args.n,
+    if ws > 1:
+        torch.distributed.barrier()
+    t_e2e = max_over_ranks(g0.elapsed_time(g1) / 1e3 / e2e_steps, ws, dev)
+    e2e = {"value": ws * args.n / t_e2e, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": ws * 5 * 8 * args.n, "d2h_bytes_per_step": ws * 6 * 8 * args.n,
            "ms_per_step": 1e3 * t_e2e,
            "path": "pinned host arrays -> bh_load -> bh_step_graph(1) -> bh_store -> pinned host"}
 
@@ -429,6 +537,8 @@ def main():
     side = {}
     if not args.quick and rank == 0:
         side["batched"] = batched_benchmark(torch, dev)
+        side["free_run_1m"] = free_run(torch, dev)
+        side["precision"] = precision_study(torch, dev, batch)
         side["learned"] = learned_benchmark(torch, dev, batch, t_dev / K, acc)
 
     cpu = None
