@@ -29,6 +29,7 @@ BH_PREC_FP32_KAHAN = 1
 BH_PREC_FP64 = 2
 
 BH_FLAG_LEARNED = 1
+BH_FLAG_WALK = 2
 
 # every symbol include/bh_gb300.h declares
 EXPORTS = (

@@ -5,6 +5,7 @@
 // caller binds one workspace buffer.  Kernels read the plan's device tables
 // and a device-side epoch that selects the current state buffer, so a step
 // captured into a CUDA graph replays correctly.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -29,7 +30,9 @@ struct bh_plan {
     size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
     size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_tiles, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
-        o_rec2;
+        o_rec2, o_lfar, o_lnear, o_lcnt;
+    bool stream = false;  // theta-mode interaction lists built once per group and streamed
+    int chunk = TARGET_CHUNK;
     void *ws = nullptr;
     int device = -1;
     DevPlan dev;
@@ -168,6 +171,28 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
         if (L > p->Lmax) p->Lmax = L;
     }
     p->n_total = p->poff[nsys];
+    // list-streaming force path: theta mode, FP32 pairs, softening > 0, no cutoff, G <= 16384
+    int maxG = 0;
+    for (int s = 0; s < nsys; s++) maxG = std::max(maxG, p->sys[s].G);
+    p->stream = !flat && pr.precision != BH_PREC_FP64 && pr.cutoff_r2 == 0.0 && pr.softening > 0.0 &&
+                !(pr.flags & BH_FLAG_WALK) && maxG <= LIST_MAX_G;
+    p->chunk = p->stream ? STREAM_CHUNK : TARGET_CHUNK;
+    long long lf_total = 0, ln_total = 0;
+    if (p->stream) {
+        // a level's accepted cells are a subset of its frontier (at most FRONTIER_CAP cells), and
+        // the near boxes a subset of the leaf level's frontier
+        for (int s = 0; s < nsys; s++) {
+            SysDesc &d = p->sys[s];
+            long long cap = 0;
+            for (int l = 0; l < d.L; l++) cap += std::min<long long>(FRONTIER_CAP, (long long)d.lvg[l] * d.lvg[l]);
+            d.lfcap = (int)cap;
+            d.lncap = (int)std::min<long long>(FRONTIER_CAP, (long long)d.G * d.G);
+            d.lfoff = lf_total;
+            d.lnoff = ln_total;
+            lf_total += (long long)d.NGs * d.NGs * d.lfcap;
+            ln_total += (long long)d.NGs * d.NGs * (d.lncap + 1);
+        }
+    }
     p->B_total = p->boff[nsys];
     p->C_total = p->coff[nsys];
     p->NG_total = p->goff[nsys];
@@ -216,7 +241,10 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_tiles = take(4 * (B / 4096 + 2));
     p->o_icnt = take(4 * (size_t)p->NG_total);
     p->o_ioff = take(4 * ((size_t)p->NG_total + 1));
-    p->o_igrp = take(4 * ((size_t)p->NG_total + N / TARGET_CHUNK + 1));
+    p->o_igrp = take(4 * ((size_t)p->NG_total + N / p->chunk + 1));
+    p->o_lfar = take(4 * (size_t)lf_total);
+    p->o_lnear = take(16 * (size_t)ln_total);
+    p->o_lcnt = take(p->stream ? 8 * (size_t)p->NG_total : 0);
     p->o_mom = take(48 * C);
     p->o_rec = take(16 * C);
     p->o_rec2 = take(16 * C);
@@ -284,6 +312,11 @@ static void fill_dev(bh_plan *p) {
     d.mom = (double *)(w + p->o_mom);
     d.rec = (float4 *)(w + p->o_rec);
     d.rec2 = (float4 *)(w + p->o_rec2);
+    d.lfar = (int *)(w + p->o_lfar);
+    d.lnear = (int4 *)(w + p->o_lnear);
+    d.lcnt = (int2 *)(w + p->o_lcnt);
+    d.stream = p->stream ? 1 : 0;
+    d.chunk = p->chunk;
     const bh_params &pr = p->params;
     d.gconst = pr.grav_constant;
     d.dt = pr.tick_seconds;
@@ -486,8 +519,8 @@ extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     if (!p || !count) return BH_ERR_INVALID;
     // prologue, 3 box-scan phases, work items (count, 3 scan phases, fill),
     // pyramid levels 1..Lmax-1, records; with particles also bbox, bbox
-    // finalize, place, scatter, leaf moments, force
-    *count = 1 + 3 + 5 + (p->Lmax - 1) + 1 + (p->n_total > 0 ? 6 : 0);
+    // finalize, place, scatter, leaf moments, force (and the list build before it)
+    *count = 1 + 3 + 5 + (p->Lmax - 1) + 1 + (p->n_total > 0 ? 6 : 0) + (p->stream && p->n_total > 0 ? 1 : 0);
     return BH_OK;
 }
 

@@ -21,64 +21,18 @@
 // contributions Kahan-compensated when requested; BH_PREC_FP64 runs the same lists in FP64.
 // Positions are box-relative offsets rounded once from FP64, so dx keeps ~1e-7 of a box edge.
 #include "bh_internal.cuh"
+#include "bh_pairs.cuh"
 #include "bh_tc.cuh"
 
 namespace bh {
-
-constexpr int FT = FORCE_THREADS;
-constexpr int FAR_CAP = 256;   // far entries per flush
-constexpr int NEAR_CAP = 256;  // near boxes per flush
-constexpr int SRC_CAP = 384;   // near sources per staging pass
-constexpr int FR_CAP = FRONTIER_CAP;
-constexpr int MAX_TG = 8;
 
 template <typename R> struct Src;
 template <> struct Src<float> { using T = float4; };
 template <> struct Src<double> { struct T { double x, y, m; int idx, pad; }; };
 
-__device__ __forceinline__ float rcp_approx(float x) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
 template <typename R> __device__ __forceinline__ R rinv(R x);
 template <> __device__ __forceinline__ float rinv<float>(float x) { return rcp_approx(x); }
 template <> __device__ __forceinline__ double rinv<double>(double x) { return 1.0 / x; }
-
-// Packed FP32 pairs (sm_100-family f32x2 instructions): two lanes of work per instruction.
-typedef unsigned long long f2_t;
-__device__ __forceinline__ f2_t f2_pack(float a, float b) {
-    f2_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void f2_unpack(f2_t v, float &a, float &b) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b) {
-    f2_t r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
-    f2_t r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
-    f2_t r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-__device__ __forceinline__ f2_t f2_rcp(f2_t a) {
-    f2_t r;
-    asm("{\n.reg .f32 a0, a1, r0, r1;\nmov.b64 {a0, a1}, %1;\nrcp.approx.ftz.f32 r0, a0;\n"
-        "rcp.approx.ftz.f32 r1, a1;\nmov.b64 %0, {r0, r1};\n}"
-        : "=l"(r)
-        : "l"(a));
-    return r;
-}
 
 __device__ __forceinline__ void src_get(const float4 &e, float &x, float &y, float &m, int &idx) {
     x = e.x; y = e.y; m = e.z; idx = __float_as_int(e.w);
@@ -88,27 +42,6 @@ __device__ __forceinline__ void src_get(const Src<double>::T &e, double &x, doub
     x = e.x; y = e.y; m = e.m; idx = e.idx;
 }
 
-// Exclusive block scan of one int per thread; *total = block sum.
-__device__ __forceinline__ int block_scan(int v, int *sh, int *total) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    int x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) sh[w] = x;
-    __syncthreads();
-    int pre = x - v, tot = 0;
-    for (int k = 0; k < nw; k++) {
-        int s = sh[k];
-        if (k < w) pre += s;
-        tot += s;
-    }
-    *total = tot;
-    __syncthreads();
-    return pre;
-}
 
 // bytes per staged far entry: the record, or (x, x, y, y) + (M, M) for the packed path
 template <typename R> __host__ __device__ constexpr int far_bytes() {
@@ -190,8 +123,8 @@ k_force(DevPlan d, int tick, int accumulate) {
         int nfar = 0, nnear = 0, nnext = 0;
         bool ovf = false;
         const int nt = s_colpre[ncol];
-        const int c0 = chunk * TARGET_CHUNK;
-        const int T = min(TARGET_CHUNK, nt - c0);
+        int c0, T;
+        item_range(nt, d.item_cnt[g], chunk, &c0, &T);
         const float step_f = __double2float_rn(dy.step);
         const float W_f = __fmul_rn((float)TG, step_f);
         const double gox = box_origin(dy.minx, gx0, dy.step), goy = box_origin(dy.miny, gy0, dy.step);
@@ -690,7 +623,7 @@ static cudaError_t launch_force_t(const DevPlan &d, bool tick, bool accumulate, 
     static_assert(FT * NR >= TARGET_CHUNK, "a CTA must cover every target of a work item");
     auto k = k_force<R, NR, KAHAN, TEST, EXACT, MINB>;
     size_t sm = force_smem<R>();
-    long long items_max = d.NG_total + d.n_total / TARGET_CHUNK + 1;
+    long long items_max = d.NG_total + d.n_total / d.chunk + 1;
     long long grid = 152LL * MINB;
     if (grid > items_max) grid = items_max;
     if (grid < 1) grid = 1;
@@ -711,6 +644,7 @@ static cudaError_t init_force_t() {
 // any stream capture).
 cudaError_t force_init() {
     cudaError_t e;
+    if ((e = fstream_init()) != cudaSuccess) return e;
     if ((e = init_force_t<double, FORCE_R, false, true, false>()) != cudaSuccess) return e;
     if ((e = init_force_t<double, FORCE_R, false, false, false>()) != cudaSuccess) return e;
     if ((e = init_force_t<float, FORCE_R, true, true, true>()) != cudaSuccess) return e;
@@ -725,6 +659,11 @@ cudaError_t force_init() {
 
 cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
+    if (d.stream) {  // prebuilt interaction lists, streamed (bh_lists.cu, bh_fstream.cu)
+        cudaError_t e = launch_lists(d, st);
+        if (e != cudaSuccess) return e;
+        return launch_fstream(d, tick, accumulate, st);
+    }
     const bool test = d.cutoff > 0.0 || d.eps2 == 0.0;
     const bool exact = d.cutoff > 0.0;
     if (d.prec == 2) {

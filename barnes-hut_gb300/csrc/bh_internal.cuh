@@ -32,6 +32,8 @@ constexpr int FORCE_THREADS = 128;
 constexpr int FORCE_R = 4;                                   // targets per thread (FP32)
 constexpr int TARGET_CHUNK = FORCE_THREADS * FORCE_R;        // targets per work item
 constexpr int FRONTIER_CAP = 512;                            // traversal frontier per level
+constexpr int STREAM_CHUNK = 128;  // targets per work item of the list-streaming force kernel
+constexpr int LIST_MAX_G = 16384;  // far-list codes hold (level, cell) in 4 + 28 bits
 
 struct SysDesc {
     long long n, poff;  // particle count, first particle (concatenated)
@@ -41,6 +43,8 @@ struct SysDesc {
     int G, L, TG, NGs;  // boxes per side, pyramid levels, group dim, groups per side
     int lvg[MAX_LEVELS];         // cells per side per level
     long long lvoff[MAX_LEVELS]; // first cell of each level, relative to coff
+    long long lfoff, lnoff;      // first far / near list slot of the system's groups
+    int lfcap, lncap;            // far / near list slots per group
 };
 
 struct SysDyn {
@@ -80,6 +84,17 @@ struct DevPlan {
     int *item_cnt, *item_off, *item_group;  // force work items (group, target chunk)
     double *mom;
     float4 *rec, *rec2;
+    // interaction lists of every target group (list-streaming path), in fixed per-group slots
+    // (SysDesc lfcap far codes, lncap + 1 near descriptors), counts in lcnt (x far, y near):
+    //   far code: level << 28 | cell index within the level;
+    //   near descriptor: (first particle, exclusive prefix of the boxes' particle counts, shift
+    //   of the box origin from the group origin as float bits x, y); entry [count] carries the
+    //   total in .y
+    int *lfar;
+    int4 *lnear;
+    int2 *lcnt;
+    int stream;  // 1: lists are built by k_lists and streamed by k_fstream
+    int chunk;   // targets per work item (TARGET_CHUNK, or STREAM_CHUNK when stream)
     // parameters
     double gconst, dt, eps2, cutoff;
     float theta2_f, eps2_f, cut_f;
@@ -146,6 +161,14 @@ __device__ __forceinline__ double box_origin(double mn, int k, double step) {
     return __dadd_rn(mn, __dmul_rn((double)k, step));
 }
 
+// Targets [c0, c0 + T) of work item k of a group whose nt targets are split into nch items of
+// near-equal size (each at most ceil(nt / nch)).
+__device__ __forceinline__ void item_range(int nt, int nch, int k, int *c0, int *T) {
+    const int a = (int)((long long)k * nt / nch), b = (int)((long long)(k + 1) * nt / nch);
+    *c0 = a;
+    *T = b - a;
+}
+
 __device__ __forceinline__ void raise_err(Globals *g, unsigned f) {
     if ((atomicOr(&g->err, 0u) & f) == 0) atomicOr(&g->err, f);
 }
@@ -162,6 +185,9 @@ cudaError_t launch_items(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st);
+cudaError_t launch_lists(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_fstream(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st);
+cudaError_t fstream_init();
 cudaError_t force_init();
 cudaError_t launch_tick(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_load(const DevPlan &d, const double *x, const double *y, const double *m,

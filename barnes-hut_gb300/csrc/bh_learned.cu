@@ -78,8 +78,7 @@ __device__ __forceinline__ void item_geom(const DevPlan &d, long long g, int chu
     }
     __syncthreads();
     ig.nt = colpre[ig.ncol];
-    ig.c0 = chunk * TARGET_CHUNK;
-    ig.T = min(TARGET_CHUNK, ig.nt - ig.c0);
+    item_range(ig.nt, d.item_cnt[g], chunk, &ig.c0, &ig.T);
 }
 
 __device__ __forceinline__ int item_target(const ItemGeom &ig, const int *col0, const int *colpre,
@@ -461,7 +460,7 @@ cudaError_t launch_learned_correct(const DevPlan &d, double theta_lo, const uint
     if (d.n_total == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(&d.glob->item_next2, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    long long items_max = d.NG_total + d.n_total / TARGET_CHUNK + 1;
+    long long items_max = d.NG_total + d.n_total / d.chunk + 1;
     long long grid = 152LL * 2;
     if (grid > items_max) grid = items_max;
     k_learned_correct<<<(unsigned)grid, LT, LSmem::TOTAL + 1024, st>>>(

@@ -1,0 +1,156 @@
+// bh_lists.cu -- interaction lists of every target group, for the list-streaming force kernel.
+//
+// The reference evaluates every box against its 3 x 3 neighbourhood and the centre of mass of
+// every other box (kernels/grid_decomposition/gpu/grid.py:116-157,
+// sequential/evaluation.py:73-109); in theta mode this project replaces the flat far field with
+// a walk of the cell pyramid, and this kernel does that walk once per target group instead of
+// once per work item.  One CTA per group (grid-stride over groups) walks the pyramid level by
+// level: every thread tests one frontier cell; a cell whose centre of mass lies at distance d
+// from the group's box rectangle is accepted when s^2 < theta^2 d^2 (s = cell edge) and goes to
+// the far list, a rejected leaf goes to the near list, any other rejected cell opens into its
+// children.  A block scan places every thread's entries, so list order is deterministic.  The
+// test is the same FP32 arithmetic the walking force kernel uses, so both paths accept the same
+// cells.
+//
+// Output per group g of system s: far codes (level << 28 | cell index within the level) at
+// lfar[s.lfoff + lg * s.lfcap ..]; near descriptors (first particle, exclusive prefix of the
+// boxes' particle counts, box-origin shift in the group frame) at lnear[s.lnoff + lg * (s.lncap
+// + 1) ..] with the total in entry [count]; lcnt[g] = (far count, near count).  The slots are
+// sized on the host so that a level's accepted cells never exceed FRONTIER_CAP; the kernel still
+// checks and raises BH_DEV_LIST_OVERFLOW.
+#include "bh_internal.cuh"
+#include "bh_pairs.cuh"
+
+namespace bh {
+
+constexpr int LT = 128;  // threads per list-building CTA
+
+__global__ void __launch_bounds__(LT) k_lists(DevPlan d) {
+    __shared__ int front[2][FR_CAP];
+    __shared__ int s_near[FR_CAP];  // near box ids (local to the system) in list order
+    __shared__ int sh_scan[32];
+    const int tid = threadIdx.x;
+    const float theta2 = d.theta2_f;
+    for (long long g = blockIdx.x; g < d.NG_total; g += gridDim.x) {
+        const int s = find_seg(d.goff_tab, d.nsys, g);
+        const SysDesc &sd = d.sys[s];
+        const SysDyn &dy = d.dyn[s];
+        const long long lg = g - sd.goff;
+        const int TG = sd.TG;
+        const int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
+        const int gx0 = gi * TG, gy0 = gj * TG;
+        const int gx1 = min(sd.G, gx0 + TG), gy1 = min(sd.G, gy0 + TG);
+        const float step_f = __double2float_rn(dy.step);
+        const float W_f = __fmul_rn((float)TG, step_f);
+        int *far_out = d.lfar + sd.lfoff + lg * sd.lfcap;
+        int4 *near_out = d.lnear + sd.lnoff + lg * (sd.lncap + 1);
+        int nfar = 0, nnear = 0, nfr = 1, cur = 0;
+        bool ovf = false;
+        if (tid == 0) front[0][0] = 0;
+        for (int l = sd.L - 1; l >= 0 && nfr > 0; l--) {
+            const int gl = sd.lvg[l];
+            const int gc = l > 0 ? sd.lvg[l - 1] : 0;
+            const float s_f = ldexpf(step_f, l);
+            const float s2 = __fmul_rn(s_f, s_f);
+            int nnext = 0;
+            __syncthreads();  // this level's frontier is visible
+            const int *fr = front[cur];
+            int *fn = front[cur ^ 1];
+            for (int q0 = 0; q0 < nfr; q0 += LT) {
+                const int q = q0 + tid;
+                int kind = 0, ci = 0, cj = 0, loc = 0;
+                if (q < nfr) {
+                    loc = fr[q];
+                    if ((unsigned)loc >= (unsigned)(gl * gl)) {
+                        raise_err(d.glob, 4u /*BH_DEV_BAD_KEY*/);  // never expected: skip it
+                    } else {
+                        ci = loc / gl;
+                        cj = loc - ci * gl;
+                        const float4 rr = d.rec[sd.coff + sd.lvoff[l] + loc];
+                        if (rr.z > 0.f) {
+                            const int lo_x = ci << l, hi_x = (ci + 1) << l;
+                            const int lo_y = cj << l, hi_y = (cj + 1) << l;
+                            const bool overlap = lo_x < gx1 && hi_x > gx0 && lo_y < gy1 && hi_y > gy0;
+                            bool accept = false;
+                            if (!overlap) {
+                                const float rx = __fadd_rn(__fmul_rn((float)(lo_x - gx0), step_f), rr.x);
+                                const float ry = __fadd_rn(__fmul_rn((float)(lo_y - gy0), step_f), rr.y);
+                                const float dxo = fmaxf(0.f, fmaxf(-rx, __fsub_rn(rx, W_f)));
+                                const float dyo = fmaxf(0.f, fmaxf(-ry, __fsub_rn(ry, W_f)));
+                                const float d2 = __fadd_rn(__fmul_rn(dxo, dxo), __fmul_rn(dyo, dyo));
+                                accept = s2 < __fmul_rn(theta2, d2);
+                            }
+                            kind = accept ? 1 : (l == 0 ? 2 : 3);
+                        }
+                    }
+                }
+                int nch = 0;
+                if (kind == 3) nch = (2 * ci + 1 < gc ? 2 : 1) * (2 * cj + 1 < gc ? 2 : 1);
+                const int packed = (kind == 1 ? 1 : 0) | ((kind == 2 ? 1 : 0) << 10) | (nch << 20);
+                int tot;
+                const int pre = block_scan(packed, sh_scan, &tot);
+                if (kind == 1) {
+                    const int pos = nfar + (pre & 1023);
+                    if (pos < sd.lfcap) far_out[pos] = (int)(((unsigned)l << 28) | (unsigned)loc);
+                } else if (kind == 2) {
+                    const int pos = nnear + ((pre >> 10) & 1023);
+                    if (pos < sd.lncap) s_near[pos] = loc;
+                } else if (kind == 3) {
+                    int pos = nnext + (pre >> 20);
+                    if (pos + nch <= FR_CAP) {
+                        for (int a = 0; a < 2; a++)
+                            for (int b = 0; b < 2; b++)
+                                if (2 * ci + a < gc && 2 * cj + b < gc) fn[pos++] = (2 * ci + a) * gc + (2 * cj + b);
+                    }
+                }
+                nfar += tot & 1023;
+                nnear += (tot >> 10) & 1023;
+                if (nnext + (tot >> 20) > FR_CAP) ovf = true;
+                nnext += tot >> 20;
+            }
+            cur ^= 1;
+            // an overflowed frontier may hold unwritten slots: abandon the walk (flagged)
+            nfr = ovf ? 0 : nnext;
+        }
+        // near descriptors: first particle, exclusive prefix of the particle counts, box shift
+        const int nn = min(nnear, sd.lncap);
+        __syncthreads();  // s_near is complete
+        {
+            int base = 0;
+            for (int k0 = 0; k0 <= nn; k0 += LT) {
+                const int k = k0 + tid;
+                int st = 0, c = 0, loc = 0;
+                if (k < nn) {
+                    loc = s_near[k];
+                    st = d.box_start[sd.boff + loc];
+                    c = d.box_start[sd.boff + loc + 1] - st;
+                }
+                int tot;
+                const int pre = block_scan(c, sh_scan, &tot) + base;
+                if (k < nn) {
+                    const int kx = loc / sd.G, ky = loc - kx * sd.G;
+                    near_out[k] = make_int4(st, pre, __float_as_int(__fmul_rn((float)(kx - gx0), step_f)),
+                                            __float_as_int(__fmul_rn((float)(ky - gy0), step_f)));
+                } else if (k == nn) {
+                    near_out[k] = make_int4(0, pre, 0, 0);
+                }
+                base += tot;
+            }
+        }
+        if (tid == 0) {
+            if (ovf || nfar > sd.lfcap || nnear > sd.lncap) raise_err(d.glob, 2u /*BH_DEV_LIST_OVERFLOW*/);
+            d.lcnt[g] = make_int2(min(nfar, sd.lfcap), nn);
+        }
+        __syncthreads();  // front[] and s_near are rewritten for the next group
+    }
+}
+
+cudaError_t launch_lists(const DevPlan &d, cudaStream_t st) {
+    if (d.NG_total == 0) return cudaSuccess;
+    long long grid = 152LL * 16;
+    if (grid > d.NG_total) grid = d.NG_total;
+    k_lists<<<(unsigned)grid, LT, 0, st>>>(d);
+    return cudaGetLastError();
+}
+
+}  // namespace bh

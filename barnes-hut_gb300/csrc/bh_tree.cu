@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(TPB) k_group_items(DevPlan d) {
             long long b0 = sd.boff + (long long)c * sd.G + gy0;
             nt += d.box_start[b0 + (gy1 - gy0)] - d.box_start[b0];
         }
-        d.item_cnt[g] = (nt + TARGET_CHUNK - 1) / TARGET_CHUNK;
+        d.item_cnt[g] = (nt + d.chunk - 1) / d.chunk;
     }
 }
 

@@ -51,6 +51,10 @@ extern "C" {
 
 /* bh_params.flags */
 #define BH_FLAG_LEARNED 1 /* apply the learned far-field correction (weights bound) */
+#define BH_FLAG_WALK 2    /* theta mode: walk the cell pyramid inside the force kernel for
+                           every work item instead of building each target group's
+                           interaction lists once and streaming them (the default for
+                           FP32 pairs with softening > 0, no cutoff and grid_dim <= 16384) */
 
 typedef struct bh_params {
     double grav_constant; /* [bh] grav_constant (python-bh/configs/default.ini) */

@@ -163,14 +163,21 @@ def test_unfused_phases_equal_fused():
 # ---------------------------------------------------------------- theta mode
 @pytest.mark.parametrize("theta,TG,G", [(0.3, 1, 16), (0.5, 2, 16), (0.5, 4, 19), (0.8, 2, 32)])
 @pytest.mark.parametrize("prec", [0, 1, 2])
-def test_theta_vs_fp64_oracle(theta, TG, G, prec):
+@pytest.mark.parametrize("walk", [False, True], ids=["lists", "walk"])
+def test_theta_vs_fp64_oracle(theta, TG, G, prec, walk):
+    """Both theta-mode force paths -- interaction lists built once per group and streamed (the
+    default for FP32 pairs), and the pyramid walk inside the force kernel (BH_FLAG_WALK; always
+    used for FP64 pairs) -- against the FP64 oracle with the same opening rule."""
     from barneshut.gb300 import workloads
     from oracle import oracle
 
+    if walk and prec == 2:
+        pytest.skip("FP64 pairs always walk")
     x, y, m, vx, vy = workloads.cluster_mixture(20000, seed=31)
     eps = 1e-3
     plan = make_plan(20000, G, grav_constant=1.0, tick_seconds=1e-5, softening=eps, cutoff_r2=0.0,
-                     theta=theta, group_dim=TG, precision=prec)
+                     theta=theta, group_dim=TG, precision=prec,
+                     flags=native().BH_FLAG_WALK if walk else 0)
     plan.load(x, y, m, vx, vy)
     plan.create_tree()
     plan.summarize()
