@@ -30,7 +30,7 @@ struct bh_plan {
     size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
     size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_tiles, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
-        o_rec2, o_lfar, o_lnear, o_lcnt;
+        o_rec2, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt;
     bool stream = false;  // theta-mode interaction lists built once per group and streamed
     int chunk = TARGET_CHUNK;
     void *ws = nullptr;
@@ -245,6 +245,8 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_lfar = take(4 * (size_t)lf_total);
     p->o_lnear = take(16 * (size_t)ln_total);
     p->o_lcnt = take(p->stream ? 8 * (size_t)p->NG_total : 0);
+    p->o_iord = take(p->stream ? 4 * ((size_t)p->NG_total + N / p->chunk + 1) : 0);
+    p->o_ibkt = take(p->stream ? 4 * 2 * ITEM_BUCKETS : 0);
     p->o_mom = take(48 * C);
     p->o_rec = take(16 * C);
     p->o_rec2 = take(16 * C);
@@ -315,6 +317,8 @@ static void fill_dev(bh_plan *p) {
     d.lfar = (int *)(w + p->o_lfar);
     d.lnear = (int4 *)(w + p->o_lnear);
     d.lcnt = (int2 *)(w + p->o_lcnt);
+    d.item_order = (int *)(w + p->o_iord);
+    d.item_bucket = (int *)(w + p->o_ibkt);
     d.stream = p->stream ? 1 : 0;
     d.chunk = p->chunk;
     const bh_params &pr = p->params;
@@ -519,8 +523,9 @@ extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     if (!p || !count) return BH_ERR_INVALID;
     // prologue, 3 box-scan phases, work items (count, 3 scan phases, fill),
     // pyramid levels 1..Lmax-1, records; with particles also bbox, bbox
-    // finalize, place, scatter, leaf moments, force (and the list build before it)
-    *count = 1 + 3 + 5 + (p->Lmax - 1) + 1 + (p->n_total > 0 ? 6 : 0) + (p->stream && p->n_total > 0 ? 1 : 0);
+    // finalize, place, scatter, leaf moments, force (and before it the list build and the
+    // two kernels of the heaviest-first item order)
+    *count = 1 + 3 + 5 + (p->Lmax - 1) + 1 + (p->n_total > 0 ? 6 : 0) + (p->stream && p->n_total > 0 ? 3 : 0);
     return BH_OK;
 }
 

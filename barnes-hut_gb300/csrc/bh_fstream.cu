@@ -6,18 +6,22 @@
 // The interaction lists come from k_lists (one pyramid walk per target group); this kernel only
 // streams them.
 //
-// Work items are a group's targets split into near-equal chunks of at most STREAM_CHUNK, pulled
-// from a device queue.  Per item:
+// One warp owns one work item at a time (a group's targets split into near-equal chunks of at
+// most STREAM_CHUNK, pulled from a device queue); the warps of a CTA share nothing but the CTA's
+// shared memory carve-up, so there is no CTA-wide barrier and a warp waiting on memory leaves
+// the SM to the other warps.  Per item:
 //   * far field: the group's far codes are decoded (level, cell -> record; centre of mass shifted
-//     into the group frame) into shared memory as packed (x, x, y, y) + (M, M) entries, FAR_CAP
-//     at a time, and swept with Kahan compensation;
+//     into the group frame) into the warp's staging as packed (x, x, y, y) + (M, M) entries,
+//     WFAR at a time, and swept; each pass's plain FP32 sum enters the running total through a
+//     Kahan-compensated addition (BH_PREC_FP32_KAHAN) or a plain one (BH_PREC_FP32);
 //   * near field: the near boxes' 32-byte packed records (x, x, y, y), (m, m, index, 0) are copied
-//     box by box into shared memory by bulk asynchronous copies (TMA) completing on one mbarrier,
-//     SRC_CAP sources per pass, and swept box piece by box piece with the piece's shift folded
-//     into the targets (the slices split every piece, so the CTA's warps stay converged).
-// Each thread owns FORCE_R targets as two packed pairs (one f32x2 instruction serves two targets);
-// the CTA's threads form slices that sweep disjoint parts of every staged list, and the slice
-// partials are reduced in shared memory before the FP64 write-back and the fused tick.
+//     box piece by box piece into the warp's staging by bulk asynchronous copies (TMA), WSRC
+//     sources per pass, double-buffered on two mbarriers so the copy of pass p + 1 overlaps the
+//     sweep of pass p; the lanes shift each staged source from its box frame into the group
+//     frame in place before the sweep.
+// Each lane owns FORCE_R targets as two packed pairs (one f32x2 instruction serves two targets);
+// the lanes form slices that split every staged list; slice partials are reduced through the
+// warp's staging before the FP64 write-back and the fused tick.
 #include "bh_internal.cuh"
 #include "bh_pairs.cuh"
 #include "bh_tc.cuh"
@@ -25,41 +29,62 @@
 namespace bh {
 
 constexpr int NR = FORCE_R;
-constexpr size_t FS_SMEM = (size_t)FAR_CAP * 24 + (size_t)SRC_CAP * 32 + (size_t)(NEAR_CAP + 1) * 16;
-static_assert(2 * FT * NR * sizeof(float) <= (size_t)FAR_CAP * 24, "slice partials alias the far staging");
-static_assert(FT * NR >= STREAM_CHUNK, "a CTA must cover every target of a work item");
+constexpr int FW = 4;       // warps per CTA
+constexpr int WFAR = 64;    // far entries per staging pass (per warp)
+constexpr int WSRC = 64;    // near sources per bulk-copy pass (per warp, per buffer)
+constexpr int WDESC = 64;   // near descriptors per batch (per warp)
+
+// per-warp shared-memory carve-up (bytes)
+constexpr int W_FARXY = 0;                           // WFAR x float4 (x, x, y, y)
+constexpr int W_FARM = W_FARXY + WFAR * 16;          // WFAR x float2 (M, M)
+constexpr int W_SRC = W_FARM + WFAR * 8;             // 2 x WSRC x 32 bytes
+constexpr int W_SHIFT = W_SRC + 2 * WSRC * 32;       // (WDESC + 1) x float2
+constexpr int W_NBOX = W_SHIFT + (WDESC + 1) * 8;    // (WDESC + 1) x int
+constexpr int W_NPRE = W_NBOX + (WDESC + 1) * 4;     // (WDESC + 1) x int
+constexpr int W_COL = W_NPRE + (WDESC + 1) * 4;      // 2 x (MAX_TG + 1) x int
+constexpr int W_MBAR = (W_COL + 2 * (MAX_TG + 1) * 4 + 7) / 8 * 8;  // 2 x uint64
+constexpr int W_BYTES = (W_MBAR + 16 + 127) / 128 * 128;
+constexpr size_t FS_SMEM = (size_t)FW * W_BYTES;
+static_assert(2 * 32 * NR * sizeof(float) <= (size_t)W_SRC, "slice partials alias the far staging");
+static_assert(32 * NR >= STREAM_CHUNK, "a warp must cover every target of a work item");
+static_assert(W_SRC % 16 == 0 && W_BYTES % 128 == 0, "bulk-copy destinations must be 16-byte aligned");
 
 template <bool KAHAN, int MINB>
-__global__ void __launch_bounds__(FT, MINB) k_fstream(DevPlan d, int tick, int accumulate) {
+__global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, int accumulate) {
     extern __shared__ __align__(128) unsigned char smem[];
-    float4 *farxy = reinterpret_cast<float4 *>(smem);                 // FAR_CAP x (x, x, y, y)
-    float2 *farm = reinterpret_cast<float2 *>(farxy + FAR_CAP);       // FAR_CAP x (M, M)
-    unsigned char *src = smem + FAR_CAP * 24;                         // SRC_CAP x 32 bytes
-    float2 *nshift = reinterpret_cast<float2 *>(src + SRC_CAP * 32);  // NEAR_CAP + 1
-    int *nbox = reinterpret_cast<int *>(nshift + NEAR_CAP + 1);       // first particle of a box
-    int *npre = nbox + NEAR_CAP + 1;                                  // NEAR_CAP + 1
-    float *red = reinterpret_cast<float *>(smem);                     // aliases farxy / farm
-    __shared__ uint64_t s_mbar;  // completion of the near-source bulk copies
-    __shared__ int s_item;
-    __shared__ int s_col0[MAX_TG + 1], s_colpre[MAX_TG + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned char *ws = smem + warp * W_BYTES;
+    float4 *farxy = reinterpret_cast<float4 *>(ws + W_FARXY);
+    float2 *farm = reinterpret_cast<float2 *>(ws + W_FARM);
+    unsigned char *srcb = ws + W_SRC;
+    float2 *nshift = reinterpret_cast<float2 *>(ws + W_SHIFT);
+    int *nbox = reinterpret_cast<int *>(ws + W_NBOX);
+    int *npre = reinterpret_cast<int *>(ws + W_NPRE);
+    int *col0 = reinterpret_cast<int *>(ws + W_COL);
+    int *colpre = col0 + MAX_TG + 1;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(ws + W_MBAR);
+    float *red = reinterpret_cast<float *>(ws);  // aliases the far staging
 
-    const int tid = threadIdx.x;
     const int nxt = (d.glob->epoch + 1) & 1;
     const double *Xs = d.X[nxt], *Ys = d.Y[nxt];
     const long long nitems = d.item_off[d.NG_total];
-    unsigned long long npairs = 0, fpairs = 0;  // counted by thread 0
-    uint32_t tphase = 0;                        // parity of s_mbar's current phase
-    bool tma_ok = true;  // block-uniform; cleared (and flagged) when a copy wait times out
-    if (tid == 0) {
-        tc::mbar_init(&s_mbar, 1);
+    unsigned long long npairs = 0, fpairs = 0;  // counted by lane 0
+    uint32_t phases = 0u;  // bit b: parity of buffer b's current mbarrier phase
+    bool tma_ok = true;  // warp-uniform; cleared (and flagged) when a copy wait times out
+    if (lane == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    __syncthreads();
+    __syncwarp();
 
     for (;;) {
-        if (tid == 0) s_item = (int)atomicAdd(&d.glob->item_next, 1u);
-        __syncthreads();
-        const int item = s_item;
+        int item = 0;
+        if (lane == 0) {
+            const int q = (int)atomicAdd(&d.glob->item_next, 1u);
+            item = q < nitems ? d.item_order[q] : q;  // heaviest items first
+        }
+        item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= nitems) break;
         const long long g = d.item_group[item];
         const int chunk = item - d.item_off[g];
@@ -72,42 +97,52 @@ __global__ void __launch_bounds__(FT, MINB) k_fstream(DevPlan d, int tick, int a
         const int gx0 = gi * TG, gy0 = gj * TG;
         const int gx1 = min(G, gx0 + TG), gy1 = min(G, gy0 + TG);
         const int ncol = gx1 - gx0;
-        if (tid < ncol) {
-            const long long b0 = sd.boff + (long long)(gx0 + tid) * G + gy0;
-            const int st = d.box_start[b0];
-            s_col0[tid] = st;
-            s_colpre[tid + 1] = d.box_start[b0 + (gy1 - gy0)] - st;
+        // the group's targets: ncol box columns, each a contiguous run of particles
+        {
+            int st = 0, len = 0;
+            if (lane < ncol) {
+                const long long b0 = sd.boff + (long long)(gx0 + lane) * G + gy0;
+                st = d.box_start[b0];
+                len = d.box_start[b0 + (gy1 - gy0)] - st;
+            }
+            int inc = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += y;
+            }
+            if (lane < ncol) {
+                col0[lane] = st;
+                colpre[lane + 1] = inc;
+            }
+            if (lane == 0) colpre[0] = 0;
         }
-        __syncthreads();
-        if (tid == 0) {
-            s_colpre[0] = 0;
-            for (int c = 1; c <= ncol; c++) s_colpre[c] += s_colpre[c - 1];
-        }
-        __syncthreads();
-        const int nt = s_colpre[ncol];
+        __syncwarp();
+        const int nt = colpre[ncol];
         int c0, T;
         item_range(nt, d.item_cnt[g], chunk, &c0, &T);
         const float step_f = __double2float_rn(dy.step);
         const float eps2 = d.eps2_f;
 
-        // ---- thread -> (slice, NR targets)
+        // ---- lane -> (slice, NR targets)
         const int nthr = (T + NR - 1) / NR;
-        const int nslice = FT / nthr;
-        const bool active = tid < nslice * nthr;
-        const int slice = active ? tid / nthr : 0, tl = active ? tid % nthr : 0;
-        int ti[NR];
-        bool tv[NR];
+        const int nslice = 32 / nthr;
+        const bool active = lane < nslice * nthr;
+        const int slice = active ? lane / nthr : 0, tl = active ? lane % nthr : 0;
+        // sorted index of the lane's target r (recomputed in the epilogue rather than kept live)
+        auto target_index = [&](int r) {
+            const int v = tl * NR + r;
+            const int u = c0 + (v < T ? v : 0);
+            int c = 0;
+            while (c + 1 < ncol && colpre[c + 1] <= u) c++;
+            return col0[c] + (u - colpre[c]);
+        };
         float tx[NR], ty[NR];
 #pragma unroll
         for (int r = 0; r < NR; r++) {
-            const int v = tl * NR + r;
-            tv[r] = v < T;
-            const int u = c0 + (tv[r] ? v : 0);
-            int c = 0;
-            while (c + 1 < ncol && s_colpre[c + 1] <= u) c++;
-            ti[r] = s_col0[c] + (u - s_colpre[c]);
-            const float4 p = d.P[ti[r]];
-            const int lb = d.skey[ti[r]] - (int)sd.boff;
+            const int ti = target_index(r);
+            const float4 p = d.P[ti];
+            const int lb = d.skey[ti] - (int)sd.boff;
             const int kx = lb / G, ky = lb - kx * G;
             tx[r] = __fadd_rn(__fmul_rn((float)(kx - gx0), step_f), p.x);
             ty[r] = __fadd_rn(__fmul_rn((float)(ky - gy0), step_f), p.y);
@@ -129,9 +164,9 @@ __global__ void __launch_bounds__(FT, MINB) k_fstream(DevPlan d, int tick, int a
         const int4 *ln = d.lnear + sd.lnoff + lg * (sd.lncap + 1);
 
         // ---- far field
-        for (int f0 = 0; f0 < cnt.x; f0 += FAR_CAP) {
-            const int nf = min(FAR_CAP, cnt.x - f0);
-            for (int k = tid; k < nf; k += FT) {
+        for (int f0 = 0; f0 < cnt.x; f0 += WFAR) {
+            const int nf = min(WFAR, cnt.x - f0);
+            for (int k = lane; k < nf; k += 32) {
                 const unsigned code = (unsigned)lf[f0 + k];
                 const int l = (int)(code >> 28), loc = (int)(code & 0x0FFFFFFFu);
                 const int gl = sd.lvg[l];
@@ -142,10 +177,16 @@ __global__ void __launch_bounds__(FT, MINB) k_fstream(DevPlan d, int tick, int a
                 farxy[k] = make_float4(rx, rx, ry, ry);
                 farm[k] = make_float2(rr.z, rr.z);
             }
-            __syncthreads();
+            __syncwarp();
             if (active) {
+                // plain FP32 sums over the pass's (at most WFAR / nslice) entries, then one
+                // compensated (Kahan) addition of the pass sum into the running total
                 const ulonglong2 *fp = reinterpret_cast<const ulonglong2 *>(farxy);
                 const f2_t *fm = reinterpret_cast<const f2_t *>(farm);
+                f2_t px2[NR / 2], py2[NR / 2];
+#pragma unroll
+                for (int kk = 0; kk < NR / 2; kk++) px2[kk] = py2[kk] = f2_pack(0.f, 0.f);
+#pragma unroll 2
                 for (int k = slice; k < nf; k += nslice) {
                     const ulonglong2 rxy = fp[k];  // (rx, rx), (ry, ry)
                     const f2_t mm = fm[k];         // (M, M)
@@ -153,23 +194,27 @@ __global__ void __launch_bounds__(FT, MINB) k_fstream(DevPlan d, int tick, int a
                     for (int kk = 0; kk < NR / 2; kk++) {
                         const f2_t dx = f2_add(rxy.x, ntx2[kk]), dyy = f2_add(rxy.y, nty2[kk]);
                         const f2_t w = f2_mul(mm, f2_rcp(f2_fma(dx, dx, f2_fma(dyy, dyy, eps2x2))));
-                        const f2_t fx = f2_mul(w, dx), fy = f2_mul(w, dyy);
-                        if (KAHAN) {  // y = f - c; t = s + y; c = (t - s) - y; s = t
-                            const f2_t yx = f2_fma(fcx2[kk], m1x2, fx), t1 = f2_add(fsx2[kk], yx);
-                            fcx2[kk] = f2_fma(yx, m1x2, f2_fma(fsx2[kk], m1x2, t1));
-                            fsx2[kk] = t1;
-                            const f2_t yy = f2_fma(fcy2[kk], m1x2, fy), t2 = f2_add(fsy2[kk], yy);
-                            fcy2[kk] = f2_fma(yy, m1x2, f2_fma(fsy2[kk], m1x2, t2));
-                            fsy2[kk] = t2;
-                        } else {
-                            fsx2[kk] = f2_add(fsx2[kk], fx);
-                            fsy2[kk] = f2_add(fsy2[kk], fy);
-                        }
+                        px2[kk] = f2_fma(w, dx, px2[kk]);
+                        py2[kk] = f2_fma(w, dyy, py2[kk]);
+                    }
+                }
+#pragma unroll
+                for (int kk = 0; kk < NR / 2; kk++) {
+                    if (KAHAN) {  // y = f - c; t = s + y; c = (t - s) - y; s = t
+                        const f2_t yx = f2_fma(fcx2[kk], m1x2, px2[kk]), t1 = f2_add(fsx2[kk], yx);
+                        fcx2[kk] = f2_fma(yx, m1x2, f2_fma(fsx2[kk], m1x2, t1));
+                        fsx2[kk] = t1;
+                        const f2_t yy = f2_fma(fcy2[kk], m1x2, py2[kk]), t2 = f2_add(fsy2[kk], yy);
+                        fcy2[kk] = f2_fma(yy, m1x2, f2_fma(fsy2[kk], m1x2, t2));
+                        fsy2[kk] = t2;
+                    } else {
+                        fsx2[kk] = f2_add(fsx2[kk], px2[kk]);
+                        fsy2[kk] = f2_add(fsy2[kk], py2[kk]);
                     }
                 }
             }
             fpairs += (unsigned long long)T * nf;
-            __syncthreads();  // farxy / farm are restaged by the next pass
+            __syncwarp();  // the staging is rewritten by the next pass
         }
         // compensated far sums s - c; the compensations are dead from here on
 #pragma unroll
@@ -178,80 +223,93 @@ __global__ void __launch_bounds__(FT, MINB) k_fstream(DevPlan d, int tick, int a
             fsy2[kk] = f2_fma(fcy2[kk], m1x2, fsy2[kk]);
         }
 
-        // ---- near field: boxes in batches of NEAR_CAP, sources in bulk-copy passes of SRC_CAP.
-        // Descriptor k of the group's near list is (first particle, exclusive prefix of the
-        // particle counts, shift of the box origin in the group frame); entry nnb holds the total.
-        for (int b0 = 0; b0 < cnt.y && tma_ok; b0 += NEAR_CAP) {
-            const int nn = min(NEAR_CAP, cnt.y - b0);
-            for (int k = tid; k <= nn; k += FT) {
+        // ---- near field: descriptors in batches of WDESC; sources in double-buffered passes.
+        // Descriptor k is (first particle, exclusive prefix of the boxes' particle counts, box
+        // shift in the group frame); entry [count] carries the total.
+        for (int b0 = 0; b0 < cnt.y && tma_ok; b0 += WDESC) {
+            const int nn = min(WDESC, cnt.y - b0);
+            for (int k = lane; k <= nn; k += 32) {
                 const int4 e = ln[b0 + k];
                 nbox[k] = e.x;
                 npre[k] = e.y;
                 nshift[k] = make_float2(__int_as_float(e.z), __int_as_float(e.w));
             }
-            __syncthreads();
-            const int pend = npre[nn];
-            int kfirst = 0;  // first box of the batch overlapping the current pass (block-uniform)
-            for (int s0 = npre[0]; s0 < pend; s0 += SRC_CAP) {
-                const int ns = min(SRC_CAP, pend - s0);
-                // every box piece inside [s0, s0 + ns) is one bulk copy; all complete on s_mbar
-                if (tid == 0) tc::mbar_expect_tx(&s_mbar, (uint32_t)ns * 32u);
+            __syncwarp();
+            const int pbeg = npre[0], pend = npre[nn];
+            const int npass = (pend - pbeg + WSRC - 1) / WSRC;
+            // issue pass p into buffer p & 1: one bulk copy per box piece, all on that buffer's
+            // mbarrier (lane 0 announces the bytes before any lane copies)
+            auto issue = [&](int p) {
+                const int s0 = pbeg + p * WSRC, ns = min(WSRC, pend - s0);
+                unsigned char *dst = srcb + (p & 1) * (WSRC * 32);
+                if (lane == 0) tc::mbar_expect_tx(&mbar[p & 1], (uint32_t)ns * 32u);
+                __syncwarp();
                 tc::fence_async_smem();
-                for (int k = tid; k < nn; k += FT) {
+                for (int k = lane; k < nn; k += 32) {
                     const int lo = max(npre[k], s0), hi = min(npre[k + 1], s0 + ns);
                     if (lo < hi)
-                        tc::bulk_g2s(src + 32 * (lo - s0), d.PD + 2 * (long long)(nbox[k] + (lo - npre[k])),
-                                     (uint32_t)(hi - lo) * 32u, &s_mbar);
+                        tc::bulk_g2s(dst + 32 * (lo - s0), d.PD + 2 * (long long)(nbox[k] + (lo - npre[k])),
+                                     (uint32_t)(hi - lo) * 32u, &mbar[p & 1]);
                 }
-                const bool ok = tc::mbar_wait(&s_mbar, tphase);
-                tphase ^= 1u;
-                if (!__syncthreads_and(ok ? 1 : 0)) {
+            };
+            if (npass > 0) issue(0);
+            if (npass > 1) issue(1);
+            int kfirst = 0;  // first descriptor overlapping the current pass (warp-uniform)
+            for (int p = 0; p < npass; p++) {
+                const int s0 = pbeg + p * WSRC, ns = min(WSRC, pend - s0);
+                const int buf = p & 1;
+                const bool ok = tc::mbar_wait(&mbar[buf], (phases >> buf) & 1u);
+                phases ^= 1u << buf;
+                if (!__all_sync(0xffffffffu, ok)) {
                     // flagged; give the copies in flight a second bounded wait, then stage
-                    // nothing more in this launch (the barrier phase is no longer known)
-                    if (tid == 0) raise_err(d.glob, 8u /*BH_DEV_WAIT_TIMEOUT*/);
-                    tc::mbar_wait(&s_mbar, tphase ^ 1u);
+                    // nothing more in this launch (the barrier phases are no longer known)
+                    if (lane == 0) raise_err(d.glob, 8u /*BH_DEV_WAIT_TIMEOUT*/);
+                    tc::mbar_wait(&mbar[buf], ((phases >> buf) & 1u) ^ 1u);
+                    if (p + 1 < npass) tc::mbar_wait(&mbar[buf ^ 1], (phases >> (buf ^ 1)) & 1u);
                     tma_ok = false;
-                    __syncthreads();
                     break;
                 }
-                while (kfirst + 1 < nn && npre[kfirst + 1] <= s0) kfirst++;
-                if (active) {
-                    // every thread walks the same box pieces; the slices split each piece, and
-                    // the piece's shift is folded into the (negated) target coordinates
-                    const float4 *s4 = reinterpret_cast<const float4 *>(src);
-                    for (int k = kfirst; k < nn && npre[k] < s0 + ns; k++) {
-                        const int lo = max(npre[k], s0) - s0, hi = min(npre[k + 1], s0 + ns) - s0;
+                // shift the staged sources into the group frame in place: lane-strided over the
+                // pass, each lane following its sources' boxes forward through the descriptors
+                float4 *s4 = reinterpret_cast<float4 *>(srcb + buf * (WSRC * 32));
+                {
+                    int k = kfirst;
+                    for (int j = lane; j < ns; j += 32) {
+                        while (k + 1 < nn && npre[k + 1] <= s0 + j) k++;
                         const float2 sh = nshift[k];
-                        const f2_t shx = f2_pack(sh.x, sh.x), shy = f2_pack(sh.y, sh.y);
-                        f2_t bx[NR / 2], by[NR / 2];
+                        float4 v = s4[2 * j];
+                        v.x = __fadd_rn(sh.x, v.x);
+                        v.y = v.x;
+                        v.z = __fadd_rn(sh.y, v.z);
+                        v.w = v.z;
+                        s4[2 * j] = v;
+                    }
+                    while (kfirst + 1 < nn && npre[kfirst + 1] <= s0 + ns) kfirst++;  // next pass
+                }
+                __syncwarp();
+                if (active) {
+#pragma unroll 2
+                    for (int j = slice; j < ns; j += nslice) {
+                        const ulonglong2 sxy = *reinterpret_cast<const ulonglong2 *>(s4 + 2 * j);
+                        const f2_t mm = *reinterpret_cast<const f2_t *>(s4 + 2 * j + 1);
 #pragma unroll
                         for (int kk = 0; kk < NR / 2; kk++) {
-                            bx[kk] = f2_add(ntx2[kk], shx);
-                            by[kk] = f2_add(nty2[kk], shy);
-                        }
-#pragma unroll 2
-                        for (int j = lo + slice; j < hi; j += nslice) {
-                            const ulonglong2 sxy = *reinterpret_cast<const ulonglong2 *>(s4 + 2 * j);
-                            const f2_t mm = *reinterpret_cast<const f2_t *>(s4 + 2 * j + 1);
-#pragma unroll
-                            for (int kk = 0; kk < NR / 2; kk++) {
-                                const f2_t dx = f2_add(sxy.x, bx[kk]), dyy = f2_add(sxy.y, by[kk]);
-                                const f2_t r2 = f2_fma(dx, dx, f2_fma(dyy, dyy, eps2x2));
-                                const f2_t w = f2_mul(mm, f2_rcp(r2));
-                                nax2[kk] = f2_fma(w, dx, nax2[kk]);
-                                nay2[kk] = f2_fma(w, dyy, nay2[kk]);
-                            }
+                            const f2_t dx = f2_add(sxy.x, ntx2[kk]), dyy = f2_add(sxy.y, nty2[kk]);
+                            const f2_t r2 = f2_fma(dx, dx, f2_fma(dyy, dyy, eps2x2));
+                            const f2_t w = f2_mul(mm, f2_rcp(r2));
+                            nax2[kk] = f2_fma(w, dx, nax2[kk]);
+                            nay2[kk] = f2_fma(w, dyy, nay2[kk]);
                         }
                     }
                 }
                 npairs += (unsigned long long)T * ns;
-                __syncthreads();  // the staging buffer is refilled by the next pass
+                __syncwarp();  // every lane is done with this buffer
+                if (p + 2 < npass) issue(p + 2);
             }
-            __syncthreads();  // the descriptors are rewritten by the next batch
+            __syncwarp();  // the descriptors are rewritten by the next batch
         }
-        __syncthreads();  // red aliases the far staging
 
-        // ---- reduce slice partials and write
+        // ---- reduce slice partials (through the far staging) and write
         if (active) {
 #pragma unroll
             for (int k = 0; k < NR / 2; k++) {
@@ -267,18 +325,18 @@ __global__ void __launch_bounds__(FT, MINB) k_fstream(DevPlan d, int tick, int a
                 o[3] = b1 + t1;
             }
         }
-        __syncthreads();
+        __syncwarp();
         if (active && slice == 0) {
 #pragma unroll
             for (int r = 0; r < NR; r++) {
-                if (!tv[r]) continue;
+                if (tl * NR + r >= T) continue;
                 float sx = 0.f, sy = 0.f;
                 for (int k = 0; k < nslice; k++) {
                     const float *o = red + 2 * ((k * nthr + tl) * NR + r);
                     sx += o[0];
                     sy += o[1];
                 }
-                const int t = ti[r];
+                const int t = target_index(r);
                 double ax = d.gconst * (double)sx, ay = d.gconst * (double)sy;
                 if (accumulate) {
                     ax += d.AX[t];
@@ -295,9 +353,9 @@ __global__ void __launch_bounds__(FT, MINB) k_fstream(DevPlan d, int tick, int a
                 }
             }
         }
-        __syncthreads();  // red and s_item are reused by the next item
+        __syncwarp();  // the staging and the column table are reused by the next item
     }
-    if (tid == 0) {
+    if (lane == 0) {
         atomicAdd(&d.glob->near_pairs, npairs);
         atomicAdd(&d.glob->far_pairs, fpairs);
     }
@@ -307,11 +365,11 @@ template <bool KAHAN, int MINB>
 static cudaError_t launch_fstream_t(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
     long long items_max = d.NG_total + d.n_total / d.chunk + 1;
     long long grid = 152LL * MINB;
-    if (grid > items_max) grid = items_max;
+    if (grid * FW > items_max) grid = (items_max + FW - 1) / FW;
     if (grid < 1) grid = 1;
     cudaError_t e = cudaMemsetAsync(&d.glob->item_next, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    k_fstream<KAHAN, MINB><<<(unsigned)grid, FT, FS_SMEM, st>>>(d, tick ? 1 : 0, accumulate ? 1 : 0);
+    k_fstream<KAHAN, MINB><<<(unsigned)grid, FW * 32, FS_SMEM, st>>>(d, tick ? 1 : 0, accumulate ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -34,6 +34,7 @@ constexpr int TARGET_CHUNK = FORCE_THREADS * FORCE_R;        // targets per work
 constexpr int FRONTIER_CAP = 512;                            // traversal frontier per level
 constexpr int STREAM_CHUNK = 128;  // targets per work item of the list-streaming force kernel
 constexpr int LIST_MAX_G = 16384;  // far-list codes hold (level, cell) in 4 + 28 bits
+constexpr int ITEM_BUCKETS = 32;   // log2 cost buckets of the heaviest-first item order
 
 struct SysDesc {
     long long n, poff;  // particle count, first particle (concatenated)
@@ -93,6 +94,8 @@ struct DevPlan {
     int *lfar;
     int4 *lnear;
     int2 *lcnt;
+    int *item_order;  // work items, heaviest cost bucket first (list-streaming path)
+    int *item_bucket;  // ITEM_BUCKETS counts + ITEM_BUCKETS cursors
     int stream;  // 1: lists are built by k_lists and streamed by k_fstream
     int chunk;   // targets per work item (TARGET_CHUNK, or STREAM_CHUNK when stream)
     // parameters

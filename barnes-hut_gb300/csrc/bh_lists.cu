@@ -145,11 +145,94 @@ __global__ void __launch_bounds__(LT) k_lists(DevPlan d) {
     }
 }
 
+// ---------------------------------------------------------------- heaviest-first item order
+// A warp of the force kernel owns one work item, so an item's duration grows with its pair count
+// and the launch ends with its slowest warp.  Items are therefore handed out heaviest first:
+// bucket b holds the items whose estimated cost T x (near sources + 2 x far cells) lies in
+// [2^b, 2^(b+1)); buckets are laid out from the top down.  Order inside a bucket follows atomic
+// arrival, which changes only which warp evaluates an item, not its result.
+__device__ __forceinline__ int item_cost_bucket(const DevPlan &d, long long item) {
+    const long long g = d.item_group[item];
+    const int chunk = (int)(item - d.item_off[g]);
+    const int s = find_seg(d.goff_tab, d.nsys, g);
+    const SysDesc &sd = d.sys[s];
+    const long long lg = g - sd.goff;
+    const int2 cnt = d.lcnt[g];
+    const int near_total = d.lnear[sd.lnoff + lg * (sd.lncap + 1) + cnt.y].y;
+    // targets of the item: the group's count is the item count's share (chunks differ by <= 1)
+    const int nch = d.item_cnt[g];
+    const int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
+    const int gx0 = gi * sd.TG, gy0 = gj * sd.TG;
+    const int gx1 = min(sd.G, gx0 + sd.TG), gy1 = min(sd.G, gy0 + sd.TG);
+    int nt = 0;
+    for (int c = gx0; c < gx1; c++) {
+        const long long b0 = sd.boff + (long long)c * sd.G + gy0;
+        nt += d.box_start[b0 + (gy1 - gy0)] - d.box_start[b0];
+    }
+    int c0, T;
+    item_range(nt, nch, chunk, &c0, &T);
+    const unsigned long long cost = (unsigned long long)T * (unsigned long long)(near_total + 2 * cnt.x) + 1ull;
+    const int b = 63 - __clzll((long long)cost);
+    return min(b, ITEM_BUCKETS - 1);
+}
+
+__global__ void __launch_bounds__(256) k_item_hist(DevPlan d) {
+    __shared__ int h[ITEM_BUCKETS];
+    if (threadIdx.x < ITEM_BUCKETS) h[threadIdx.x] = 0;
+    __syncthreads();
+    const long long nitems = d.item_off[d.NG_total];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += (long long)gridDim.x * blockDim.x)
+        atomicAdd(&h[item_cost_bucket(d, i)], 1);
+    __syncthreads();
+    if (threadIdx.x < ITEM_BUCKETS && h[threadIdx.x]) atomicAdd(&d.item_bucket[threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void __launch_bounds__(256) k_item_order(DevPlan d) {
+    __shared__ int off[ITEM_BUCKETS], h[ITEM_BUCKETS], base[ITEM_BUCKETS];
+    if (threadIdx.x == 0) {
+        int o = 0;
+        for (int b = ITEM_BUCKETS - 1; b >= 0; b--) {  // heaviest bucket first
+            off[b] = o;
+            o += d.item_bucket[b];
+        }
+    }
+    if (threadIdx.x < ITEM_BUCKETS) h[threadIdx.x] = 0;
+    __syncthreads();
+    const long long nitems = d.item_off[d.NG_total];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    // one pass of the grid per round; each round reserves a range per bucket for its block
+    for (long long r0 = (long long)blockIdx.x * blockDim.x; r0 < nitems; r0 += stride) {
+        const long long i = r0 + threadIdx.x;
+        int b = -1, rank = 0;
+        if (i < nitems) {
+            b = item_cost_bucket(d, i);
+            rank = atomicAdd(&h[b], 1);
+        }
+        __syncthreads();
+        if (threadIdx.x < ITEM_BUCKETS) {
+            base[threadIdx.x] = h[threadIdx.x] ? atomicAdd(&d.item_bucket[ITEM_BUCKETS + threadIdx.x], h[threadIdx.x]) : 0;
+            h[threadIdx.x] = 0;
+        }
+        __syncthreads();
+        if (b >= 0) d.item_order[off[b] + base[b] + rank] = (int)i;
+        __syncthreads();
+    }
+}
+
 cudaError_t launch_lists(const DevPlan &d, cudaStream_t st) {
     if (d.NG_total == 0) return cudaSuccess;
     long long grid = 152LL * 16;
     if (grid > d.NG_total) grid = d.NG_total;
     k_lists<<<(unsigned)grid, LT, 0, st>>>(d);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(d.item_bucket, 0, sizeof(int) * 2 * ITEM_BUCKETS, st);
+    if (e != cudaSuccess) return e;
+    long long items_max = d.NG_total + d.n_total / d.chunk + 1;
+    long long ig = (items_max + 255) / 256;
+    if (ig > 152LL * 8) ig = 152LL * 8;
+    k_item_hist<<<(unsigned)ig, 256, 0, st>>>(d);
+    k_item_order<<<(unsigned)ig, 256, 0, st>>>(d);
     return cudaGetLastError();
 }
 
