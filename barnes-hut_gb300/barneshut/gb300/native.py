@@ -30,6 +30,7 @@ BH_PREC_FP64 = 2
 
 BH_FLAG_LEARNED = 1
 BH_FLAG_WALK = 2
+BH_STREAM_DENSE_MIN = 64  # include/bh_gb300.h
 
 # every symbol include/bh_gb300.h declares
 EXPORTS = (

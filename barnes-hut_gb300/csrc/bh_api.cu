@@ -30,7 +30,7 @@ struct bh_plan {
     size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
     size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_tiles, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
-        o_rec2, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt;
+        o_rec2, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk;
     bool stream = false;  // theta-mode interaction lists built once per group and streamed
     int chunk = TARGET_CHUNK;
     void *ws = nullptr;
@@ -186,11 +186,15 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
             long long cap = 0;
             for (int l = 0; l < d.L; l++) cap += std::min<long long>(FRONTIER_CAP, (long long)d.lvg[l] * d.lvg[l]);
             d.lfcap = (int)cap;
-            d.lncap = (int)std::min<long long>(FRONTIER_CAP, (long long)d.G * d.G);
+            // a near leaf is rejected for the group rectangle, so its centre of mass lies within
+            // 1/theta box edges of it: at most floor(1/theta) + 1 boxes away (one more for rounding)
+            const long long reach = (long long)std::floor(1.0 / pr.theta) + 2;
+            const long long side = std::min<long long>(d.G, d.TG + 2 * reach);
+            d.lncap = (int)std::min<long long>(FRONTIER_CAP, side * side);
             d.lfoff = lf_total;
             d.lnoff = ln_total;
             lf_total += (long long)d.NGs * d.NGs * d.lfcap;
-            ln_total += (long long)d.NGs * d.NGs * (d.lncap + 1);
+            ln_total += (long long)d.NGs * d.NGs * 2 * (d.lncap + 1);
         }
     }
     p->B_total = p->boff[nsys];
@@ -245,7 +249,13 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_lfar = take(4 * (size_t)lf_total);
     p->o_lnear = take(16 * (size_t)ln_total);
     p->o_lcnt = take(p->stream ? 8 * (size_t)p->NG_total : 0);
-    p->o_iord = take(p->stream ? 4 * ((size_t)p->NG_total + N / p->chunk + 1) : 0);
+    const size_t sitems = p->stream ? (size_t)p->NG_total + N / DENSE_MIN + N / p->chunk + 1 : 0;
+    p->o_iord = take(4 * sitems);
+    p->o_sicnt = take(p->stream ? 4 * (size_t)p->NG_total : 0);
+    p->o_sioff = take(p->stream ? 4 * ((size_t)p->NG_total + 1) : 0);
+    p->o_sigrp = take(4 * sitems);
+    p->o_sisub = take(4 * sitems);
+    p->o_sichk = take(8 * sitems);
     p->o_ibkt = take(p->stream ? 4 * 2 * ITEM_BUCKETS : 0);
     p->o_mom = take(48 * C);
     p->o_rec = take(16 * C);
@@ -318,6 +328,12 @@ static void fill_dev(bh_plan *p) {
     d.lnear = (int4 *)(w + p->o_lnear);
     d.lcnt = (int2 *)(w + p->o_lcnt);
     d.item_order = (int *)(w + p->o_iord);
+    d.sitem_cnt = (int *)(w + p->o_sicnt);
+    d.sitem_off = (int *)(w + p->o_sioff);
+    d.sitem_group = (int *)(w + p->o_sigrp);
+    d.sitem_sub = (int *)(w + p->o_sisub);
+    d.sitem_chunk = (int2 *)(w + p->o_sichk);
+    d.dense_min = DENSE_MIN;
     d.item_bucket = (int *)(w + p->o_ibkt);
     d.stream = p->stream ? 1 : 0;
     d.chunk = p->chunk;
@@ -524,8 +540,9 @@ extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     // prologue, 3 box-scan phases, work items (count, 3 scan phases, fill),
     // pyramid levels 1..Lmax-1, records; with particles also bbox, bbox
     // finalize, place, scatter, leaf moments, force (and before it the list build and the
-    // two kernels of the heaviest-first item order)
-    *count = 1 + 3 + 5 + (p->Lmax - 1) + 1 + (p->n_total > 0 ? 6 : 0) + (p->stream && p->n_total > 0 ? 3 : 0);
+    // two kernels of the heaviest-first item order); list streaming also builds its own work
+    // items (count, 3 scan phases, fill)
+    *count = 1 + 3 + 5 + (p->Lmax - 1) + 1 + (p->n_total > 0 ? 6 : 0) + (p->stream ? 5 : 0) + (p->stream && p->n_total > 0 ? 3 : 0);
     return BH_OK;
 }
 

@@ -30,24 +30,28 @@ namespace bh {
 
 constexpr int NR = FORCE_R;
 constexpr int FW = 4;       // warps per CTA
-constexpr int WFAR = 64;    // far entries per staging pass (per warp)
-constexpr int WSRC = 64;    // near sources per bulk-copy pass (per warp, per buffer)
+constexpr int WFAR = 128;   // far entries per staging pass (per warp)
+constexpr int WSRC = 80;    // near sources per bulk-copy pass (per warp, per buffer)
 constexpr int WDESC = 64;   // near descriptors per batch (per warp)
 
-// per-warp shared-memory carve-up (bytes)
-constexpr int W_FARXY = 0;                           // WFAR x float4 (x, x, y, y)
-constexpr int W_FARM = W_FARXY + WFAR * 16;          // WFAR x float2 (M, M)
-constexpr int W_SRC = W_FARM + WFAR * 8;             // 2 x WSRC x 32 bytes
+// per-warp shared-memory carve-up (bytes).  The far phase of an item ends before its near phase
+// starts, and the slice reduction follows both, so the far staging and the reduction buffer
+// share the two near-source buffers.
+constexpr int W_SRC = 0;                             // 2 x WSRC x 32 bytes
+constexpr int W_FARXY = 0;                           // WFAR x float4 (x, x, y, y), aliases W_SRC
+constexpr int W_FARM = W_FARXY + WFAR * 16;          // WFAR x float2 (M, M), aliases W_SRC
 constexpr int W_SHIFT = W_SRC + 2 * WSRC * 32;       // (WDESC + 1) x float2
 constexpr int W_NBOX = W_SHIFT + (WDESC + 1) * 8;    // (WDESC + 1) x int
 constexpr int W_NPRE = W_NBOX + (WDESC + 1) * 4;     // (WDESC + 1) x int
-constexpr int W_COL = W_NPRE + (WDESC + 1) * 4;      // 2 x (MAX_TG + 1) x int
-constexpr int W_MBAR = (W_COL + 2 * (MAX_TG + 1) * 4 + 7) / 8 * 8;  // 2 x uint64
+constexpr int NRUN = MAX_TG * MAX_TG;                // target runs (boxes) of a work item
+constexpr int W_RUN = W_NPRE + (WDESC + 1) * 4;      // 2 x (NRUN + 1) x int
+constexpr int W_MBAR = (W_RUN + 2 * (NRUN + 1) * 4 + 7) / 8 * 8;  // 2 x uint64
 constexpr int W_BYTES = (W_MBAR + 16 + 127) / 128 * 128;
 constexpr size_t FS_SMEM = (size_t)FW * W_BYTES;
-static_assert(2 * 32 * NR * sizeof(float) <= (size_t)W_SRC, "slice partials alias the far staging");
+static_assert(W_FARM + WFAR * 8 <= W_SHIFT, "far staging must fit in the near-source buffers");
+static_assert(2 * 32 * NR * sizeof(float) <= (size_t)W_SHIFT, "slice partials alias the source buffers");
 static_assert(32 * NR >= STREAM_CHUNK, "a warp must cover every target of a work item");
-static_assert(W_SRC % 16 == 0 && W_BYTES % 128 == 0, "bulk-copy destinations must be 16-byte aligned");
+static_assert((WSRC * 32) % 16 == 0 && W_BYTES % 128 == 0, "bulk-copy destinations must be 16-byte aligned");
 
 template <bool KAHAN, int MINB>
 __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, int accumulate) {
@@ -60,14 +64,14 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
     float2 *nshift = reinterpret_cast<float2 *>(ws + W_SHIFT);
     int *nbox = reinterpret_cast<int *>(ws + W_NBOX);
     int *npre = reinterpret_cast<int *>(ws + W_NPRE);
-    int *col0 = reinterpret_cast<int *>(ws + W_COL);
-    int *colpre = col0 + MAX_TG + 1;
+    int *rstart = reinterpret_cast<int *>(ws + W_RUN);  // first particle of target run r
+    int *rpre = rstart + NRUN + 1;                       // exclusive prefix of the run lengths
     uint64_t *mbar = reinterpret_cast<uint64_t *>(ws + W_MBAR);
-    float *red = reinterpret_cast<float *>(ws);  // aliases the far staging
+    float *red = reinterpret_cast<float *>(ws);  // aliases the source buffers
 
     const int nxt = (d.glob->epoch + 1) & 1;
     const double *Xs = d.X[nxt], *Ys = d.Y[nxt];
-    const long long nitems = d.item_off[d.NG_total];
+    const long long nitems = d.sitem_off[d.NG_total];
     unsigned long long npairs = 0, fpairs = 0;  // counted by lane 0
     uint32_t phases = 0u;  // bit b: parity of buffer b's current mbarrier phase
     bool tma_ok = true;  // warp-uniform; cleared (and flagged) when a copy wait times out
@@ -86,8 +90,9 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         }
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= nitems) break;
-        const long long g = d.item_group[item];
-        const int chunk = item - d.item_off[g];
+        const long long g = d.sitem_group[item];
+        const int sub = d.sitem_sub[item];  // box within the group, or -1: the sparse boxes
+        const int2 ck = d.sitem_chunk[item];
         const int s = find_seg(d.goff_tab, d.nsys, g);
         const SysDesc &sd = d.sys[s];
         const SysDyn &dy = d.dyn[s];
@@ -95,32 +100,41 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         const int TG = sd.TG, G = sd.G;
         const int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
         const int gx0 = gi * TG, gy0 = gj * TG;
-        const int gx1 = min(G, gx0 + TG), gy1 = min(G, gy0 + TG);
-        const int ncol = gx1 - gx0;
-        // the group's targets: ncol box columns, each a contiguous run of particles
+        // the item's targets: runs of box-sorted particles, one per box of the group (column-major;
+        // a box outside the item's set is an empty run)
+        const int nrun = TG * TG;
         {
-            int st = 0, len = 0;
-            if (lane < ncol) {
-                const long long b0 = sd.boff + (long long)(gx0 + lane) * G + gy0;
-                st = d.box_start[b0];
-                len = d.box_start[b0 + (gy1 - gy0)] - st;
-            }
-            int inc = len;
+            int carry = 0;
+            for (int b0 = 0; b0 < nrun; b0 += 32) {
+                const int b = b0 + lane;
+                int st = 0, len = 0;
+                if (b < nrun) {
+                    const int cx = b / TG, cy = b - cx * TG;
+                    if (gx0 + cx < G && gy0 + cy < G) {
+                        const long long bb = sd.boff + (long long)(gx0 + cx) * G + gy0 + cy;
+                        st = d.box_start[bb];
+                        len = d.box_start[bb + 1] - st;
+                        if (sub >= 0 ? b != sub : len >= d.dense_min) len = 0;
+                    }
+                }
+                int inc = len;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= o) inc += y;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += y;
+                }
+                if (b < nrun) {
+                    rstart[b] = st;
+                    rpre[b + 1] = carry + inc;
+                }
+                carry += __shfl_sync(0xffffffffu, inc, 31);
             }
-            if (lane < ncol) {
-                col0[lane] = st;
-                colpre[lane + 1] = inc;
-            }
-            if (lane == 0) colpre[0] = 0;
+            if (lane == 0) rpre[0] = 0;
         }
         __syncwarp();
-        const int nt = colpre[ncol];
+        const int nt = rpre[nrun];
         int c0, T;
-        item_range(nt, d.item_cnt[g], chunk, &c0, &T);
+        item_range(nt, ck.y, ck.x, &c0, &T);
         const float step_f = __double2float_rn(dy.step);
         const float eps2 = d.eps2_f;
 
@@ -133,9 +147,12 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         auto target_index = [&](int r) {
             const int v = tl * NR + r;
             const int u = c0 + (v < T ? v : 0);
-            int c = 0;
-            while (c + 1 < ncol && colpre[c + 1] <= u) c++;
-            return col0[c] + (u - colpre[c]);
+            int lo = 0, hi = nrun;  // the run r with rpre[r] <= u < rpre[r + 1]
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (rpre[mid] <= u) lo = mid; else hi = mid;
+            }
+            return rstart[lo] + (u - rpre[lo]);
         };
         float tx[NR], ty[NR];
 #pragma unroll
@@ -161,26 +178,12 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         }
         const int2 cnt = d.lcnt[g];
         const int *lf = d.lfar + sd.lfoff + lg * sd.lfcap;
-        const int4 *ln = d.lnear + sd.lnoff + lg * (sd.lncap + 1);
+        const int4 *ln = d.lnear + sd.lnoff + lg * 2 * (sd.lncap + 1);
 
-        // ---- far field
-        for (int f0 = 0; f0 < cnt.x; f0 += WFAR) {
-            const int nf = min(WFAR, cnt.x - f0);
-            for (int k = lane; k < nf; k += 32) {
-                const unsigned code = (unsigned)lf[f0 + k];
-                const int l = (int)(code >> 28), loc = (int)(code & 0x0FFFFFFFu);
-                const int gl = sd.lvg[l];
-                const int ci = loc / gl, cj = loc - ci * gl;
-                const float4 rr = d.rec[sd.coff + sd.lvoff[l] + loc];
-                const float rx = __fadd_rn(__fmul_rn((float)((ci << l) - gx0), step_f), rr.x);
-                const float ry = __fadd_rn(__fmul_rn((float)((cj << l) - gy0), step_f), rr.y);
-                farxy[k] = make_float4(rx, rx, ry, ry);
-                farm[k] = make_float2(rr.z, rr.z);
-            }
-            __syncwarp();
+        // sweep nf staged far entries; the pass's plain FP32 sum enters the running total through
+        // a Kahan-compensated addition when compensate (and the compensations are live) is set
+        auto far_sweep = [&](int nf, bool compensate) {
             if (active) {
-                // plain FP32 sums over the pass's (at most WFAR / nslice) entries, then one
-                // compensated (Kahan) addition of the pass sum into the running total
                 const ulonglong2 *fp = reinterpret_cast<const ulonglong2 *>(farxy);
                 const f2_t *fm = reinterpret_cast<const f2_t *>(farm);
                 f2_t px2[NR / 2], py2[NR / 2];
@@ -200,7 +203,7 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                 }
 #pragma unroll
                 for (int kk = 0; kk < NR / 2; kk++) {
-                    if (KAHAN) {  // y = f - c; t = s + y; c = (t - s) - y; s = t
+                    if (KAHAN && compensate) {  // y = f - c; t = s + y; c = (t - s) - y; s = t
                         const f2_t yx = f2_fma(fcx2[kk], m1x2, px2[kk]), t1 = f2_add(fsx2[kk], yx);
                         fcx2[kk] = f2_fma(yx, m1x2, f2_fma(fsx2[kk], m1x2, t1));
                         fsx2[kk] = t1;
@@ -214,27 +217,103 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                 }
             }
             fpairs += (unsigned long long)T * nf;
-            __syncwarp();  // the staging is rewritten by the next pass
+            __syncwarp();  // the staging is rewritten next
+        };
+
+        // ---- far field: the group's accepted cells
+        for (int f0 = 0; f0 < cnt.x; f0 += WFAR) {
+            const int nf = min(WFAR, cnt.x - f0);
+            for (int k = lane; k < nf; k += 32) {
+                const unsigned code = (unsigned)lf[f0 + k];
+                const int l = (int)(code >> 28), loc = (int)(code & 0x0FFFFFFFu);
+                const int gl = sd.lvg[l];
+                const int ci = loc / gl, cj = loc - ci * gl;
+                const float4 rr = d.rec[sd.coff + sd.lvoff[l] + loc];
+                const float rx = __fadd_rn(__fmul_rn((float)((ci << l) - gx0), step_f), rr.x);
+                const float ry = __fadd_rn(__fmul_rn((float)((cj << l) - gy0), step_f), rr.y);
+                farxy[k] = make_float4(rx, rx, ry, ry);
+                farm[k] = make_float2(rr.z, rr.z);
+            }
+            __syncwarp();
+            far_sweep(nf, true);
         }
         // compensated far sums s - c; the compensations are dead from here on
 #pragma unroll
         for (int kk = 0; kk < NR / 2; kk++) {
             fsx2[kk] = f2_fma(fcx2[kk], m1x2, fsx2[kk]);
             fsy2[kk] = f2_fma(fcy2[kk], m1x2, fsy2[kk]);
+            fcx2[kk] = fcy2[kk] = f2_pack(0.f, 0.f);
         }
 
         // ---- near field: descriptors in batches of WDESC; sources in double-buffered passes.
         // Descriptor k is (first particle, exclusive prefix of the boxes' particle counts, box
         // shift in the group frame); entry [count] carries the total.
         for (int b0 = 0; b0 < cnt.y && tma_ok; b0 += WDESC) {
-            const int nn = min(WDESC, cnt.y - b0);
-            for (int k = lane; k <= nn; k += 32) {
-                const int4 e = ln[b0 + k];
-                nbox[k] = e.x;
-                npre[k] = e.y;
-                nshift[k] = make_float2(__int_as_float(e.z), __int_as_float(e.w));
+            int nn = min(WDESC, cnt.y - b0);
+            if (sub < 0) {
+                for (int k = lane; k <= nn; k += 32) {
+                    const int4 e = ln[2 * (b0 + k)];
+                    nbox[k] = e.x;
+                    npre[k] = e.y;
+                    nshift[k] = make_float2(__int_as_float(e.z), __int_as_float(e.w));
+                }
+                __syncwarp();
+            } else {
+                // a dense box's own lists: a near leaf of the group that passes the opening test
+                // against the single box (its offsets taken relative to the box origin) is swept
+                // as a far entry; the others stay near and are re-prefixed
+                const int bcx = sub / TG, bcy = sub - bcx * TG;
+                const float oxb = __fmul_rn((float)bcx, step_f), oyb = __fmul_rn((float)bcy, step_f);
+                const float s2 = __fmul_rn(step_f, step_f), theta2 = d.theta2_f;
+                const int own = (gx0 + bcx) * G + (gy0 + bcy);
+                int nkeep = 0, nacc = 0, base = 0;
+                for (int k0 = 0; k0 < nn; k0 += 32) {
+                    const int k = k0 + lane;
+                    int4 e0 = make_int4(0, 0, 0, 0), e1 = make_int4(-1, 0, 0, 0);
+                    int c = 0;
+                    bool acc = false;
+                    if (k < nn) {
+                        e0 = ln[2 * (b0 + k)];
+                        e1 = ln[2 * (b0 + k) + 1];
+                        c = ln[2 * (b0 + k + 1)].y - e0.y;
+                        if (e1.x != own) {
+                            const float rxb = __fsub_rn(__int_as_float(e1.z), oxb);
+                            const float ryb = __fsub_rn(__int_as_float(e1.w), oyb);
+                            const float dxo = fmaxf(0.f, fmaxf(-rxb, __fsub_rn(rxb, step_f)));
+                            const float dyo = fmaxf(0.f, fmaxf(-ryb, __fsub_rn(ryb, step_f)));
+                            const float d2 = __fadd_rn(__fmul_rn(dxo, dxo), __fmul_rn(dyo, dyo));
+                            acc = s2 < __fmul_rn(theta2, d2);
+                        }
+                    }
+                    const bool keep = k < nn && !acc;
+                    const unsigned mk = __ballot_sync(0xffffffffu, keep), ma = __ballot_sync(0xffffffffu, acc);
+                    const unsigned lt = (1u << lane) - 1u;
+                    int inc = keep ? c : 0;  // inclusive scan of the kept particle counts
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+                        if (lane >= o) inc += y;
+                    }
+                    if (keep) {
+                        const int q = nkeep + __popc(mk & lt);
+                        nbox[q] = e0.x;
+                        npre[q] = base + inc - c;
+                        nshift[q] = make_float2(__int_as_float(e0.z), __int_as_float(e0.w));
+                    } else if (acc) {
+                        const int q = nacc + __popc(ma & lt);
+                        const float rx = __int_as_float(e1.z), ry = __int_as_float(e1.w), m = __int_as_float(e1.y);
+                        farxy[q] = make_float4(rx, rx, ry, ry);
+                        farm[q] = make_float2(m, m);
+                    }
+                    nkeep += __popc(mk);
+                    nacc += __popc(ma);
+                    base += __shfl_sync(0xffffffffu, inc, 31);
+                }
+                if (lane == 0) npre[nkeep] = base;
+                __syncwarp();
+                if (nacc > 0) far_sweep(nacc, false);  // (also orders the staging for the copies)
+                nn = nkeep;
             }
-            __syncwarp();
             const int pbeg = npre[0], pend = npre[nn];
             const int npass = (pend - pbeg + WSRC - 1) / WSRC;
             // issue pass p into buffer p & 1: one bulk copy per box piece, all on that buffer's
@@ -309,7 +388,7 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
             __syncwarp();  // the descriptors are rewritten by the next batch
         }
 
-        // ---- reduce slice partials (through the far staging) and write
+        // ---- reduce slice partials (through the source buffers) and write
         if (active) {
 #pragma unroll
             for (int k = 0; k < NR / 2; k++) {

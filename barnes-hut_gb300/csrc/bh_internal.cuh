@@ -25,6 +25,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/bh_gb300.h"
+
 namespace bh {
 
 constexpr int MAX_LEVELS = 16;  // G <= 32768
@@ -35,6 +37,9 @@ constexpr int FRONTIER_CAP = 512;                            // traversal fronti
 constexpr int STREAM_CHUNK = 128;  // targets per work item of the list-streaming force kernel
 constexpr int LIST_MAX_G = 16384;  // far-list codes hold (level, cell) in 4 + 28 bits
 constexpr int ITEM_BUCKETS = 32;   // log2 cost buckets of the heaviest-first item order
+constexpr int DENSE_MIN = BH_STREAM_DENSE_MIN;  // list streaming: a box with at least this many
+                                               // particles gets its own work items and per-box
+                                               // refined near lists
 
 struct SysDesc {
     long long n, poff;  // particle count, first particle (concatenated)
@@ -88,13 +93,19 @@ struct DevPlan {
     // interaction lists of every target group (list-streaming path), in fixed per-group slots
     // (SysDesc lfcap far codes, lncap + 1 near descriptors), counts in lcnt (x far, y near):
     //   far code: level << 28 | cell index within the level;
-    //   near descriptor: (first particle, exclusive prefix of the boxes' particle counts, shift
-    //   of the box origin from the group origin as float bits x, y); entry [count] carries the
-    //   total in .y
+    //   near descriptor: two int4 -- (first particle, exclusive prefix of the boxes' particle
+    //   counts, shift of the box origin from the group origin as float bits x, y) and (box index
+    //   in the system, mass, centre of mass in the group frame x, y as float bits); descriptor
+    //   [count] carries the total in .y of its first int4
     int *lfar;
     int4 *lnear;
     int2 *lcnt;
-    int *item_order;  // work items, heaviest cost bucket first (list-streaming path)
+    // list-streaming work items (per group: its sparse boxes together, then every dense box):
+    // group, box within the group (cx * TG + cy, or -1 for the sparse boxes), (chunk, chunks)
+    int *sitem_cnt, *sitem_off, *sitem_group, *sitem_sub;
+    int2 *sitem_chunk;
+    int dense_min;
+    int *item_order;  // list-streaming work items, heaviest cost bucket first
     int *item_bucket;  // ITEM_BUCKETS counts + ITEM_BUCKETS cursors
     int stream;  // 1: lists are built by k_lists and streamed by k_fstream
     int chunk;   // targets per work item (TARGET_CHUNK, or STREAM_CHUNK when stream)

@@ -273,6 +273,69 @@ __global__ void __launch_bounds__(TPB) k_fill_items(DevPlan d) {
     }
 }
 
+// List-streaming work items.  Per group: the boxes holding fewer than dense_min particles share
+// ceil(n_sparse / chunk) items (sub = -1); every other box gets ceil(n_box / chunk) items of its
+// own (sub = cx * TG + cy), which use per-box refined near lists.  Chunks split their targets
+// into near-equal parts (item_range).
+__global__ void __launch_bounds__(TPB) k_sitem_count(DevPlan d) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < d.NG_total; g += stride) {
+        int s = find_seg(d.goff_tab, d.nsys, g);
+        const SysDesc &sd = d.sys[s];
+        long long lg = g - sd.goff;
+        int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
+        int gx0 = gi * sd.TG, gy0 = gj * sd.TG;
+        int gx1 = min(sd.G, gx0 + sd.TG), gy1 = min(sd.G, gy0 + sd.TG);
+        int sparse = 0, cnt = 0;
+        for (int c = gx0; c < gx1; c++)
+            for (int r = gy0; r < gy1; r++) {
+                const long long b = sd.boff + (long long)c * sd.G + r;
+                const int nb = d.box_start[b + 1] - d.box_start[b];
+                if (nb >= d.dense_min) cnt += (nb + d.chunk - 1) / d.chunk;
+                else sparse += nb;
+            }
+        d.sitem_cnt[g] = cnt + (sparse + d.chunk - 1) / d.chunk;
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_sitem_fill(DevPlan d) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < d.NG_total; g += stride) {
+        int s = find_seg(d.goff_tab, d.nsys, g);
+        const SysDesc &sd = d.sys[s];
+        long long lg = g - sd.goff;
+        int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
+        int gx0 = gi * sd.TG, gy0 = gj * sd.TG;
+        int gx1 = min(sd.G, gx0 + sd.TG), gy1 = min(sd.G, gy0 + sd.TG);
+        int o = d.sitem_off[g];
+        int sparse = 0;
+        for (int c = gx0; c < gx1; c++)
+            for (int r = gy0; r < gy1; r++) {
+                const long long b = sd.boff + (long long)c * sd.G + r;
+                const int nb = d.box_start[b + 1] - d.box_start[b];
+                if (nb < d.dense_min) sparse += nb;
+            }
+        const int ns = (sparse + d.chunk - 1) / d.chunk;
+        for (int k = 0; k < ns; k++, o++) {
+            d.sitem_group[o] = (int)g;
+            d.sitem_sub[o] = -1;
+            d.sitem_chunk[o] = make_int2(k, ns);
+        }
+        for (int c = gx0; c < gx1; c++)
+            for (int r = gy0; r < gy1; r++) {
+                const long long b = sd.boff + (long long)c * sd.G + r;
+                const int nb = d.box_start[b + 1] - d.box_start[b];
+                if (nb < d.dense_min) continue;
+                const int nk = (nb + d.chunk - 1) / d.chunk;
+                for (int k = 0; k < nk; k++, o++) {
+                    d.sitem_group[o] = (int)g;
+                    d.sitem_sub[o] = (c - gx0) * sd.TG + (r - gy0);
+                    d.sitem_chunk[o] = make_int2(k, nk);
+                }
+            }
+    }
+}
+
 // ------------------------------------------------------------------ scatter
 // Counting-sort scatter into box order: destination = box_start[key] + slot.
 // Writes the FP64 state of the next buffer, the packed float4 record (offsets
@@ -438,6 +501,12 @@ cudaError_t launch_items(const DevPlan &d, cudaStream_t st) {
     cudaError_t e = scan_excl(d.item_cnt, d.item_off, d.NG_total, d.tile_sums, st);
     if (e != cudaSuccess) return e;
     k_fill_items<<<g, TPB, 0, st>>>(d);
+    if (d.stream) {
+        k_sitem_count<<<g, TPB, 0, st>>>(d);
+        e = scan_excl(d.sitem_cnt, d.sitem_off, d.NG_total, d.tile_sums, st);
+        if (e != cudaSuccess) return e;
+        k_sitem_fill<<<g, TPB, 0, st>>>(d);
+    }
     return cudaGetLastError();
 }
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {

@@ -51,6 +51,10 @@ extern "C" {
 
 /* bh_params.flags */
 #define BH_FLAG_LEARNED 1 /* apply the learned far-field correction (weights bound) */
+/* List streaming (the theta-mode default): a box holding at least this many particles is
+   evaluated with its own near list, refined from its group's -- a near leaf whose centre of mass
+   passes the opening test against the single box becomes a far entry for that box's particles. */
+#define BH_STREAM_DENSE_MIN 64
 #define BH_FLAG_WALK 2    /* theta mode: walk the cell pyramid inside the force kernel for
                            every work item instead of building each target group's
                            interaction lists once and streaming them (the default for

@@ -631,9 +631,16 @@ void oref_moments(long long n, const double *x, const double *y, const double *m
  * skipped (cutoff = 1e-5 reproduces cpu_numba.py; 0 skips coincident points).
  * Output ax/ay in pid order.  counts[0..1] = near / far pair interactions.
  */
+/*
+ * dense_min > 0 (theta mode): the targets of a box holding at least dense_min particles use
+ * per-box lists refined from their group's lists -- a near leaf whose centre of mass passes the
+ * opening test against the single box (same float arithmetic as the CUDA list-streaming kernel:
+ * offsets in the group frame, then relative to the box origin) becomes a far entry for those
+ * targets.  dense_min <= 0 keeps the group lists for every target (the walking force kernel).
+ */
 int oref_theta_evaluate(long long n, const double *x, const double *y, const double *m, int G,
                         int TG, double theta, double eps2, double cutoff, double gconst,
-                        double *ax, double *ay, long long *counts, int nthreads)
+                        double *ax, double *ay, long long *counts, int nthreads, int dense_min)
 {
     if (n <= 0) return 0;
     double bb[5];
@@ -748,16 +755,61 @@ int oref_theta_evaluate(long long n, const double *x, const double *y, const dou
             free(fr);
             free(nx);
         }
-        long long nsrc = 0;
-        for (long long q = 0; q < nnear; q++) nsrc += bstart[near[q] + 1] - bstart[near[q]];
-        cnt_near += nt * nsrc;
-        cnt_far += nt * nfar;
+        long long *bnear = (long long *)malloc(sizeof(long long) * (size_t)(nnear + 1));
+        long long *bfar = (long long *)malloc(sizeof(long long) * (size_t)(nnear + 1));
         for (int bx = gx0; bx < gx1; bx++) {
-            for (long long k = bstart[(long long)bx * G + gy0]; k < bstart[(long long)bx * G + gy1]; k++) {
+            for (int by = gy0; by < gy1; by++) {
+                const long long bb0 = (long long)bx * G + by;
+                const long long nb = bstart[bb0 + 1] - bstart[bb0];
+                if (nb == 0) continue;
+                /* this box's lists: the group's, or the refined per-box lists of a dense box */
+                const long long *nl = near;
+                long long nnl = nnear, nacc = 0;
+                if (!flat && dense_min > 0 && nb >= dense_min) {
+                    const float ox = (float)(bx - gx0) * step_f, oy = (float)(by - gy0) * step_f;
+                    nnl = 0;
+                    for (long long q = 0; q < nnear; q++) {
+                        const long long c = near[q];
+                        const int qi = (int)(c / G), qj = (int)(c % G);
+                        int acc = 0;
+                        if (!(qi == bx && qj == by)) {
+                            float rx = (float)(qi - gx0) * step_f + rec[4 * c];
+                            float ry = (float)(qj - gy0) * step_f + rec[4 * c + 1];
+                            float rxb = rx - ox, ryb = ry - oy;
+                            float dxo = fmaxf(0.0f, fmaxf(-rxb, rxb - step_f));
+                            float dyo = fmaxf(0.0f, fmaxf(-ryb, ryb - step_f));
+                            float d2 = dxo * dxo + dyo * dyo;
+                            acc = (step_f * step_f) < (theta2_f * d2);
+                        }
+                        if (acc)
+                            bfar[nacc++] = c; /* a leaf: level 0, cell index = box index */
+                        else
+                            bnear[nnl++] = c;
+                    }
+                    nl = bnear;
+                }
+                long long nsrc = 0;
+                for (long long q = 0; q < nnl; q++) nsrc += bstart[nl[q] + 1] - bstart[nl[q]];
+                cnt_near += nb * nsrc;
+                cnt_far += nb * (nfar + nacc);
+            for (long long k = bstart[bb0]; k < bstart[bb0 + 1]; k++) {
                 long long t = order[k];
                 double xt = x[t], yt = y[t], sx = 0.0, sy = 0.0;
-                for (long long q = 0; q < nnear; q++)
-                    for (long long kk = bstart[near[q]]; kk < bstart[near[q] + 1]; kk++) {
+                for (long long q = 0; q < nacc; q++) {
+                    long long cell = bfar[q];
+                    int ci = (int)(cell / G), cj = (int)(cell % G);
+                    const double *qm = mom + 6 * cell;
+                    double cx = (bb[0] + (double)ci * bb[4]) + qm[1] / qm[0];
+                    double cy = (bb[1] + (double)cj * bb[4]) + qm[2] / qm[0];
+                    double dx = cx - xt, dy = cy - yt;
+                    double r2 = dx * dx + dy * dy;
+                    if (!(r2 > cutoff)) continue;
+                    double w = qm[0] / (r2 + eps2);
+                    sx += w * dx;
+                    sy += w * dy;
+                }
+                for (long long q = 0; q < nnl; q++)
+                    for (long long kk = bstart[nl[q]]; kk < bstart[nl[q] + 1]; kk++) {
                         long long j = order[kk];
                         double dx = x[j] - xt, dy = y[j] - yt;
                         double r2 = dx * dx + dy * dy;
@@ -785,7 +837,10 @@ int oref_theta_evaluate(long long n, const double *x, const double *y, const dou
                 ax[t] = gconst * sx;
                 ay[t] = gconst * sy;
             }
+            }
         }
+        free(bnear);
+        free(bfar);
         free(far);
         free(near);
     }

@@ -184,7 +184,10 @@ def test_theta_vs_fp64_oracle(theta, TG, G, prec, walk):
     plan.evaluate()
     out = plan.store()
     nn, nf = plan.pair_counts()
-    ax, ay, on, of = oracle.theta_evaluate(x, y, m, G, TG=TG, theta=theta, eps2=eps * eps, cutoff=0.0)
+    # list streaming refines the near lists of dense boxes; the walk keeps the group lists
+    dense = 0 if (walk or prec == 2) else native().BH_STREAM_DENSE_MIN
+    ax, ay, on, of = oracle.theta_evaluate(x, y, m, G, TG=TG, theta=theta, eps2=eps * eps, cutoff=0.0,
+                                           dense_min=dense)
     assert (nn, nf) == (on, of), "interaction lists differ from the oracle's"
     err = oracle.rel_rms(out["ax"].cpu().numpy(), out["ay"].cpu().numpy(), ax, ay)
     assert err <= (1e-8 if prec == 2 else 1e-5), err

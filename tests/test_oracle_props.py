@@ -23,6 +23,20 @@ def test_theta_error_shrinks_with_theta(oracle_mod, theta, TG):
     assert nn > 0 and nf > 0
 
 
+@pytest.mark.parametrize("TG", [2, 4])
+def test_dense_box_refinement(oracle_mod, TG):
+    """Per-box refinement of dense boxes' near lists moves near pairs to far entries, keeps the
+    error within the opening-angle bound, and is the identity when no box is dense."""
+    x, y, m, _, _ = workloads.cluster_mixture(20000, seed=7)
+    dax, day = oracle_mod.direct(x, y, m, eps2=1e-6, cutoff=0.0)
+    a0 = oracle_mod.theta_evaluate(x, y, m, 16, TG=TG, theta=0.5, eps2=1e-6)
+    a1 = oracle_mod.theta_evaluate(x, y, m, 16, TG=TG, theta=0.5, eps2=1e-6, dense_min=64)
+    a2 = oracle_mod.theta_evaluate(x, y, m, 16, TG=TG, theta=0.5, eps2=1e-6, dense_min=10 ** 9)
+    assert a1[2] < a0[2] and a1[3] > a0[3]
+    assert a2[2:] == a0[2:] and np.array_equal(a2[0], a0[0])
+    assert oracle_mod.rel_rms(a1[0], a1[1], dax, day) < 1e-3
+
+
 def test_theta_tiny_is_direct(oracle_mod):
     x, y, m, _, _ = workloads.uniform(800, seed=4)
     dax, day = oracle_mod.direct(x, y, m, eps2=1e-6, cutoff=0.0)
