@@ -1,12 +1,17 @@
 """Autotuner for the force kernel's tile shape.
 
 Tunables (per plan): group_dim -- target group edge in leaf boxes (1, 2, 4 or 8;
-TG^2 boxes share one interaction list and one CTA work item) -- and tune -- the
-force-kernel variant (0: 8 CTAs per SM with 64 registers per thread, 1: 6 CTAs
-per SM with 80).  Candidates are timed with CUDA events on the caller's own
-particles (create_tree + summarize once, then the force kernel alone, median of
-a few launches); the fastest is returned and cached in memory (and optionally in
-a JSON file) under a key made of the workload's shape: particle count, grid,
+TG^2 boxes share one interaction list) --, dense_min -- boxes holding at least
+this many particles get their own work items and per-box refined near lists
+(list-streaming path) -- and tune -- the force-kernel variant (0: 8 CTAs per SM
+with 64 registers per thread, 1: 6 CTAs per SM with 80).  Every candidate keeps
+the opening-angle rule for every target (a cell accepted for a group rectangle
+passes the test for each of its boxes); they differ in how far the lists are
+refined, so the chosen one's accuracy is measured and reported by the caller.
+Candidates are timed with CUDA events on the caller's own particles
+(create_tree + summarize once, then the force phase alone, median of a few
+launches); the fastest is returned and cached in memory (and optionally in a
+JSON file) under a key made of the workload's shape: particle count, grid,
 opening angle, softening and occupancy per box.
 """
 import json
@@ -29,16 +34,17 @@ def _key(n, grids, theta, softening, precision):
 
 def candidates(theta):
     out = []
-    for tg in (1, 2, 4):
-        for tune in (0, 1):
-            out.append({"group_dim": tg, "tune": tune})
+    for tg in (1, 2, 4, 8):
+        for dm in ((0,) if tg == 1 else (16, 32, 64)):
+            for tune in (0, 1):
+                out.append({"group_dim": tg, "dense_min": dm, "tune": tune})
     return out
 
 
 def tune(systems, grids, grav_constant=1.0, dt=1e-5, softening=1e-4, theta=0.5,
          precision=native.BH_PREC_FP32_KAHAN, repeats=3, device="cuda", cache_path=None,
          log=None):
-    """Pick {group_dim, tune} for these systems (list of (x, y, m, vx, vy)).
+    """Pick {group_dim, dense_min, tune} for these systems (list of (x, y, m, vx, vy)).
 
     Returns (best config dict, {config: seconds} timings)."""
     import numpy as np
@@ -56,7 +62,7 @@ def tune(systems, grids, grav_constant=1.0, dt=1e-5, softening=1e-4, theta=0.5,
     stream = torch.cuda.current_stream(device)
     for c in candidates(theta):
         prm = native.make_params(grav_constant, dt, softening, 0.0, theta, c["group_dim"],
-                                 precision, 0, c["tune"])
+                                 precision, 0, c["tune"], dense_min=c["dense_min"])
         try:
             plan = native.Plan(n, grids, prm, device=device)
         except native.BHError:

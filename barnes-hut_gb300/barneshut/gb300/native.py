@@ -67,6 +67,7 @@ class Params(ctypes.Structure):
         ("flags", ctypes.c_int),
         ("tune", ctypes.c_int),
         ("correction_theta", ctypes.c_double),
+        ("dense_min", ctypes.c_int),
     ]
 
 
@@ -130,10 +131,10 @@ def grid_dim(n, max_particles_per_box):
 
 def make_params(grav_constant=1.0, tick_seconds=0.005, softening=0.0, cutoff_r2=1e-5,
                 theta=0.0, group_dim=0, precision=BH_PREC_FP32_KAHAN, flags=0, tune=0,
-                correction_theta=0.0):
+                correction_theta=0.0, dense_min=0):
     return Params(float(grav_constant), float(tick_seconds), float(softening), float(cutoff_r2),
                   float(theta), int(group_dim), int(precision), int(flags), int(tune),
-                  float(correction_theta))
+                  float(correction_theta), int(dense_min))
 
 
 def _ptr(t):

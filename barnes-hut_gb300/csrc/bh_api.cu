@@ -33,6 +33,7 @@ struct bh_plan {
         o_rec2, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk;
     bool stream = false;  // theta-mode interaction lists built once per group and streamed
     int chunk = TARGET_CHUNK;
+    int dense_min = BH_STREAM_DENSE_MIN;
     void *ws = nullptr;
     int device = -1;
     DevPlan dev;
@@ -177,6 +178,8 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->stream = !flat && pr.precision != BH_PREC_FP64 && pr.cutoff_r2 == 0.0 && pr.softening > 0.0 &&
                 !(pr.flags & BH_FLAG_WALK) && maxG <= LIST_MAX_G;
     p->chunk = p->stream ? STREAM_CHUNK : TARGET_CHUNK;
+    if (pr.dense_min < 0) return bad("dense_min < 0");
+    p->dense_min = pr.dense_min > 0 ? pr.dense_min : BH_STREAM_DENSE_MIN;
     long long lf_total = 0, ln_total = 0;
     if (p->stream) {
         // a level's accepted cells are a subset of its frontier (at most FRONTIER_CAP cells), and
@@ -249,7 +252,7 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_lfar = take(4 * (size_t)lf_total);
     p->o_lnear = take(16 * (size_t)ln_total);
     p->o_lcnt = take(p->stream ? 8 * (size_t)p->NG_total : 0);
-    const size_t sitems = p->stream ? (size_t)p->NG_total + N / DENSE_MIN + N / p->chunk + 1 : 0;
+    const size_t sitems = p->stream ? (size_t)p->NG_total + N / p->dense_min + N / p->chunk + 1 : 0;
     p->o_iord = take(4 * sitems);
     p->o_sicnt = take(p->stream ? 4 * (size_t)p->NG_total : 0);
     p->o_sioff = take(p->stream ? 4 * ((size_t)p->NG_total + 1) : 0);
@@ -333,7 +336,7 @@ static void fill_dev(bh_plan *p) {
     d.sitem_group = (int *)(w + p->o_sigrp);
     d.sitem_sub = (int *)(w + p->o_sisub);
     d.sitem_chunk = (int2 *)(w + p->o_sichk);
-    d.dense_min = DENSE_MIN;
+    d.dense_min = p->dense_min;
     d.item_bucket = (int *)(w + p->o_ibkt);
     d.stream = p->stream ? 1 : 0;
     d.chunk = p->chunk;

@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         __syncwarp();
         const int nt = rpre[nrun];
         int c0, T;
-        item_range(nt, ck.y, ck.x, &c0, &T);
+        sitem_range(nt, ck.x, &c0, &T);
         const float step_f = __double2float_rn(dy.step);
         const float eps2 = d.eps2_f;
 

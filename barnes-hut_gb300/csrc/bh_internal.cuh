@@ -37,9 +37,6 @@ constexpr int FRONTIER_CAP = 512;                            // traversal fronti
 constexpr int STREAM_CHUNK = 128;  // targets per work item of the list-streaming force kernel
 constexpr int LIST_MAX_G = 16384;  // far-list codes hold (level, cell) in 4 + 28 bits
 constexpr int ITEM_BUCKETS = 32;   // log2 cost buckets of the heaviest-first item order
-constexpr int DENSE_MIN = BH_STREAM_DENSE_MIN;  // list streaming: a box with at least this many
-                                               // particles gets its own work items and per-box
-                                               // refined near lists
 
 struct SysDesc {
     long long n, poff;  // particle count, first particle (concatenated)
@@ -181,6 +178,13 @@ __device__ __forceinline__ void item_range(int nt, int nch, int k, int *c0, int 
     const int a = (int)((long long)k * nt / nch), b = (int)((long long)(k + 1) * nt / nch);
     *c0 = a;
     *T = b - a;
+}
+
+// Targets [c0, c0 + T) of list-streaming work item k of a target set of nt particles: full
+// chunks of STREAM_CHUNK (one warp, FORCE_R targets per lane) and one remainder.
+__device__ __forceinline__ void sitem_range(int nt, int k, int *c0, int *T) {
+    *c0 = k * STREAM_CHUNK;
+    *T = min(STREAM_CHUNK, nt - *c0);
 }
 
 __device__ __forceinline__ void raise_err(Globals *g, unsigned f) {

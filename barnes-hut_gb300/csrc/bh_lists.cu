@@ -199,7 +199,7 @@ __device__ __forceinline__ int item_cost_bucket(const DevPlan &d, long long item
             if (sub >= 0 ? (c - gx0) * sd.TG + (r - gy0) == sub : nb < d.dense_min) nt += nb;
         }
     int c0, T;
-    item_range(nt, ck.y, ck.x, &c0, &T);
+    sitem_range(nt, ck.x, &c0, &T);
     const unsigned long long cost = (unsigned long long)T * (unsigned long long)(near_total + 2 * cnt.x) + 1ull;
     const int b = 63 - __clzll((long long)cost);
     return min(b, ITEM_BUCKETS - 1);
@@ -257,7 +257,7 @@ cudaError_t launch_lists(const DevPlan &d, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(d.item_bucket, 0, sizeof(int) * 2 * ITEM_BUCKETS, st);
     if (e != cudaSuccess) return e;
-    long long items_max = d.NG_total + d.n_total / d.dense_min + d.n_total / d.chunk + 1;
+    long long items_max = d.NG_total + d.n_total / d.dense_min + d.n_total / d.chunk + 1;  // >= items
     long long ig = (items_max + 255) / 256;
     if (ig > 152LL * 8) ig = 152LL * 8;
     k_item_hist<<<(unsigned)ig, 256, 0, st>>>(d);

@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(TPB) k_fill_items(DevPlan d) {
 // List-streaming work items.  Per group: the boxes holding fewer than dense_min particles share
 // ceil(n_sparse / chunk) items (sub = -1); every other box gets ceil(n_box / chunk) items of its
 // own (sub = cx * TG + cy), which use per-box refined near lists.  Chunks split their targets
-// into near-equal parts (item_range).
+// into full chunks of STREAM_CHUNK and a remainder (sitem_range).
 __global__ void __launch_bounds__(TPB) k_sitem_count(DevPlan d) {
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < d.NG_total; g += stride) {

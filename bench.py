@@ -193,7 +193,7 @@ def batched_benchmark(torch, dev, nsys=512, steps=50, warmup=3):
     n = [len(s[0]) for s in systems]
     tile, _ = autotune.tune(systems, grids, 1.0, 1e-6, 1e-4, 0.5, device=dev)
     prm = native.make_params(1.0, 1e-6, 1e-4, 0.0, 0.5, tile["group_dim"],
-                             native.BH_PREC_FP32_KAHAN, 0, tile["tune"])
+                             native.BH_PREC_FP32_KAHAN, 0, tile["tune"], dense_min=tile.get("dense_min", 0))
     plan = native.Plan(n, grids, prm, device=dev)
     plan.load(*[np.concatenate([s[k] for s in systems]) for k in range(5)])
     for _ in range(warmup):
@@ -413,7 +413,7 @@ def main():
     # batch in box order (the state's order between steps of a running simulation)
     order = workloads.box_order(x, y, args.grid)
     x, y, m, vx, vy = (a[order].copy() for a in (x, y, m, vx, vy))
-    tile = {"group_dim": 0, "tune": 0}
+    tile = {"group_dim": 0, "tune": 0, "dense_min": 0}
     tune_ms = None
     if not args.quick:
         from barneshut.gb300 import autotune
@@ -422,7 +422,7 @@ def main():
                                  device=dev)
         tune_ms = {k: round(1e3 * v, 3) for k, v in tt.items()}
     prm = native.make_params(1.0, DT, SOFTENING, 0.0, THETA, tile["group_dim"],
-                             native.BH_PREC_FP32_KAHAN, 0, tile["tune"])
+                             native.BH_PREC_FP32_KAHAN, 0, tile["tune"], dense_min=tile.get("dense_min", 0))
     plan = native.Plan([args.n], [args.grid], prm, device=dev)
     stream = torch.cuda.current_stream(dev)
     batch = [torch.from_numpy(a).to(dev) for a in (x, y, m, vx, vy)]
@@ -556,7 +556,7 @@ def main():
                        "softening": SOFTENING, "dt": DT, "seed": SEED,
                        "l2": "state ~400 MB > 129 MB L2 (no flush needed)",
                        "parallelism": f"{ws} independent replica(s)"},
-            "gpu_launches": kernels_per_step * K,
+            "gpu_launches": (kernels_per_step + 1) * K,  # + the bh_load kernel of each step
             "roofline": {"bound": "fp32", "kernel": "k_force (near + far pair loop)",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": None,

@@ -51,9 +51,10 @@ extern "C" {
 
 /* bh_params.flags */
 #define BH_FLAG_LEARNED 1 /* apply the learned far-field correction (weights bound) */
-/* List streaming (the theta-mode default): a box holding at least this many particles is
-   evaluated with its own near list, refined from its group's -- a near leaf whose centre of mass
-   passes the opening test against the single box becomes a far entry for that box's particles. */
+/* List streaming (the theta-mode default): a box holding at least bh_params.dense_min particles
+   (default below) is evaluated with its own near list, refined from its group's -- a near leaf
+   whose centre of mass passes the opening test against the single box becomes a far entry for
+   that box's particles. */
 #define BH_STREAM_DENSE_MIN 64
 #define BH_FLAG_WALK 2    /* theta mode: walk the cell pyramid inside the force kernel for
                            every work item instead of building each target group's
@@ -77,6 +78,8 @@ typedef struct bh_params {
                              SM with more registers), picked by the autotuner */
     double correction_theta; /* with BH_FLAG_LEARNED: cells accepted at theta but
                                 not at correction_theta get the learned correction */
+    int dense_min;        /* list streaming: boxes with at least this many particles get
+                             per-box refined near lists (0 = BH_STREAM_DENSE_MIN) */
 } bh_params;
 
 typedef struct bh_plan bh_plan;
