@@ -41,6 +41,7 @@ DT = 1e-5
 SEED = 2
 METRIC = "particle-steps/s at N=4M on 1 GB300 (plain theta=0.5 step)"
 WORKLOAD = "cluster-mixture N=4,194,304, 512x512 boxes, theta=0.5, eps=1e-4, dt=1e-5, FP32+Kahan"
+K_FSTREAM_TRAFFIC = 877.7e6  # bytes per force launch, from the committed ncu summary
 
 
 def parse():
@@ -55,6 +56,8 @@ def parse():
     ap.add_argument("--ref-sample-boxes", type=int, default=1024)
     ap.add_argument("--quick", action="store_true",
                     help="skip the autotuner and the batched / learned side measurements")
+    ap.add_argument("--tile", default=None,
+                    help="group_dim,dense_min,tune: use this tile instead of the autotuner's")
     return ap.parse_args()
 
 
@@ -415,7 +418,10 @@ def main():
     x, y, m, vx, vy = (a[order].copy() for a in (x, y, m, vx, vy))
     tile = {"group_dim": 0, "tune": 0, "dense_min": 0}
     tune_ms = None
-    if not args.quick:
+    if args.tile:
+        tg, dm, tu = (int(v) for v in args.tile.split(","))
+        tile = {"group_dim": tg, "dense_min": dm, "tune": tu}
+    elif not args.quick:
         from barneshut.gb300 import autotune
 
         tile, tt = autotune.tune([(x, y, m, vx, vy)], [args.grid], 1.0, DT, SOFTENING, THETA,
@@ -559,7 +565,10 @@ def main():
             "gpu_launches": (kernels_per_step + 1) * K,  # + the bh_load kernel of each step
             "roofline": {"bound": "fp32", "kernel": "k_force (near + far pair loop)",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak, "traffic": K_FSTREAM_TRAFFIC,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                           "k_fstream launch at this workload "
+                                           "(profiles/k_fstream_cluster4M_theta05.md)",
                          "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off",
                          "algorithmic": f"12 flop x {near2} near + 20 flop x {far2} far pairs",
                          "kernel_ms": 1e3 * t_force},
