@@ -55,6 +55,9 @@ struct SysDyn {
     unsigned long long bbmax[2];  // ordered bits of max x, max y (atomicMax)
     double minx, miny, step;      // square bounding box origin and box edge
     double inv_step;              // 1 / step (0 when step is not positive)
+    float minx_f, miny_f;         // the origin rounded to float
+    float inv_step_f;             // 1 / step rounded to float
+    float key_tol;                // bound on |float quotient - exact quotient| (box edges)
 };
 
 struct Globals {
@@ -165,6 +168,20 @@ __device__ __forceinline__ int box_key1_fast(double p, double mn, double step, d
     if (fr < 1e-10 || fr > 1.0 - 1e-10) k = floor(__ddiv_rn(d, step));
     k = fmin(fmax(k, 0.0), (double)(G - 1));
     return (int)k;
+}
+
+// The same key with a float estimate first: q_f = (float(p) - float(mn)) * float(1 / step) is
+// within tol of the FP64 quotient (tol from the system's extent, set in k_bbox_finalize), so
+// floor(q_f) is the exact key unless q_f lies within tol of an integer; only then (and for an
+// unusable tol) is the FP64 key computed.  GB300 runs FP64 at 1/64 of the FP32 rate, and the
+// FP64 key costs about nine FP64 operations per coordinate.
+__device__ __forceinline__ int box_key1_f32(double p, double mn, double step, double inv, float mn_f,
+                                            float inv_f, float tol, int G) {
+    const float q = __fmul_rn(__fsub_rn(__double2float_rn(p), mn_f), inv_f);
+    const float k = floorf(q);
+    const float fr = q - k;
+    if (!(tol < 0.25f) || fr < tol || fr > 1.f - tol) return box_key1_fast(p, mn, step, inv, G);
+    return min(max((int)k, 0), G - 1);
 }
 
 // Origin of leaf box k along one axis: mn + k * step, FP64, no contraction.

@@ -120,6 +120,20 @@ __global__ void k_bbox_finalize(DevPlan d) {
     dy.miny = mny;
     dy.step = step;
     dy.inv_step = step > 0.0 ? 1.0 / step : 0.0;
+    // float key estimate: p and mn rounded to float (relative error 2^-24 each), their
+    // difference and the product with float(1 / step) rounded (2^-24 each); in box edges the
+    // error is at most ((|p| + |mn|) / step + 2 q) 2^-24 <= ((2 |mn| + |edge|) / step + 2 G) 2^-24;
+    // a factor 4 covers the remaining roundings
+    dy.minx_f = __double2float_rn(mnx);
+    dy.miny_f = __double2float_rn(mny);
+    dy.inv_step_f = __double2float_rn(dy.inv_step);
+    if (step > 0.0 && isfinite(step)) {
+        const double am = fmax(fabs(mnx), fabs(mny)), G = (double)d.sys[s].G;
+        const double tol = 4.0 * ((2.0 * am + G * step) / step + 2.0 * G) * 5.9604644775390625e-8;
+        dy.key_tol = tol < 0.25 ? (float)tol : 1.f;
+    } else {
+        dy.key_tol = 1.f;  // the FP64 key for every particle
+    }
 }
 
 // -------------------------------------------------------------------- place
@@ -140,9 +154,12 @@ __global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
             const SysDesc &sd = d.sys[s];
             const SysDyn &dy = d.dyn[s];
             double x = X[i], y = Y[i];
-            if (!(isfinite(x) && isfinite(y))) raise_err(d.glob, 1u /*BH_DEV_NAN_POSITION*/);
-            int kx = box_key1_fast(x, dy.minx, dy.step, dy.inv_step, sd.G);
-            int ky = box_key1_fast(y, dy.miny, dy.step, dy.inv_step, sd.G);
+            // finite test on the exponent bits (no FP64 operation)
+            const unsigned hx = (unsigned)(__double_as_longlong(x) >> 52) & 0x7FFu;
+            const unsigned hy = (unsigned)(__double_as_longlong(y) >> 52) & 0x7FFu;
+            if (hx == 0x7FFu || hy == 0x7FFu) raise_err(d.glob, 1u /*BH_DEV_NAN_POSITION*/);
+            int kx = box_key1_f32(x, dy.minx, dy.step, dy.inv_step, dy.minx_f, dy.inv_step_f, dy.key_tol, sd.G);
+            int ky = box_key1_f32(y, dy.miny, dy.step, dy.inv_step, dy.miny_f, dy.inv_step_f, dy.key_tol, sd.G);
             key = (int)(sd.boff + (long long)kx * sd.G + ky);
         }
         unsigned peers = __match_any_sync(0xffffffffu, key);
