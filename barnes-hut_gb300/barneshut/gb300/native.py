@@ -40,8 +40,9 @@ EXPORTS = (
     "bh_pair_counts", "bh_box_moments", "bh_grid_info", "bh_direct_sample", "bh_diagnostics",
     "bh_kernels_per_step", "bh_mlp_param_count", "bh_mlp_image_bytes", "bh_mlp_pack",
     "bh_mlp_forward", "bh_mlp_train_batch", "bh_mlp_adam", "bh_set_correction", "bh_learned_pairs",
-    "bh_direct_sum_noalloc",
+    "bh_direct_sum_noalloc", "bh_generate",
 )
+BH_GEN_UNIFORM, BH_GEN_GAUSS, BH_GEN_CLUSTER = 0, 1, 2
 BH_NOALLOC_MAX_TARGETS = 4096
 
 
@@ -117,6 +118,7 @@ def load_library(path=None):
     L.bh_set_correction.argtypes = [vp, vp, vp]
     L.bh_direct_sum_noalloc.argtypes = [vp, vp, vp, ll, vp, ll, d, d, vp, vp, vp]
     L.bh_learned_pairs.argtypes = [vp, d, d, i, ll, ll, i, vp, vp, vp, ll, vp]
+    L.bh_generate.argtypes = [i, ll, ctypes.c_ulonglong, vp, vp, vp, vp, vp, vp]
     for name in EXPORTS:
         f = getattr(L, name)
         if name not in ("bh_last_error",):
@@ -127,6 +129,20 @@ def load_library(path=None):
 
 def grid_dim(n, max_particles_per_box):
     return load_library().bh_grid_dim(int(n), int(max_particles_per_box))
+
+
+def generate(distribution, n, seed, device="cuda"):
+    """n particles drawn on the device (bh_generate): dict of FP64 tensors x, y, m, vx, vy."""
+    import torch
+
+    L = load_library()
+    out = {k: torch.empty(int(n), dtype=torch.float64, device=device) for k in ("x", "y", "m", "vx", "vy")}
+    st = torch.cuda.current_stream(out["x"].device).cuda_stream
+    rc = L.bh_generate(int(distribution), int(n), int(seed) & 0xFFFFFFFFFFFFFFFF,
+                       *[_ptr(out[k]) for k in ("x", "y", "m", "vx", "vy")], ctypes.c_void_p(st))
+    if rc != BH_OK:
+        raise BHError(rc, (L.bh_last_error(None) or b"").decode())
+    return out
 
 
 def make_params(grav_constant=1.0, tick_seconds=0.005, softening=0.0, cutoff_r2=1e-5,

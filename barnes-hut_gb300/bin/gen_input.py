@@ -1,7 +1,9 @@
 #!/usr/bin/env python3
 """Input generator with the interface of python-bh/bin/gen_input.py:15-33:
-gen_input.py <distribution> <num_particles> <fout> [--seed S]
-distributions: normal, gauss (as the reference), uniform01, cluster (seeded)."""
+gen_input.py <distribution> <num_particles> <fout> [--seed S] [--device]
+distributions: normal, gauss (as the reference), uniform01, cluster (seeded).
+--device draws normal / gauss / cluster on the GPU (bh_generate, Philox4x32-10 counters)
+instead of numpy on the host; the file format is the same."""
 import argparse
 import os
 import sys
@@ -16,9 +18,18 @@ if __name__ == "__main__":
     ap.add_argument("num_particles", type=int)
     ap.add_argument("fout")
     ap.add_argument("--seed", type=int, default=None)
+    ap.add_argument("--device", action="store_true", help="generate on the GPU")
     a = ap.parse_args()
     n = a.num_particles
-    if a.distribution in ("normal", "gauss"):
+    if a.device:
+        from barneshut.gb300 import native
+
+        kinds = {"normal": native.BH_GEN_UNIFORM, "gauss": native.BH_GEN_GAUSS, "cluster": native.BH_GEN_CLUSTER}
+        if a.distribution not in kinds:
+            sys.exit(f"--device supports {sorted(kinds)}")
+        out = native.generate(kinds[a.distribution], n, 0 if a.seed is None else a.seed)
+        data = tuple(out[k].cpu().numpy() for k in ("x", "y", "m", "vx", "vy"))
+    elif a.distribution in ("normal", "gauss"):
         data = workloads.gen_input(n, a.distribution, seed=a.seed)
     elif a.distribution == "uniform01":
         data = workloads.uniform(n, seed=0 if a.seed is None else a.seed)

@@ -303,6 +303,7 @@ static void fill_dev(bh_plan *p) {
     d.coff_tab = (const long long *)(w + p->o_coff);
     d.goff_tab = (const long long *)(w + p->o_goff);
     d.lvl_tab = (const long long *)(w + p->o_lvl);
+    for (int l = 0; l < p->Lmax && l < MAX_LEVELS; l++) d.lvl_cells[l] = p->lvl[(size_t)l * (p->nsys + 1) + p->nsys];
     for (int b = 0; b < 2; b++) {
         d.X[b] = (double *)(w + p->o_X[b]);
         d.Y[b] = (double *)(w + p->o_Y[b]);

@@ -79,6 +79,7 @@ struct DevPlan {
     const long long *coff_tab;  // nsys + 1 cell offsets
     const long long *goff_tab;  // nsys + 1 group offsets
     const long long *lvl_tab;   // Lmax x (nsys + 1): prefix of level-l cells over systems
+    long long lvl_cells[MAX_LEVELS];  // level-l cells over all systems (host copy, sizes grids)
     double *X[2], *Y[2], *VX[2], *VY[2], *M[2];
     int *PID[2];
     double *AX, *AY;  // accelerations, box-sorted order

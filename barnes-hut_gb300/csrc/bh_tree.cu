@@ -534,9 +534,8 @@ cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st) {
     if (d.n_total > 0) k_leaf_moments<<<grid_for(d.n_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
     for (int l = 1; l < d.Lmax; l++) {
-        // level-l cell count across systems is known on the host side of the
-        // plan; the kernel reads it from lvl_tab, so launch a generous grid.
-        k_pyramid_level<<<152 * 4, TPB, 0, st>>>(d, l);
+        // the level's cell count over all systems is known on the host: one thread per cell
+        k_pyramid_level<<<grid_for(d.lvl_cells[l], TPB, 152LL * 4), TPB, 0, st>>>(d, l);
     }
     k_records<<<grid_for(d.C_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
     return cudaGetLastError();

@@ -268,6 +268,22 @@ int bh_learned_pairs(bh_plan *plan, double theta_hi, double theta_lo, int max_le
                      float *feats, float *targets, unsigned *counter, long long capacity,
                      void *stream);
 
+/* ------------------------------------------------------------ input generators
+ * Replaces python-bh/bin/gen_input.py:38-55 (per-particle host loop) with a device
+ * generator: n particles into caller-owned device arrays (FP64), a pure function of
+ * (distribution, n, seed) -- Philox4x32-10 counters per particle.
+ *   BH_GEN_UNIFORM: x, y uniform in [0, 499) (gen_input.py "normal"), v uniform in
+ *                   [-1, 1), m uniform in [0.5, 5)
+ *   BH_GEN_GAUSS:   x, y ~ N(249.5, (499 / 12)^2) (gen_input.py "gauss"), v and m as above
+ *   BH_GEN_CLUSTER: 8 Gaussian clusters (sigma 0.05, centres uniform in [0.2, 0.8)^2) with
+ *                   20 % uniform background on [0, 1)^2, m uniform in [1, 2), v = 0
+ * No plan needed; asynchronous on stream; errors via bh_last_error(NULL). */
+#define BH_GEN_UNIFORM 0
+#define BH_GEN_GAUSS 1
+#define BH_GEN_CLUSTER 2
+int bh_generate(int distribution, long long n, unsigned long long seed, double *x, double *y,
+                double *m, double *vx, double *vy, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
