@@ -31,6 +31,7 @@ BH_PREC_FP64 = 2
 BH_FLAG_LEARNED = 1
 BH_FLAG_WALK = 2
 BH_STREAM_DENSE_MIN = 64  # include/bh_gb300.h
+BH_STREAM_QUAD_MIN = 128
 
 # every symbol include/bh_gb300.h declares
 EXPORTS = (
@@ -69,6 +70,7 @@ class Params(ctypes.Structure):
         ("tune", ctypes.c_int),
         ("correction_theta", ctypes.c_double),
         ("dense_min", ctypes.c_int),
+        ("quad_min", ctypes.c_int),
     ]
 
 
@@ -147,10 +149,10 @@ def generate(distribution, n, seed, device="cuda"):
 
 def make_params(grav_constant=1.0, tick_seconds=0.005, softening=0.0, cutoff_r2=1e-5,
                 theta=0.0, group_dim=0, precision=BH_PREC_FP32_KAHAN, flags=0, tune=0,
-                correction_theta=0.0, dense_min=0):
+                correction_theta=0.0, dense_min=0, quad_min=0):
     return Params(float(grav_constant), float(tick_seconds), float(softening), float(cutoff_r2),
                   float(theta), int(group_dim), int(precision), int(flags), int(tune),
-                  float(correction_theta), int(dense_min))
+                  float(correction_theta), int(dense_min), int(quad_min))
 
 
 def _ptr(t):

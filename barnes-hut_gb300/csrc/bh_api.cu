@@ -30,10 +30,11 @@ struct bh_plan {
     size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
     size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_tiles, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
-        o_rec2, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk;
+        o_rec2, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk, o_qcnt;
     bool stream = false;  // theta-mode interaction lists built once per group and streamed
     int chunk = TARGET_CHUNK;
     int dense_min = BH_STREAM_DENSE_MIN;
+    int quad_min = BH_STREAM_QUAD_MIN;
     void *ws = nullptr;
     int device = -1;
     DevPlan dev;
@@ -180,6 +181,7 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->chunk = p->stream ? STREAM_CHUNK : TARGET_CHUNK;
     if (pr.dense_min < 0) return bad("dense_min < 0");
     p->dense_min = pr.dense_min > 0 ? pr.dense_min : BH_STREAM_DENSE_MIN;
+    p->quad_min = pr.quad_min > 0 ? pr.quad_min : (pr.quad_min == 0 ? BH_STREAM_QUAD_MIN : 0);
     long long lf_total = 0, ln_total = 0;
     if (p->stream) {
         // a level's accepted cells are a subset of its frontier (at most FRONTIER_CAP cells), and
@@ -203,8 +205,8 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->B_total = p->boff[nsys];
     p->C_total = p->coff[nsys];
     p->NG_total = p->goff[nsys];
-    if (p->n_total >= (1LL << 31) || p->C_total >= (1LL << 31) || p->B_total >= (1LL << 31))
-        return bad("total particles, boxes or cells >= 2^31");
+    if (p->n_total >= (1LL << 31) || p->C_total >= (1LL << 31) || p->B_total >= (1LL << 29))
+        return bad("total particles or cells >= 2^31, or boxes >= 2^29");
     // level tables: prefix of level-l cell counts over systems
     p->lvl.assign((size_t)p->Lmax * (nsys + 1), 0);
     for (int l = 0; l < p->Lmax; l++)
@@ -244,6 +246,7 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_slot = take(4 * N);
     p->o_skey = take(4 * N);
     p->o_counts = take(4 * B);
+    p->o_qcnt = take(16 * B);
     p->o_bstart = take(4 * (B + 1));
     p->o_tiles = take(4 * (B / 4096 + 2));
     p->o_icnt = take(4 * (size_t)p->NG_total);
@@ -252,7 +255,10 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_lfar = take(4 * (size_t)lf_total);
     p->o_lnear = take(16 * (size_t)ln_total);
     p->o_lcnt = take(p->stream ? 8 * (size_t)p->NG_total : 0);
-    const size_t sitems = p->stream ? (size_t)p->NG_total + N / p->dense_min + N / p->chunk + 1 : 0;
+    // at most one partial chunk per sparse set, dense box and quadrant of a quadrant box
+    const size_t sitems = p->stream ? (size_t)p->NG_total + N / p->dense_min +
+                                          (p->quad_min > 0 ? 4 * (N / p->quad_min) : 0) + N / p->chunk + 1
+                                    : 0;
     p->o_iord = take(4 * sitems);
     p->o_sicnt = take(p->stream ? 4 * (size_t)p->NG_total : 0);
     p->o_sioff = take(p->stream ? 4 * ((size_t)p->NG_total + 1) : 0);
@@ -320,6 +326,7 @@ static void fill_dev(bh_plan *p) {
     d.slot = (int *)(w + p->o_slot);
     d.skey = (int *)(w + p->o_skey);
     d.counts = (int *)(w + p->o_counts);
+    d.qcounts = (int *)(w + p->o_qcnt);
     d.box_start = (int *)(w + p->o_bstart);
     d.tile_sums = (int *)(w + p->o_tiles);
     d.item_cnt = (int *)(w + p->o_icnt);
@@ -338,6 +345,7 @@ static void fill_dev(bh_plan *p) {
     d.sitem_sub = (int *)(w + p->o_sisub);
     d.sitem_chunk = (int2 *)(w + p->o_sichk);
     d.dense_min = p->dense_min;
+    d.quad_min = p->quad_min;
     d.item_bucket = (int *)(w + p->o_ibkt);
     d.stream = p->stream ? 1 : 0;
     d.chunk = p->chunk;

@@ -101,8 +101,9 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         const int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
         const int gx0 = gi * TG, gy0 = gj * TG;
         // the item's targets: runs of box-sorted particles, one per box of the group (column-major;
-        // a box outside the item's set is an empty run)
+        // a box outside the item's set is an empty run; a quadrant item's box run is the quadrant)
         const int nrun = TG * TG;
+        const int qbox = sub >= nrun ? (sub - nrun) >> 2 : -1, quad = sub >= nrun ? (sub - nrun) & 3 : 0;
         {
             int carry = 0;
             for (int b0 = 0; b0 < nrun; b0 += 32) {
@@ -114,7 +115,17 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                         const long long bb = sd.boff + (long long)(gx0 + cx) * G + gy0 + cy;
                         st = d.box_start[bb];
                         len = d.box_start[bb + 1] - st;
-                        if (sub >= 0 ? b != sub : len >= d.dense_min) len = 0;
+                        if (qbox >= 0) {
+                            if (b != qbox) {
+                                len = 0;
+                            } else {
+                                const int4 qc = reinterpret_cast<const int4 *>(d.qcounts)[bb];
+                                st += (quad > 0 ? qc.x : 0) + (quad > 1 ? qc.y : 0) + (quad > 2 ? qc.z : 0);
+                                len = quad == 0 ? qc.x : quad == 1 ? qc.y : quad == 2 ? qc.z : qc.w;
+                            }
+                        } else if (sub >= 0 ? b != sub : box_item_kind(len, d.dense_min, d.quad_min) != 0) {
+                            len = 0;
+                        }
                     }
                 }
                 int inc = len;
@@ -259,11 +270,23 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                 }
                 __syncwarp();
             } else {
-                // a dense box's own lists: a near leaf of the group that passes the opening test
-                // against the single box (its offsets taken relative to the box origin) is swept
-                // as a far entry; the others stay near and are re-prefixed
-                const int bcx = sub / TG, bcy = sub - bcx * TG;
-                const float oxb = __fmul_rn((float)bcx, step_f), oyb = __fmul_rn((float)bcy, step_f);
+                // a dense box's (or quadrant's) own lists: a near leaf of the group that passes the
+                // opening test against the single box or quadrant (its offsets taken relative to
+                // that rectangle's origin) is swept as a far entry; the others stay near and are
+                // re-prefixed
+                const int bsel = qbox >= 0 ? qbox : sub;
+                const int bcx = bsel / TG, bcy = bsel - bcx * TG;
+                float oxb, oyb, wr;  // rectangle origin in the group frame, edge
+                if (qbox >= 0) {
+                    const float half_f = 0.5f * step_f;
+                    oxb = __fmul_rn((float)(2 * bcx + (quad >> 1)), half_f);
+                    oyb = __fmul_rn((float)(2 * bcy + (quad & 1)), half_f);
+                    wr = half_f;
+                } else {
+                    oxb = __fmul_rn((float)bcx, step_f);
+                    oyb = __fmul_rn((float)bcy, step_f);
+                    wr = step_f;
+                }
                 const float s2 = __fmul_rn(step_f, step_f), theta2 = d.theta2_f;
                 const int own = (gx0 + bcx) * G + (gy0 + bcy);
                 int nkeep = 0, nacc = 0, base = 0;
@@ -279,8 +302,8 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                         if (e1.x != own) {
                             const float rxb = __fsub_rn(__int_as_float(e1.z), oxb);
                             const float ryb = __fsub_rn(__int_as_float(e1.w), oyb);
-                            const float dxo = fmaxf(0.f, fmaxf(-rxb, __fsub_rn(rxb, step_f)));
-                            const float dyo = fmaxf(0.f, fmaxf(-ryb, __fsub_rn(ryb, step_f)));
+                            const float dxo = fmaxf(0.f, fmaxf(-rxb, __fsub_rn(rxb, wr)));
+                            const float dyo = fmaxf(0.f, fmaxf(-ryb, __fsub_rn(ryb, wr)));
                             const float d2 = __fadd_rn(__fmul_rn(dxo, dxo), __fmul_rn(dyo, dyo));
                             acc = s2 < __fmul_rn(theta2, d2);
                         }

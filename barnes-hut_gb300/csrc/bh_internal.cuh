@@ -88,6 +88,8 @@ struct DevPlan {
                  // near-field record, staged into shared memory by bulk copies
     int *key, *slot, *skey;
     int *counts, *box_start, *tile_sums;
+    int *qcounts;  // per box, particles in each quadrant (x half * 2 + y half); a box's particles
+                   // are stored quadrant by quadrant
     int *item_cnt, *item_off, *item_group;  // force work items (group, target chunk)
     double *mom;
     float4 *rec, *rec2;
@@ -106,6 +108,8 @@ struct DevPlan {
     int *sitem_cnt, *sitem_off, *sitem_group, *sitem_sub;
     int2 *sitem_chunk;
     int dense_min;
+    int quad_min;  // list streaming: boxes with at least this many particles get per-quadrant
+                   // work items and near lists (0: none)
     int *item_order;  // list-streaming work items, heaviest cost bucket first
     int *item_bucket;  // ITEM_BUCKETS counts + ITEM_BUCKETS cursors
     int stream;  // 1: lists are built by k_lists and streamed by k_fstream
@@ -183,6 +187,37 @@ __device__ __forceinline__ int box_key1_f32(double p, double mn, double step, do
     const float fr = q - k;
     if (!(tol < 0.25f) || fr < tol || fr > 1.f - tol) return box_key1_fast(p, mn, step, inv, G);
     return min(max((int)k, 0), G - 1);
+}
+
+// Key of one coordinate at twice the box resolution: clip(floor(2 q), 0, 2 G - 1) with q the
+// FP64 quotient (p - mn) / step of box_key1.  Its high part (>> 1) is box_key1's key (floor(2 q)
+// >> 1 = floor(q) for q >= 0, and the clips agree), its low bit the half of the box.
+__device__ __forceinline__ int half_key1_fast(double p, double mn, double step, double inv, int G) {
+    if (!(step > 0.0)) return 0;
+    double d = __dsub_rn(p, mn);
+    double q = __dmul_rn(__dmul_rn(d, inv), 2.0);
+    double k = floor(q);
+    double fr = q - k;
+    if (fr < 1e-10 || fr > 1.0 - 1e-10) k = floor(__dmul_rn(__ddiv_rn(d, step), 2.0));
+    k = fmin(fmax(k, 0.0), (double)(2 * G - 1));
+    return (int)k;
+}
+// The same from the float estimate (2 q_f carries twice box_key1_f32's error bound).
+__device__ __forceinline__ int half_key1_f32(double p, double mn, double step, double inv, float mn_f,
+                                             float inv_f, float tol, int G) {
+    const float q = 2.f * __fmul_rn(__fsub_rn(__double2float_rn(p), mn_f), inv_f);
+    const float k = floorf(q);
+    const float fr = q - k;
+    const float tol2 = 2.f * tol;
+    if (!(tol2 < 0.25f) || fr < tol2 || fr > 1.f - tol2) return half_key1_fast(p, mn, step, inv, G);
+    return min(max((int)k, 0), 2 * G - 1);
+}
+
+// Work-item kind of a box with nb particles (list streaming): 2 per-quadrant items, 1 own items,
+// 0 shared with the group's other sparse boxes.
+__device__ __forceinline__ int box_item_kind(int nb, int dense_min, int quad_min) {
+    if (quad_min > 0 && nb >= quad_min) return 2;
+    return nb >= dense_min ? 1 : 0;
 }
 
 // Origin of leaf box k along one axis: mn + k * step, FP64, no contraction.

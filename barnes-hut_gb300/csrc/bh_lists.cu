@@ -191,12 +191,18 @@ __device__ __forceinline__ int item_cost_bucket(const DevPlan &d, long long item
     const int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
     const int gx0 = gi * sd.TG, gy0 = gj * sd.TG;
     const int gx1 = min(sd.G, gx0 + sd.TG), gy1 = min(sd.G, gy0 + sd.TG);
-    int nt = 0;  // the item's target set: one dense box, or the group's sparse boxes
+    const int nbox = sd.TG * sd.TG;
+    int nt = 0;  // the item's target set: a quadrant, one dense box, or the group's sparse boxes
     for (int c = gx0; c < gx1; c++)
         for (int r = gy0; r < gy1; r++) {
             const long long b = sd.boff + (long long)c * sd.G + r;
             const int nb = d.box_start[b + 1] - d.box_start[b];
-            if (sub >= 0 ? (c - gx0) * sd.TG + (r - gy0) == sub : nb < d.dense_min) nt += nb;
+            const int bi = (c - gx0) * sd.TG + (r - gy0);
+            if (sub >= nbox) {
+                if (bi == (sub - nbox) >> 2) nt += d.qcounts[4 * b + ((sub - nbox) & 3)];
+            } else if (sub >= 0 ? bi == sub : box_item_kind(nb, d.dense_min, d.quad_min) == 0) {
+                nt += nb;
+            }
         }
     int c0, T;
     sitem_range(nt, ck.x, &c0, &T);
@@ -257,7 +263,8 @@ cudaError_t launch_lists(const DevPlan &d, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(d.item_bucket, 0, sizeof(int) * 2 * ITEM_BUCKETS, st);
     if (e != cudaSuccess) return e;
-    long long items_max = d.NG_total + d.n_total / d.dense_min + d.n_total / d.chunk + 1;  // >= items
+    long long items_max = d.NG_total + d.n_total / d.dense_min +
+                          (d.quad_min > 0 ? 4 * (d.n_total / d.quad_min) : 0) + d.n_total / d.chunk + 1;  // >= items
     long long ig = (items_max + 255) / 256;
     if (ig > 152LL * 8) ig = 152LL * 8;
     k_item_hist<<<(unsigned)ig, 256, 0, st>>>(d);

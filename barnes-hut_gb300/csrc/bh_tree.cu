@@ -37,6 +37,7 @@ __global__ void k_prologue(DevPlan d) {
     }
     for (long long b = tid; b < d.B_total; b += stride) {
         d.counts[b] = 0;
+        reinterpret_cast<int4 *>(d.qcounts)[b] = make_int4(0, 0, 0, 0);
         int s = find_seg(d.boff_tab, d.nsys, b);
         long long c = d.sys[s].coff + (b - d.sys[s].boff);
         double *q = d.mom + 6 * c;
@@ -137,9 +138,9 @@ __global__ void k_bbox_finalize(DevPlan d) {
 }
 
 // -------------------------------------------------------------------- place
-// FP64 box keys (bit-exact with the reference), warp-aggregated histogram:
-// lanes with the same key elect one leader that adds the group's size; each
-// lane's rank in the group plus the leader's old count is its slot in the box.
+// Box keys bit-exact with the reference's FP64 keys (computed at twice the box resolution, so
+// each particle also gets its quadrant within the box), and a warp-aggregated histogram of
+// boxes and of (box, quadrant) pairs; a particle's slot is its rank within its quadrant.
 __global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
     const int cur = d.glob->epoch & 1;
     const double *X = d.X[cur], *Y = d.Y[cur];
@@ -158,18 +159,26 @@ __global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
             const unsigned hx = (unsigned)(__double_as_longlong(x) >> 52) & 0x7FFu;
             const unsigned hy = (unsigned)(__double_as_longlong(y) >> 52) & 0x7FFu;
             if (hx == 0x7FFu || hy == 0x7FFu) raise_err(d.glob, 1u /*BH_DEV_NAN_POSITION*/);
-            int kx = box_key1_f32(x, dy.minx, dy.step, dy.inv_step, dy.minx_f, dy.inv_step_f, dy.key_tol, sd.G);
-            int ky = box_key1_f32(y, dy.miny, dy.step, dy.inv_step, dy.miny_f, dy.inv_step_f, dy.key_tol, sd.G);
-            key = (int)(sd.boff + (long long)kx * sd.G + ky);
+            // keys at twice the box resolution: box key and quadrant within the box
+            const int k2x = half_key1_f32(x, dy.minx, dy.step, dy.inv_step, dy.minx_f, dy.inv_step_f, dy.key_tol, sd.G);
+            const int k2y = half_key1_f32(y, dy.miny, dy.step, dy.inv_step, dy.miny_f, dy.inv_step_f, dy.key_tol, sd.G);
+            const int box = (int)(sd.boff + (long long)(k2x >> 1) * sd.G + (k2y >> 1));
+            key = 4 * box + (k2x & 1) * 2 + (k2y & 1);
         }
+        // lanes with the same (box, quadrant) elect one leader that adds the group's size to the
+        // box count (the scan's input) and to the quadrant count, whose old value is the group's
+        // first slot in the quadrant
         unsigned peers = __match_any_sync(0xffffffffu, key);
         int leader = __ffs(peers) - 1;
         int rank = __popc(peers & ((1u << lane) - 1u));
         int old = 0;
-        if (lane == leader && key >= 0) old = atomicAdd(&d.counts[key], __popc(peers));
+        if (lane == leader && key >= 0) {
+            atomicAdd(&d.counts[key >> 2], __popc(peers));
+            old = atomicAdd(&d.qcounts[key], __popc(peers));
+        }
         old = __shfl_sync(0xffffffffu, old, leader);
         if (i < d.n_total) {
-            d.key[i] = key;
+            d.key[i] = key;  // 4 * box + quadrant
             d.slot[i] = old + rank;
         }
     }
@@ -291,9 +300,11 @@ __global__ void __launch_bounds__(TPB) k_fill_items(DevPlan d) {
 }
 
 // List-streaming work items.  Per group: the boxes holding fewer than dense_min particles share
-// ceil(n_sparse / chunk) items (sub = -1); every other box gets ceil(n_box / chunk) items of its
-// own (sub = cx * TG + cy), which use per-box refined near lists.  Chunks split their targets
-// into full chunks of STREAM_CHUNK and a remainder (sitem_range).
+// ceil(n_sparse / chunk) items (sub = -1); every denser box gets ceil(n_box / chunk) items of its
+// own (sub = cx * TG + cy), which use per-box refined near lists, and a box holding at least
+// quad_min particles gets items per quadrant instead (sub = TG^2 + 4 (cx * TG + cy) + quadrant),
+// which use per-quadrant refined near lists.  Chunks split their targets into full chunks of
+// STREAM_CHUNK and a remainder (sitem_range).
 __global__ void __launch_bounds__(TPB) k_sitem_count(DevPlan d) {
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < d.NG_total; g += stride) {
@@ -308,8 +319,14 @@ __global__ void __launch_bounds__(TPB) k_sitem_count(DevPlan d) {
             for (int r = gy0; r < gy1; r++) {
                 const long long b = sd.boff + (long long)c * sd.G + r;
                 const int nb = d.box_start[b + 1] - d.box_start[b];
-                if (nb >= d.dense_min) cnt += (nb + d.chunk - 1) / d.chunk;
-                else sparse += nb;
+                const int kind = box_item_kind(nb, d.dense_min, d.quad_min);
+                if (kind == 2) {
+                    for (int q = 0; q < 4; q++) cnt += (d.qcounts[4 * b + q] + d.chunk - 1) / d.chunk;
+                } else if (kind == 1) {
+                    cnt += (nb + d.chunk - 1) / d.chunk;
+                } else {
+                    sparse += nb;
+                }
             }
         d.sitem_cnt[g] = cnt + (sparse + d.chunk - 1) / d.chunk;
     }
@@ -324,13 +341,14 @@ __global__ void __launch_bounds__(TPB) k_sitem_fill(DevPlan d) {
         int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
         int gx0 = gi * sd.TG, gy0 = gj * sd.TG;
         int gx1 = min(sd.G, gx0 + sd.TG), gy1 = min(sd.G, gy0 + sd.TG);
+        const int nbox = sd.TG * sd.TG;
         int o = d.sitem_off[g];
         int sparse = 0;
         for (int c = gx0; c < gx1; c++)
             for (int r = gy0; r < gy1; r++) {
                 const long long b = sd.boff + (long long)c * sd.G + r;
                 const int nb = d.box_start[b + 1] - d.box_start[b];
-                if (nb < d.dense_min) sparse += nb;
+                if (box_item_kind(nb, d.dense_min, d.quad_min) == 0) sparse += nb;
             }
         const int ns = (sparse + d.chunk - 1) / d.chunk;
         for (int k = 0; k < ns; k++, o++) {
@@ -342,19 +360,32 @@ __global__ void __launch_bounds__(TPB) k_sitem_fill(DevPlan d) {
             for (int r = gy0; r < gy1; r++) {
                 const long long b = sd.boff + (long long)c * sd.G + r;
                 const int nb = d.box_start[b + 1] - d.box_start[b];
-                if (nb < d.dense_min) continue;
-                const int nk = (nb + d.chunk - 1) / d.chunk;
-                for (int k = 0; k < nk; k++, o++) {
-                    d.sitem_group[o] = (int)g;
-                    d.sitem_sub[o] = (c - gx0) * sd.TG + (r - gy0);
-                    d.sitem_chunk[o] = make_int2(k, nk);
+                const int kind = box_item_kind(nb, d.dense_min, d.quad_min);
+                const int bi = (c - gx0) * sd.TG + (r - gy0);
+                if (kind == 1) {
+                    const int nk = (nb + d.chunk - 1) / d.chunk;
+                    for (int k = 0; k < nk; k++, o++) {
+                        d.sitem_group[o] = (int)g;
+                        d.sitem_sub[o] = bi;
+                        d.sitem_chunk[o] = make_int2(k, nk);
+                    }
+                } else if (kind == 2) {
+                    for (int q = 0; q < 4; q++) {
+                        const int nk = (d.qcounts[4 * b + q] + d.chunk - 1) / d.chunk;
+                        for (int k = 0; k < nk; k++, o++) {
+                            d.sitem_group[o] = (int)g;
+                            d.sitem_sub[o] = nbox + 4 * bi + q;
+                            d.sitem_chunk[o] = make_int2(k, nk);
+                        }
+                    }
                 }
             }
     }
 }
 
 // ------------------------------------------------------------------ scatter
-// Counting-sort scatter into box order: destination = box_start[key] + slot.
+// Counting-sort scatter into box order, each box's particles quadrant by quadrant:
+// destination = box_start[box] + (particles of the box's earlier quadrants) + slot.
 // Writes the FP64 state of the next buffer, the packed float4 record (offsets
 // from the box origin computed in FP64, rounded once to float) and the
 // per-sorted-particle key.
@@ -362,8 +393,11 @@ __global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
     const int cur = d.glob->epoch & 1, nxt = cur ^ 1;
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < d.n_total; i += stride) {
-        int key = d.key[i];
-        int dst = d.box_start[key] + d.slot[i];
+        const int key4 = d.key[i];
+        const int key = key4 >> 2, quad = key4 & 3;
+        const int4 qc = reinterpret_cast<const int4 *>(d.qcounts)[key];
+        const int qpre = (quad > 0 ? qc.x : 0) + (quad > 1 ? qc.y : 0) + (quad > 2 ? qc.z : 0);
+        int dst = d.box_start[key] + qpre + d.slot[i];
         int s = find_seg(d.boff_tab, d.nsys, key);
         const SysDesc &sd = d.sys[s];
         const SysDyn &dy = d.dyn[s];

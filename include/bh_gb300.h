@@ -56,6 +56,10 @@ extern "C" {
    whose centre of mass passes the opening test against the single box becomes a far entry for
    that box's particles. */
 #define BH_STREAM_DENSE_MIN 64
+/* ... and a box holding at least bh_params.quad_min particles is evaluated quadrant by
+   quadrant (its particles are stored quadrant by quadrant), each quadrant with the near leaves
+   that fail the opening test against that quarter of the box. */
+#define BH_STREAM_QUAD_MIN 128
 #define BH_FLAG_WALK 2    /* theta mode: walk the cell pyramid inside the force kernel for
                            every work item instead of building each target group's
                            interaction lists once and streaming them (the default for
@@ -80,6 +84,9 @@ typedef struct bh_params {
                                 not at correction_theta get the learned correction */
     int dense_min;        /* list streaming: boxes with at least this many particles get
                              per-box refined near lists (0 = BH_STREAM_DENSE_MIN) */
+    int quad_min;         /* list streaming: boxes with at least this many particles get
+                             per-quadrant refined near lists (0 = BH_STREAM_QUAD_MIN,
+                             < 0 = none) */
 } bh_params;
 
 typedef struct bh_plan bh_plan;

@@ -636,17 +636,32 @@ void oref_moments(long long n, const double *x, const double *y, const double *m
  * per-box lists refined from their group's lists -- a near leaf whose centre of mass passes the
  * opening test against the single box (same float arithmetic as the CUDA list-streaming kernel:
  * offsets in the group frame, then relative to the box origin) becomes a far entry for those
- * targets.  dense_min <= 0 keeps the group lists for every target (the walking force kernel).
+ * targets.  quad_min > 0: a box holding at least quad_min particles is refined quadrant by
+ * quadrant instead (the test against the quarter of the box that holds the target; a particle's
+ * quadrant is the low bit of its FP64 key at twice the box resolution).  dense_min <= 0 and
+ * quad_min <= 0 keep the group lists for every target (the walking force kernel).
  */
 int oref_theta_evaluate(long long n, const double *x, const double *y, const double *m, int G,
                         int TG, double theta, double eps2, double cutoff, double gconst,
-                        double *ax, double *ay, long long *counts, int nthreads, int dense_min)
+                        double *ax, double *ay, long long *counts, int nthreads, int dense_min,
+                        int quad_min)
 {
     if (n <= 0) return 0;
     double bb[5];
     oref_bbox(n, x, y, G, bb);
     int *kx = (int *)malloc(sizeof(int) * (size_t)n), *ky = (int *)malloc(sizeof(int) * (size_t)n);
     oref_keys(n, x, y, G, bb, kx, ky);
+    /* quadrant of each particle within its box: the low bits of the keys at twice the box
+     * resolution, clip(floor(2 (p - min) / step), 0, 2 G - 1) (x half * 2 + y half) */
+    int *quad = (int *)malloc(sizeof(int) * (size_t)n);
+    for (long long i = 0; i < n; i++) {
+        double k2x = floor(2.0 * ((x[i] - bb[0]) / bb[4])), k2y = floor(2.0 * ((y[i] - bb[1]) / bb[4]));
+        if (k2x < 0.0) k2x = 0.0;
+        if (k2x > 2.0 * G - 1.0) k2x = 2.0 * G - 1.0;
+        if (k2y < 0.0) k2y = 0.0;
+        if (k2y > 2.0 * G - 1.0) k2y = 2.0 * G - 1.0;
+        quad[i] = ((int)k2x & 1) * 2 + ((int)k2y & 1);
+    }
     long long B = (long long)G * G, ncell = oref_pyramid_cells(G);
     int L = oref_num_levels(G);
     double *mom = (double *)malloc(sizeof(double) * 6 * (size_t)ncell);
@@ -762,81 +777,105 @@ int oref_theta_evaluate(long long n, const double *x, const double *y, const dou
                 const long long bb0 = (long long)bx * G + by;
                 const long long nb = bstart[bb0 + 1] - bstart[bb0];
                 if (nb == 0) continue;
-                /* this box's lists: the group's, or the refined per-box lists of a dense box */
-                const long long *nl = near;
-                long long nnl = nnear, nacc = 0;
-                if (!flat && dense_min > 0 && nb >= dense_min) {
-                    const float ox = (float)(bx - gx0) * step_f, oy = (float)(by - gy0) * step_f;
-                    nnl = 0;
-                    for (long long q = 0; q < nnear; q++) {
-                        const long long c = near[q];
-                        const int qi = (int)(c / G), qj = (int)(c % G);
-                        int acc = 0;
-                        if (!(qi == bx && qj == by)) {
-                            float rx = (float)(qi - gx0) * step_f + rec[4 * c];
-                            float ry = (float)(qj - gy0) * step_f + rec[4 * c + 1];
-                            float rxb = rx - ox, ryb = ry - oy;
-                            float dxo = fmaxf(0.0f, fmaxf(-rxb, rxb - step_f));
-                            float dyo = fmaxf(0.0f, fmaxf(-ryb, ryb - step_f));
-                            float d2 = dxo * dxo + dyo * dyo;
-                            acc = (step_f * step_f) < (theta2_f * d2);
+                /* the box's target sets: the whole box with the group's lists (sparse box) or with
+                 * per-box refined lists (dense box), or its four quadrants, each with lists refined
+                 * against the quadrant (box with at least quad_min particles) */
+                int kind = 0;
+                if (!flat && quad_min > 0 && nb >= quad_min)
+                    kind = 2;
+                else if (!flat && dense_min > 0 && nb >= dense_min)
+                    kind = 1;
+                for (int part = 0; part < (kind == 2 ? 4 : 1); part++) {
+                    long long nt_part = 0;
+                    for (long long k = bstart[bb0]; k < bstart[bb0 + 1]; k++)
+                        if (kind != 2 || quad[order[k]] == part) nt_part++;
+                    if (nt_part == 0) continue;
+                    const long long *nl = near;
+                    long long nnl = nnear, nacc = 0;
+                    if (kind > 0) {
+                        float ox, oy, wr;  /* rectangle origin in the group frame, edge */
+                        if (kind == 2) {
+                            const float half_f = 0.5f * step_f;
+                            ox = (float)(2 * (bx - gx0) + (part >> 1)) * half_f;
+                            oy = (float)(2 * (by - gy0) + (part & 1)) * half_f;
+                            wr = half_f;
+                        } else {
+                            ox = (float)(bx - gx0) * step_f;
+                            oy = (float)(by - gy0) * step_f;
+                            wr = step_f;
                         }
-                        if (acc)
-                            bfar[nacc++] = c; /* a leaf: level 0, cell index = box index */
-                        else
-                            bnear[nnl++] = c;
+                        nnl = 0;
+                        for (long long q = 0; q < nnear; q++) {
+                            const long long c = near[q];
+                            const int qi = (int)(c / G), qj = (int)(c % G);
+                            int acc = 0;
+                            if (!(qi == bx && qj == by)) {
+                                float rx = (float)(qi - gx0) * step_f + rec[4 * c];
+                                float ry = (float)(qj - gy0) * step_f + rec[4 * c + 1];
+                                float rxb = rx - ox, ryb = ry - oy;
+                                float dxo = fmaxf(0.0f, fmaxf(-rxb, rxb - wr));
+                                float dyo = fmaxf(0.0f, fmaxf(-ryb, ryb - wr));
+                                float d2 = dxo * dxo + dyo * dyo;
+                                acc = (step_f * step_f) < (theta2_f * d2);
+                            }
+                            if (acc)
+                                bfar[nacc++] = c; /* a leaf: level 0, cell index = box index */
+                            else
+                                bnear[nnl++] = c;
+                        }
+                        nl = bnear;
                     }
-                    nl = bnear;
-                }
-                long long nsrc = 0;
-                for (long long q = 0; q < nnl; q++) nsrc += bstart[nl[q] + 1] - bstart[nl[q]];
-                cnt_near += nb * nsrc;
-                cnt_far += nb * (nfar + nacc);
-            for (long long k = bstart[bb0]; k < bstart[bb0 + 1]; k++) {
-                long long t = order[k];
-                double xt = x[t], yt = y[t], sx = 0.0, sy = 0.0;
-                for (long long q = 0; q < nacc; q++) {
-                    long long cell = bfar[q];
-                    int ci = (int)(cell / G), cj = (int)(cell % G);
-                    const double *qm = mom + 6 * cell;
-                    double cx = (bb[0] + (double)ci * bb[4]) + qm[1] / qm[0];
-                    double cy = (bb[1] + (double)cj * bb[4]) + qm[2] / qm[0];
-                    double dx = cx - xt, dy = cy - yt;
-                    double r2 = dx * dx + dy * dy;
-                    if (!(r2 > cutoff)) continue;
-                    double w = qm[0] / (r2 + eps2);
-                    sx += w * dx;
-                    sy += w * dy;
-                }
-                for (long long q = 0; q < nnl; q++)
-                    for (long long kk = bstart[nl[q]]; kk < bstart[nl[q] + 1]; kk++) {
-                        long long j = order[kk];
-                        double dx = x[j] - xt, dy = y[j] - yt;
-                        double r2 = dx * dx + dy * dy;
-                        if (!(r2 > cutoff)) continue;
-                        double w = m[j] / (r2 + eps2);
-                        sx += w * dx;
-                        sy += w * dy;
+                    long long nsrc = 0;
+                    for (long long q = 0; q < nnl; q++) nsrc += bstart[nl[q] + 1] - bstart[nl[q]];
+                    cnt_near += nt_part * nsrc;
+                    cnt_far += nt_part * (nfar + nacc);
+                    for (long long k = bstart[bb0]; k < bstart[bb0 + 1]; k++) {
+                        long long t = order[k];
+                        if (kind == 2 && quad[t] != part) continue;
+                        double xt = x[t], yt = y[t], sx = 0.0, sy = 0.0;
+                        for (long long q = 0; q < nacc; q++) {
+                            long long cell = bfar[q];
+                            int ci = (int)(cell / G), cj = (int)(cell % G);
+                            const double *qm = mom + 6 * cell;
+                            double cx = (bb[0] + (double)ci * bb[4]) + qm[1] / qm[0];
+                            double cy = (bb[1] + (double)cj * bb[4]) + qm[2] / qm[0];
+                            double dx = cx - xt, dy = cy - yt;
+                            double r2 = dx * dx + dy * dy;
+                            if (!(r2 > cutoff)) continue;
+                            double w = qm[0] / (r2 + eps2);
+                            sx += w * dx;
+                            sy += w * dy;
+                        }
+                        for (long long q = 0; q < nnl; q++)
+                            for (long long kk = bstart[nl[q]]; kk < bstart[nl[q] + 1]; kk++) {
+                                long long j = order[kk];
+                                double dx = x[j] - xt, dy = y[j] - yt;
+                                double r2 = dx * dx + dy * dy;
+                                if (!(r2 > cutoff)) continue;
+                                double w = m[j] / (r2 + eps2);
+                                sx += w * dx;
+                                sy += w * dy;
+                            }
+                        for (long long q = 0; q < nfar; q++) {
+                            long long cell = far[q];
+                            int l = 0;
+                            while (l + 1 < L && lvoff[l + 1] <= cell) l++;
+                            long long ci_ = cell - lvoff[l];
+                            int ci = (int)(ci_ / lvg[l]), cj = (int)(ci_ % lvg[l]);
+                            const double *qm = mom + 6 * cell;
+                            double cx = (bb[0] + (double)(ci << l) * bb[4]) + qm[1] / qm[0];
+                            double cy = (bb[1] + (double)(cj << l) * bb[4]) + qm[2] / qm[0];
+                            double dx = cx - xt, dy = cy - yt;
+                            double r2 = dx * dx + dy * dy;
+                            if (!(r2 > cutoff)) continue;
+                            double w = qm[0] / (r2 + eps2);
+                            sx += w * dx;
+                            sy += w * dy;
+                        }
+                        ax[t] = gconst * sx;
+                        ay[t] = gconst * sy;
                     }
-                for (long long q = 0; q < nfar; q++) {
-                    long long cell = far[q];
-                    int l = 0;
-                    while (l + 1 < L && lvoff[l + 1] <= cell) l++;
-                    long long ci_ = cell - lvoff[l];
-                    int ci = (int)(ci_ / lvg[l]), cj = (int)(ci_ % lvg[l]);
-                    const double *qm = mom + 6 * cell;
-                    double cx = (bb[0] + (double)(ci << l) * bb[4]) + qm[1] / qm[0];
-                    double cy = (bb[1] + (double)(cj << l) * bb[4]) + qm[2] / qm[0];
-                    double dx = cx - xt, dy = cy - yt;
-                    double r2 = dx * dx + dy * dy;
-                    if (!(r2 > cutoff)) continue;
-                    double w = qm[0] / (r2 + eps2);
-                    sx += w * dx;
-                    sy += w * dy;
                 }
-                ax[t] = gconst * sx;
-                ay[t] = gconst * sy;
-            }
             }
         }
         free(bnear);
@@ -849,6 +888,7 @@ int oref_theta_evaluate(long long n, const double *x, const double *y, const dou
         counts[1] = cnt_far;
     }
     free(kx);
+    free(quad);
     free(ky);
     free(mom);
     free(rec);

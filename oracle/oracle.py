@@ -66,7 +66,7 @@ def lib():
         L.oref_pyramid_cells.argtypes = [i]
         L.oref_pyramid_cells.restype = ll
         L.oref_moments.argtypes = [ll, pd, pd, pd, i, pd, pi, pi, pd, pf]
-        L.oref_theta_evaluate.argtypes = [ll, pd, pd, pd, i, i, d, d, d, d, pd, pd, pll, i, i]
+        L.oref_theta_evaluate.argtypes = [ll, pd, pd, pd, i, i, d, d, d, d, pd, pd, pll, i, i, i]
         L.oref_theta_evaluate.restype = i
         L.oref_reference_sample_time.argtypes = [ll, pd, pd, pd, i, ll, i, pd]
         _lib = L
@@ -177,9 +177,10 @@ def moments(x, y, m, G):
 
 
 def theta_evaluate(x, y, m, G, TG=1, theta=0.5, eps2=0.0, cutoff=0.0, gconst=1.0, nthreads=0,
-                   dense_min=0):
+                   dense_min=0, quad_min=0):
     """FP64 opening-angle evaluation (theta <= 0: the reference's flat mode).  dense_min > 0:
-    boxes with at least dense_min particles use per-box refined lists (see bh_oracle.c).
+    boxes with at least dense_min particles use per-box refined lists; quad_min > 0: boxes with
+    at least quad_min particles use per-quadrant refined lists (see bh_oracle.c).
     Returns (ax, ay, n_near_pairs, n_far_pairs)."""
     x, y, m = _d(x), _d(y), _d(m)
     n = len(x)
@@ -187,7 +188,7 @@ def theta_evaluate(x, y, m, G, TG=1, theta=0.5, eps2=0.0, cutoff=0.0, gconst=1.0
     cnt = np.zeros(2, np.int64)
     lib().oref_theta_evaluate(n, _p(x), _p(y), _p(m), int(G), int(TG), float(theta),
                               float(eps2), float(cutoff), float(gconst), _p(ax), _p(ay),
-                              _p(cnt, ctypes.c_longlong), int(nthreads), int(dense_min))
+                              _p(cnt, ctypes.c_longlong), int(nthreads), int(dense_min), int(quad_min))
     return ax, ay, int(cnt[0]), int(cnt[1])
 
 

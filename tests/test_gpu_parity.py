@@ -185,12 +185,39 @@ def test_theta_vs_fp64_oracle(theta, TG, G, prec, walk):
     out = plan.store()
     nn, nf = plan.pair_counts()
     # list streaming refines the near lists of dense boxes; the walk keeps the group lists
-    dense = 0 if (walk or prec == 2) else native().BH_STREAM_DENSE_MIN
+    walking = walk or prec == 2
+    dense = 0 if walking else native().BH_STREAM_DENSE_MIN
+    quad = 0 if walking else native().BH_STREAM_QUAD_MIN
     ax, ay, on, of = oracle.theta_evaluate(x, y, m, G, TG=TG, theta=theta, eps2=eps * eps, cutoff=0.0,
-                                           dense_min=dense)
+                                           dense_min=dense, quad_min=quad)
     assert (nn, nf) == (on, of), "interaction lists differ from the oracle's"
     err = oracle.rel_rms(out["ax"].cpu().numpy(), out["ay"].cpu().numpy(), ax, ay)
     assert err <= (1e-8 if prec == 2 else 1e-5), err
+    assert plan.error_flags() == 0
+
+
+@pytest.mark.parametrize("TG,dense_min,quad_min", [(2, 16, 32), (4, 8, 24), (4, 16, -1)])
+def test_refined_lists_vs_fp64_oracle(TG, dense_min, quad_min):
+    """List streaming with per-box and per-quadrant refinement thresholds low enough that many
+    boxes of a 16 x 16 grid take each path: pair counts exact, forces within 1e-5 of the oracle
+    applying the same rule (quad_min < 0: no quadrant refinement)."""
+    from barneshut.gb300 import workloads
+    from oracle import oracle
+
+    x, y, m, vx, vy = workloads.cluster_mixture(20000, seed=33)
+    eps = 1e-3
+    plan = make_plan(20000, 16, grav_constant=1.0, tick_seconds=1e-5, softening=eps, cutoff_r2=0.0,
+                     theta=0.5, group_dim=TG, precision=1, dense_min=dense_min, quad_min=quad_min)
+    plan.load(x, y, m, vx, vy)
+    plan.create_tree()
+    plan.summarize()
+    plan.evaluate()
+    out = plan.store()
+    nn, nf = plan.pair_counts()
+    ax, ay, on, of = oracle.theta_evaluate(x, y, m, 16, TG=TG, theta=0.5, eps2=eps * eps, cutoff=0.0,
+                                           dense_min=dense_min, quad_min=max(quad_min, 0))
+    assert (nn, nf) == (on, of)
+    assert oracle.rel_rms(out["ax"].cpu().numpy(), out["ay"].cpu().numpy(), ax, ay) <= 1e-5
     assert plan.error_flags() == 0
 
 

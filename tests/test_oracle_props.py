@@ -25,16 +25,20 @@ def test_theta_error_shrinks_with_theta(oracle_mod, theta, TG):
 
 @pytest.mark.parametrize("TG", [2, 4])
 def test_dense_box_refinement(oracle_mod, TG):
-    """Per-box refinement of dense boxes' near lists moves near pairs to far entries, keeps the
-    error within the opening-angle bound, and is the identity when no box is dense."""
+    """Per-box (and per-quadrant) refinement of dense boxes' near lists moves near pairs to far
+    entries, keeps the error within the opening-angle bound, and is the identity when no box is
+    dense."""
     x, y, m, _, _ = workloads.cluster_mixture(20000, seed=7)
     dax, day = oracle_mod.direct(x, y, m, eps2=1e-6, cutoff=0.0)
     a0 = oracle_mod.theta_evaluate(x, y, m, 16, TG=TG, theta=0.5, eps2=1e-6)
     a1 = oracle_mod.theta_evaluate(x, y, m, 16, TG=TG, theta=0.5, eps2=1e-6, dense_min=64)
     a2 = oracle_mod.theta_evaluate(x, y, m, 16, TG=TG, theta=0.5, eps2=1e-6, dense_min=10 ** 9)
+    a3 = oracle_mod.theta_evaluate(x, y, m, 16, TG=TG, theta=0.5, eps2=1e-6, dense_min=64, quad_min=64)
     assert a1[2] < a0[2] and a1[3] > a0[3]
+    assert a3[2] < a1[2] and a3[3] > a1[3]  # quadrants refine further
     assert a2[2:] == a0[2:] and np.array_equal(a2[0], a0[0])
     assert oracle_mod.rel_rms(a1[0], a1[1], dax, day) < 1e-3
+    assert oracle_mod.rel_rms(a3[0], a3[1], dax, day) < 1e-3
 
 
 def test_theta_tiny_is_direct(oracle_mod):
