@@ -3,7 +3,8 @@
 Tunables (per plan): group_dim -- target group edge in leaf boxes (1, 2, 4 or 8;
 TG^2 boxes share one interaction list) --, dense_min -- boxes holding at least
 this many particles get their own work items and per-box refined near lists
-(list-streaming path) -- and tune -- the force-kernel variant (0: 8 CTAs per SM
+(list-streaming path) --, quad_min -- boxes holding at least this many particles
+are refined quadrant by quadrant (-1: never) -- and tune -- the force-kernel variant (0: 8 CTAs per SM
 with 64 registers per thread, 1: 6 CTAs per SM with 80).  Every candidate keeps
 the opening-angle rule for every target (a cell accepted for a group rectangle
 passes the test for each of its boxes); they differ in how far the lists are
@@ -36,8 +37,9 @@ def candidates(theta):
     out = []
     for tg in (1, 2, 4, 8):
         for dm in ((0,) if tg == 1 else (16, 32, 64)):
-            for tune in (0, 1):
-                out.append({"group_dim": tg, "dense_min": dm, "tune": tune})
+            for qm in (-1, 128):
+                for tune in (0, 1):
+                    out.append({"group_dim": tg, "dense_min": dm, "quad_min": qm, "tune": tune})
     return out
 
 
@@ -62,7 +64,8 @@ def tune(systems, grids, grav_constant=1.0, dt=1e-5, softening=1e-4, theta=0.5,
     stream = torch.cuda.current_stream(device)
     for c in candidates(theta):
         prm = native.make_params(grav_constant, dt, softening, 0.0, theta, c["group_dim"],
-                                 precision, 0, c["tune"], dense_min=c["dense_min"])
+                                 precision, 0, c["tune"], dense_min=c["dense_min"],
+                                 quad_min=c["quad_min"])
         try:
             plan = native.Plan(n, grids, prm, device=device)
         except native.BHError:

@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--quick", action="store_true",
                     help="skip the autotuner and the batched / learned side measurements")
     ap.add_argument("--tile", default=None,
-                    help="group_dim,dense_min,tune: use this tile instead of the autotuner's")
+                    help="group_dim,dense_min,tune[,quad_min]: use this tile instead of the autotuner's")
     return ap.parse_args()
 
 
@@ -196,7 +196,8 @@ def batched_benchmark(torch, dev, nsys=512, steps=50, warmup=3):
     n = [len(s[0]) for s in systems]
     tile, _ = autotune.tune(systems, grids, 1.0, 1e-6, 1e-4, 0.5, device=dev)
     prm = native.make_params(1.0, 1e-6, 1e-4, 0.0, 0.5, tile["group_dim"],
-                             native.BH_PREC_FP32_KAHAN, 0, tile["tune"], dense_min=tile.get("dense_min", 0))
+                             native.BH_PREC_FP32_KAHAN, 0, tile["tune"], dense_min=tile.get("dense_min", 0),
+                             quad_min=tile.get("quad_min", 0))
     plan = native.Plan(n, grids, prm, device=dev)
     plan.load(*[np.concatenate([s[k] for s in systems]) for k in range(5)])
     for _ in range(warmup):
@@ -419,8 +420,8 @@ def main():
     tile = {"group_dim": 0, "tune": 0, "dense_min": 0}
     tune_ms = None
     if args.tile:
-        tg, dm, tu = (int(v) for v in args.tile.split(","))
-        tile = {"group_dim": tg, "dense_min": dm, "tune": tu}
+        v = [int(t) for t in args.tile.split(",")]
+        tile = {"group_dim": v[0], "dense_min": v[1], "tune": v[2], "quad_min": v[3] if len(v) > 3 else 0}
     elif not args.quick:
         from barneshut.gb300 import autotune
 
@@ -428,7 +429,8 @@ def main():
                                  device=dev)
         tune_ms = {k: round(1e3 * v, 3) for k, v in tt.items()}
     prm = native.make_params(1.0, DT, SOFTENING, 0.0, THETA, tile["group_dim"],
-                             native.BH_PREC_FP32_KAHAN, 0, tile["tune"], dense_min=tile.get("dense_min", 0))
+                             native.BH_PREC_FP32_KAHAN, 0, tile["tune"], dense_min=tile.get("dense_min", 0),
+                             quad_min=tile.get("quad_min", 0))
     plan = native.Plan([args.n], [args.grid], prm, device=dev)
     stream = torch.cuda.current_stream(dev)
     batch = [torch.from_numpy(a).to(dev) for a in (x, y, m, vx, vy)]
