@@ -21,9 +21,9 @@ def declared_symbols():
 
 @pytest.fixture(scope="module")
 def lib():
-    from barneshut.gb300 import native
+    from conftest import ensure_library
 
-    return native.load_library()
+    return ensure_library().load_library()
 
 
 def test_every_declared_symbol_exported(lib):
