@@ -369,6 +369,90 @@ def free_run(torch, dev, steps=100):
     return res
 
 
+def e2e_serial_ms(torch, plan, host_in, dev, stream, steps):
+    """ms per step of H2D inputs -> bh_load -> bh_step_graph(1) -> bh_store -> D2H results, one
+    stream, nothing overlapped."""
+    n = host_in[0].numel()
+    dev_in = [torch.empty_like(h, device=dev) for h in host_in]
+    host_out = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(6)]
+
+    def one():
+        for h, d in zip(host_in, dev_in):
+            d.copy_(h, non_blocking=True)
+        plan.load(*dev_in)
+        plan.step_graph(1)
+        outs = plan.store()
+        for h, k in zip(host_out, ("x", "y", "vx", "vy", "ax", "ay")):
+            h.copy_(outs[k], non_blocking=True)
+
+    for _ in range(2):
+        one()
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(steps):
+        one()
+    g1.record(stream)
+    torch.cuda.synchronize()
+    return g0.elapsed_time(g1) / steps
+
+
+def e2e_pipelined_ms(torch, plan, host_in, dev, steps):
+    """ms per step of the same sequence with three streams: H2D of step k's inputs into device
+    buffer k % 2 (after step k - 2's bh_load has read it), the step on the compute stream
+    (bh_load, bh_step_graph(1), bh_store into device buffer k % 2 once step k - 2's results have
+    left it), and D2H of step k's results into pinned host buffer k % 2.  Every step's inputs
+    and results cross the host link inside the timed region."""
+    import ctypes
+
+    from barneshut.gb300 import native
+
+    n = host_in[0].numel()
+    s_h2d, s_cmp, s_d2h = (torch.cuda.Stream(dev) for _ in range(3))
+    dev_in = [[torch.empty_like(h, device=dev) for h in host_in] for _ in range(2)]
+    dev_out = [[torch.empty(n, dtype=torch.float64, device=dev) for _ in range(6)] for _ in range(2)]
+    host_out = [[torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(6)] for _ in range(2)]
+    ev = {k: [torch.cuda.Event() for _ in range(2)] for k in ("h2d", "loaded", "stored", "d2h")}
+    L = native.load_library()
+
+    def issue(k):
+        b = k % 2
+        with torch.cuda.stream(s_h2d):
+            if k >= 2:
+                s_h2d.wait_event(ev["loaded"][b])
+            for h, d in zip(host_in, dev_in[b]):
+                d.copy_(h, non_blocking=True)
+            ev["h2d"][b].record(s_h2d)
+        with torch.cuda.stream(s_cmp):
+            s_cmp.wait_event(ev["h2d"][b])
+            st = ctypes.c_void_p(s_cmp.cuda_stream)
+            plan._check(L.bh_load(plan.h, *[native._ptr(t) for t in dev_in[b]], st))
+            ev["loaded"][b].record(s_cmp)
+            plan._check(L.bh_step_graph(plan.h, 1, st))
+            if k >= 2:
+                s_cmp.wait_event(ev["d2h"][b])
+            plan._check(L.bh_store(plan.h, *[native._ptr(t) for t in dev_out[b]], st))
+            ev["stored"][b].record(s_cmp)
+        with torch.cuda.stream(s_d2h):
+            s_d2h.wait_event(ev["stored"][b])
+            for h, d in zip(host_out[b], dev_out[b]):
+                h.copy_(d, non_blocking=True)
+            ev["d2h"][b].record(s_d2h)
+
+    for k in range(3):  # warm-up (graph already captured on the plan)
+        issue(k)
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(s_h2d)
+    s_cmp.wait_event(g0)
+    s_d2h.wait_event(g0)
+    for k in range(steps):
+        issue(k)
+    g1.record(s_d2h)  # after the last D2H, which follows every step's work
+    torch.cuda.synchronize()
+    return g0.elapsed_time(g1) / steps
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -490,39 +574,24 @@ def main():
     flops_force = 12.0 * near2 + 20.0 * far2
     peak = fp32_peak_tflops(torch, dev)
 
-    # ---- e2e through the C ABI with host buffers: H2D state, step, D2H state
+    # ---- e2e through the C ABI with host buffers: every step copies its inputs from pinned host
+    # memory, steps, and copies its results back.  Measured twice: serially on one stream, and
+    # pipelined (the copy of step k + 1's inputs and of step k - 1's results overlap step k).
     host_in = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (x, y, m, vx, vy)]
-    dev_in = [torch.empty_like(h, device=dev) for h in host_in]
-    host_out = [torch.empty(args.n, dtype=torch.float64).pin_memory() for _ in range(6)]
-    e2e_steps = max(3, min(K, 10))
-    for _ in range(2):
-        for h, d in zip(host_in, dev_in):
-            d.copy_(h, non_blocking=True)
-        plan.load(*dev_in)
-        plan.step_graph(1)
-        outs = plan.store()
-        for h, k in zip(host_out, ("x", "y", "vx", "vy", "ax", "ay")):
-            h.copy_(outs[k], non_blocking=True)
-    torch.cuda.synchronize()
-    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    g0.record(stream)
-    for _ in range(e2e_steps):
-        for h, d in zip(host_in, dev_in):
-            d.copy_(h, non_blocking=True)
-        plan.load(*dev_in)
-        plan.step_graph(1)
-        outs = plan.store()
-        for h, k in zip(host_out, ("x", "y", "vx", "vy", "ax", "ay")):
-            h.copy_(outs[k], non_blocking=True)
-    g1.record(stream)
-    torch.cuda.synchronize()
+    e2e_serial = e2e_serial_ms(torch, plan, host_in, dev, stream, max(3, min(K, 10)))
+    e2e_steps = max(6, min(K, 20))
+    t_e2e = e2e_pipelined_ms(torch, plan, host_in, dev, e2e_steps) / 1e3
     if ws > 1:
         torch.distributed.barrier()
-    t_e2e = max_over_ranks(g0.elapsed_time(g1) / 1e3 / e2e_steps, ws, dev)
+    t_e2e = max_over_ranks(t_e2e, ws, dev)
     e2e = {"value": ws * args.n / t_e2e, "unit": "particle-steps/s",
            "h2d_bytes_per_step": ws * 5 * 8 * args.n, "d2h_bytes_per_step": ws * 6 * 8 * args.n,
-           "ms_per_step": 1e3 * t_e2e,
-           "path": "pinned host arrays -> bh_load -> bh_step_graph(1) -> bh_store -> pinned host"}
+           "ms_per_step": 1e3 * t_e2e, "steps": e2e_steps,
+           "path": ("pinned host arrays -> bh_load -> bh_step_graph(1) -> bh_store -> pinned host, "
+                    "every step; three streams and double-buffered device arrays let the copies of "
+                    "step k + 1's inputs and step k - 1's results overlap step k (the first copy in "
+                    "and the last copy out are not overlapped)"),
+           "serial_ms_per_step": e2e_serial}
 
     # ---- accuracy of the measured step vs FP64 direct sum (on the device)
     acc = None
