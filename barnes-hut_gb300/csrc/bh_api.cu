@@ -550,11 +550,17 @@ extern "C" int bh_step_graph(bh_plan *p, int nsteps, void *stream) {
 extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     if (!p || !count) return BH_ERR_INVALID;
     // prologue, 3 box-scan phases, work items (count, 3 scan phases, fill),
-    // pyramid levels 1..Lmax-1, records; with particles also bbox, bbox
+    // pyramid levels, records; with particles also bbox, bbox
     // finalize, place, scatter, leaf moments, force (and before it the list build and the
     // two kernels of the heaviest-first item order); list streaming also builds its own work
     // items (count, 3 scan phases, fill)
-    *count = 1 + 3 + 5 + (p->Lmax - 1) + 1 + (p->n_total > 0 ? 6 : 0) + (p->stream ? 5 : 0) + (p->stream && p->n_total > 0 ? 3 : 0);
+    // pyramid: one launch per level while its cells exceed 256, then one for the remaining levels
+    int pyr = 0;
+    for (int l = 1; l < p->Lmax; l++) {
+        pyr++;
+        if (p->lvl[(size_t)l * (p->nsys + 1) + p->nsys] <= 256) break;
+    }
+    *count = 1 + 3 + 5 + pyr + 1 + (p->n_total > 0 ? 6 : 0) + (p->stream ? 5 : 0) + (p->stream && p->n_total > 0 ? 3 : 0);
     return BH_OK;
 }
 

@@ -467,35 +467,49 @@ __global__ void __launch_bounds__(TPB) k_leaf_moments(DevPlan d) {
 // ------------------------------------------------------------------ pyramid
 // Level-l cell = sum of its (up to) four level-(l-1) children, moments shifted
 // from the child origin to the parent origin (FP64).
-__global__ void __launch_bounds__(TPB) k_pyramid_level(DevPlan d, int l) {
+__device__ __forceinline__ void pyramid_cell(const DevPlan &d, int l, long long t) {
     const long long *tab = d.lvl_tab + (long long)l * (d.nsys + 1);
-    long long total = tab[d.nsys];
-    long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        int s = find_seg(tab, d.nsys, t);
-        const SysDesc &sd = d.sys[s];
-        double step = d.dyn[s].step;
-        long long loc = t - tab[s];
-        int gl = sd.lvg[l], gc = sd.lvg[l - 1];
-        int i = (int)(loc / gl), j = (int)(loc - (long long)i * gl);
-        double p[6] = {0, 0, 0, 0, 0, 0};
-        for (int a = 0; a < 2; a++)
-            for (int b = 0; b < 2; b++) {
-                int ci = 2 * i + a, cj = 2 * j + b;
-                if (ci >= gc || cj >= gc) continue;
-                const double *c = d.mom + 6 * (sd.coff + sd.lvoff[l - 1] + (long long)ci * gc + cj);
-                double dx = (double)(a << (l - 1)) * step, dy = (double)(b << (l - 1)) * step;
-                double M = c[0], Sx = c[1], Sy = c[2];
-                p[0] += M;
-                p[1] += Sx + M * dx;
-                p[2] += Sy + M * dy;
-                p[3] += c[3] + 2.0 * dx * Sx + M * dx * dx;
-                p[4] += c[4] + dx * Sy + dy * Sx + M * dx * dy;
-                p[5] += c[5] + 2.0 * dy * Sy + M * dy * dy;
-            }
-        double *q = d.mom + 6 * (sd.coff + sd.lvoff[l] + loc);
+    int s = find_seg(tab, d.nsys, t);
+    const SysDesc &sd = d.sys[s];
+    double step = d.dyn[s].step;
+    long long loc = t - tab[s];
+    int gl = sd.lvg[l], gc = sd.lvg[l - 1];
+    int i = (int)(loc / gl), j = (int)(loc - (long long)i * gl);
+    double p[6] = {0, 0, 0, 0, 0, 0};
+    for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++) {
+            int ci = 2 * i + a, cj = 2 * j + b;
+            if (ci >= gc || cj >= gc) continue;
+            const double *c = d.mom + 6 * (sd.coff + sd.lvoff[l - 1] + (long long)ci * gc + cj);
+            double dx = (double)(a << (l - 1)) * step, dy = (double)(b << (l - 1)) * step;
+            double M = c[0], Sx = c[1], Sy = c[2];
+            p[0] += M;
+            p[1] += Sx + M * dx;
+            p[2] += Sy + M * dy;
+            p[3] += c[3] + 2.0 * dx * Sx + M * dx * dx;
+            p[4] += c[4] + dx * Sy + dy * Sx + M * dx * dy;
+            p[5] += c[5] + 2.0 * dy * Sy + M * dy * dy;
+        }
+    double *q = d.mom + 6 * (sd.coff + sd.lvoff[l] + loc);
 #pragma unroll
-        for (int k = 0; k < 6; k++) q[k] = p[k];
+    for (int k = 0; k < 6; k++) q[k] = p[k];
+}
+
+__global__ void __launch_bounds__(TPB) k_pyramid_level(DevPlan d, int l) {
+    const long long total = d.lvl_tab[(long long)l * (d.nsys + 1) + d.nsys];
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride)
+        pyramid_cell(d, l, t);
+}
+
+// Levels l0 .. Lmax - 1 in one CTA (their cells are few): level by level, a barrier between.
+constexpr int TAIL_THREADS = 1024;
+constexpr long long TAIL_MAX_CELLS = 256;  // the first level given to the single CTA (FP64 work on one SM)
+__global__ void __launch_bounds__(TAIL_THREADS) k_pyramid_tail(DevPlan d, int l0) {
+    for (int l = l0; l < d.Lmax; l++) {
+        const long long total = d.lvl_tab[(long long)l * (d.nsys + 1) + d.nsys];
+        for (long long t = threadIdx.x; t < total; t += blockDim.x) pyramid_cell(d, l, t);
+        __syncthreads();  // level l is complete before level l + 1 reads it
     }
 }
 
@@ -569,6 +583,11 @@ cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st) {
     if (d.n_total > 0) k_leaf_moments<<<grid_for(d.n_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
     for (int l = 1; l < d.Lmax; l++) {
         // the level's cell count over all systems is known on the host: one thread per cell
+        // while the level is large, then one CTA for all the remaining (small) levels
+        if (d.lvl_cells[l] <= TAIL_MAX_CELLS) {
+            k_pyramid_tail<<<1, TAIL_THREADS, 0, st>>>(d, l);
+            break;
+        }
         k_pyramid_level<<<grid_for(d.lvl_cells[l], TPB, 152LL * 4), TPB, 0, st>>>(d, l);
     }
     k_records<<<grid_for(d.C_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
