@@ -2,7 +2,8 @@
 // layer of libbh_gb300.
 //
 // Data layout in HBM (one workspace, carved by bh_api.cu):
-//   * particle state, double-buffered, box-sorted between steps, SoA FP64:
+//   * particle state, double-buffered, box-sorted between steps (within a box,
+//     quadrant by quadrant), SoA FP64:
 //       X[2], Y[2], VX[2], VY[2], M[2] (n_total doubles each), PID[2] (int32)
 //     The up-to-date state is buffer (epoch + 1) & 1; the step prologue
 //     increments epoch, placement reads buffer epoch & 1 and scatters into
@@ -10,13 +11,18 @@
 //     buffer choice is read on the device, so a captured CUDA graph of one
 //     step replays correctly any number of times.
 //   * P: packed float4 per box-sorted particle (x - box origin, y - box origin,
-//     mass, sorted index as int bits) -- the only array the force kernel
-//     streams for near-field sources.
+//     mass, sorted index as int bits) -- targets and the walking kernel's near
+//     sources; PD: the same offsets duplicated for packed f32x2 arithmetic,
+//     32 bytes per particle -- the list-streaming kernel's near sources, copied
+//     into shared memory by bulk asynchronous copies.
 //   * AX, AY: FP64 accelerations, box-sorted order (aligned with the state).
-//   * key / slot: box key and rank-in-box per particle (placement output);
-//     skey: box key per box-sorted particle.
+//   * key / slot: 4 * box key + quadrant, and rank in the quadrant, per particle
+//     (placement output); skey: box key per box-sorted particle.
 //   * counts, box_start: per-box histogram and exclusive prefix (int32),
-//     concatenated over systems; box_start[b] is a global particle index.
+//     concatenated over systems; box_start[b] is a global particle index;
+//     qcounts: the four quadrant counts of every box.
+//   * interaction lists, streaming work items and their order (list streaming):
+//     see DevPlan.
 //   * mom: FP64 moments (M, Sx, Sy, Sxx, Sxy, Syy about the cell origin) for
 //     every pyramid cell; rec / rec2: float records the force kernel reads
 //     (centre of mass relative to the cell origin, mass; normalised second
