@@ -109,8 +109,9 @@ struct DevPlan {
     int *lfar;
     int4 *lnear;
     int2 *lcnt;
-    // list-streaming work items (per group: its sparse boxes together, then every dense box):
-    // group, box within the group (cx * TG + cy, or -1 for the sparse boxes), (chunk, chunks)
+    // list-streaming work items (per group: its sparse boxes together, then every dense box or
+    // its quadrants): group, sub (-1: the sparse boxes; b = cx * TG + cy: box b; TG^2 + 4 b + q:
+    // quadrant q of box b), (chunk, chunks)
     int *sitem_cnt, *sitem_off, *sitem_group, *sitem_sub;
     int2 *sitem_chunk;
     int dense_min;
