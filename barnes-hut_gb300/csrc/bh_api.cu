@@ -255,9 +255,10 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_lfar = take(4 * (size_t)lf_total);
     p->o_lnear = take(16 * (size_t)ln_total);
     p->o_lcnt = take(p->stream ? 8 * (size_t)p->NG_total : 0);
-    // at most one partial chunk per sparse set, dense box and quadrant of a quadrant box
+    // target sets: a sparse set per group, each dense box, each quadrant of a quadrant box; a
+    // set of nt targets has at most 1 + nt / 40 items (sitem_count)
     const size_t sitems = p->stream ? (size_t)p->NG_total + N / p->dense_min +
-                                          (p->quad_min > 0 ? 4 * (N / p->quad_min) : 0) + N / p->chunk + 1
+                                          (p->quad_min > 0 ? 4 * (N / p->quad_min) : 0) + N / STREAM_ITEM_DIV + 1
                                     : 0;
     p->o_iord = take(4 * sitems);
     p->o_sicnt = take(p->stream ? 4 * (size_t)p->NG_total : 0);

@@ -6,10 +6,10 @@
 // The interaction lists come from k_lists (one pyramid walk per target group); this kernel only
 // streams them.
 //
-// One warp owns one work item at a time (a group's targets split into near-equal chunks of at
-// most STREAM_CHUNK, pulled from a device queue); the warps of a CTA share nothing but the CTA's
-// shared memory carve-up, so there is no CTA-wide barrier and a warp waiting on memory leaves
-// the SM to the other warps.  Per item:
+// One warp owns one work item at a time (a full chunk of STREAM_CHUNK targets of a target set or
+// a piece of its remainder, sitem_range; pulled from a device queue); the warps of a CTA share
+// nothing but the CTA's shared memory carve-up, so there is no CTA-wide barrier and a warp
+// waiting on memory leaves the SM to the other warps.  Per item:
 //   * far field: the group's far codes are decoded (level, cell -> record; centre of mass shifted
 //     into the group frame) into the warp's staging as packed (x, x, y, y) + (M, M) entries,
 //     WFAR at a time, and swept; each pass's plain FP32 sum enters the running total through a
@@ -465,7 +465,8 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
 
 template <bool KAHAN, int MINB>
 static cudaError_t launch_fstream_t(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
-    long long items_max = d.NG_total + d.n_total / d.chunk + 1;
+    long long items_max = d.NG_total + d.n_total / d.dense_min +
+                          (d.quad_min > 0 ? 4 * (d.n_total / d.quad_min) : 0) + d.n_total / STREAM_ITEM_DIV + 1;
     long long grid = 152LL * MINB;
     if (grid * FW > items_max) grid = (items_max + FW - 1) / FW;
     if (grid < 1) grid = 1;

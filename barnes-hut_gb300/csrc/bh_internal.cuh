@@ -240,11 +240,38 @@ __device__ __forceinline__ void item_range(int nt, int nch, int k, int *c0, int 
     *T = b - a;
 }
 
-// Targets [c0, c0 + T) of list-streaming work item k of a target set of nt particles: full
-// chunks of STREAM_CHUNK (one warp, FORCE_R targets per lane) and one remainder.
+// List-streaming work items of a target set of nt particles: full chunks of STREAM_CHUNK, then
+// the remainder r = nt mod STREAM_CHUNK cut into pieces that keep a warp's lanes busy.  A piece of
+// T targets occupies ceil(T / FORCE_R) lanes per slice and 32 / ceil(T / FORCE_R) slices (each
+// slice sweeps its share of the sources), so its sweep takes sources / slices lane-passes for
+// T x sources pairs: 128, 64 and 32 targets use every lane, while 65..127 targets run a single
+// slice on 17..32 lanes.  The remainder therefore yields a piece of 64 first when r > 64, then a
+// piece of 32 when 41..48 targets are left (two slices of 11..12 lanes become four of 8 plus a
+// small piece), then the rest.  An extra piece needs at least 41 targets, so a set of nt targets
+// has at most 1 + nt / 40 items.
+constexpr int STREAM_ITEM_DIV = 32;  // items <= sets + n / STREAM_ITEM_DIV
+
+__host__ __device__ __forceinline__ int sitem_count(int nt) {
+    int r = nt % STREAM_CHUNK, n = nt / STREAM_CHUNK;
+    if (r > 64) { n++; r -= 64; }
+    if (r > 40 && r <= 48) { n++; r -= 32; }
+    return n + (r > 0 ? 1 : 0);
+}
+
+// Targets [c0, c0 + T) of item k of a target set of nt particles (k < sitem_count(nt)).
 __device__ __forceinline__ void sitem_range(int nt, int k, int *c0, int *T) {
-    *c0 = k * STREAM_CHUNK;
-    *T = min(STREAM_CHUNK, nt - *c0);
+    const int full = nt / STREAM_CHUNK;
+    int c = k < full ? k * STREAM_CHUNK : full * STREAM_CHUNK, r = nt - c, j = k - full;
+    if (j >= 0 && r > 64) {
+        if (j == 0) r = 64;
+        else { c += 64; r -= 64; j--; }
+    }
+    if (j >= 0 && r > 40 && r <= 48) {
+        if (j == 0) r = 32;
+        else { c += 32; r -= 32; }
+    }
+    *c0 = c;
+    *T = min(STREAM_CHUNK, r);
 }
 
 __device__ __forceinline__ void raise_err(Globals *g, unsigned f) {

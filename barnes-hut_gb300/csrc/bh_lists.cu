@@ -176,9 +176,9 @@ __global__ void __launch_bounds__(LW * 32) k_lists(DevPlan d) {
 // ---------------------------------------------------------------- heaviest-first item order
 // A warp of the force kernel owns one work item, so an item's duration grows with its pair count
 // and the launch ends with its slowest warp.  Items are therefore handed out heaviest first:
-// bucket b holds the items whose estimated cost T x (near sources + 2 x far cells) lies in
-// [2^b, 2^(b+1)); buckets are laid out from the top down.  Order inside a bucket follows atomic
-// arrival, which changes only which warp evaluates an item, not its result.
+// bucket b holds the items whose estimated cost (STREAM_CHUNK / slices) x (near sources + 2 x far
+// cells) lies in [2^b, 2^(b+1)); buckets are laid out from the top down.  Order inside a bucket
+// follows atomic arrival, which changes only which warp evaluates an item, not its result.
 __device__ __forceinline__ int item_cost_bucket(const DevPlan &d, long long item) {
     const long long g = d.sitem_group[item];
     const int sub = d.sitem_sub[item];
@@ -206,7 +206,10 @@ __device__ __forceinline__ int item_cost_bucket(const DevPlan &d, long long item
         }
     int c0, T;
     sitem_range(nt, ck.x, &c0, &T);
-    const unsigned long long cost = (unsigned long long)T * (unsigned long long)(near_total + 2 * cnt.x) + 1ull;
+    // a sweep of T targets runs 32 / ceil(T / FORCE_R) slices; cost in full-warp target units
+    const int nslice = 32 / max(1, (T + FORCE_R - 1) / FORCE_R);
+    const unsigned long long cost =
+        (unsigned long long)(STREAM_CHUNK / nslice) * (unsigned long long)(near_total + 2 * cnt.x) + 1ull;
     const int b = 63 - __clzll((long long)cost);
     return min(b, ITEM_BUCKETS - 1);
 }
@@ -264,7 +267,7 @@ cudaError_t launch_lists(const DevPlan &d, cudaStream_t st) {
     e = cudaMemsetAsync(d.item_bucket, 0, sizeof(int) * 2 * ITEM_BUCKETS, st);
     if (e != cudaSuccess) return e;
     long long items_max = d.NG_total + d.n_total / d.dense_min +
-                          (d.quad_min > 0 ? 4 * (d.n_total / d.quad_min) : 0) + d.n_total / d.chunk + 1;  // >= items
+                          (d.quad_min > 0 ? 4 * (d.n_total / d.quad_min) : 0) + d.n_total / STREAM_ITEM_DIV + 1;  // >= items
     long long ig = (items_max + 255) / 256;
     if (ig > 152LL * 8) ig = 152LL * 8;
     k_item_hist<<<(unsigned)ig, 256, 0, st>>>(d);

@@ -303,8 +303,8 @@ __global__ void __launch_bounds__(TPB) k_fill_items(DevPlan d) {
 // ceil(n_sparse / chunk) items (sub = -1); every denser box gets ceil(n_box / chunk) items of its
 // own (sub = cx * TG + cy), which use per-box refined near lists, and a box holding at least
 // quad_min particles gets items per quadrant instead (sub = TG^2 + 4 (cx * TG + cy) + quadrant),
-// which use per-quadrant refined near lists.  Chunks split their targets into full chunks of
-// STREAM_CHUNK and a remainder (sitem_range).
+// which use per-quadrant refined near lists.  A set of nt targets splits into sitem_count(nt)
+// items: full chunks of STREAM_CHUNK and the remainder's pieces (sitem_range).
 __global__ void __launch_bounds__(TPB) k_sitem_count(DevPlan d) {
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < d.NG_total; g += stride) {
@@ -321,14 +321,14 @@ __global__ void __launch_bounds__(TPB) k_sitem_count(DevPlan d) {
                 const int nb = d.box_start[b + 1] - d.box_start[b];
                 const int kind = box_item_kind(nb, d.dense_min, d.quad_min);
                 if (kind == 2) {
-                    for (int q = 0; q < 4; q++) cnt += (d.qcounts[4 * b + q] + d.chunk - 1) / d.chunk;
+                    for (int q = 0; q < 4; q++) cnt += sitem_count(d.qcounts[4 * b + q]);
                 } else if (kind == 1) {
-                    cnt += (nb + d.chunk - 1) / d.chunk;
+                    cnt += sitem_count(nb);
                 } else {
                     sparse += nb;
                 }
             }
-        d.sitem_cnt[g] = cnt + (sparse + d.chunk - 1) / d.chunk;
+        d.sitem_cnt[g] = cnt + sitem_count(sparse);
     }
 }
 
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(TPB) k_sitem_fill(DevPlan d) {
                 const int nb = d.box_start[b + 1] - d.box_start[b];
                 if (box_item_kind(nb, d.dense_min, d.quad_min) == 0) sparse += nb;
             }
-        const int ns = (sparse + d.chunk - 1) / d.chunk;
+        const int ns = sitem_count(sparse);
         for (int k = 0; k < ns; k++, o++) {
             d.sitem_group[o] = (int)g;
             d.sitem_sub[o] = -1;
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(TPB) k_sitem_fill(DevPlan d) {
                 const int kind = box_item_kind(nb, d.dense_min, d.quad_min);
                 const int bi = (c - gx0) * sd.TG + (r - gy0);
                 if (kind == 1) {
-                    const int nk = (nb + d.chunk - 1) / d.chunk;
+                    const int nk = sitem_count(nb);
                     for (int k = 0; k < nk; k++, o++) {
                         d.sitem_group[o] = (int)g;
                         d.sitem_sub[o] = bi;
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(TPB) k_sitem_fill(DevPlan d) {
                     }
                 } else if (kind == 2) {
                     for (int q = 0; q < 4; q++) {
-                        const int nk = (d.qcounts[4 * b + q] + d.chunk - 1) / d.chunk;
+                        const int nk = sitem_count(d.qcounts[4 * b + q]);
                         for (int k = 0; k < nk; k++, o++) {
                             d.sitem_group[o] = (int)g;
                             d.sitem_sub[o] = nbox + 4 * bi + q;
