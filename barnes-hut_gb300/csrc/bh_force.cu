@@ -47,7 +47,7 @@ __device__ __forceinline__ void src_get(const Src<double>::T &e, double &x, doub
 template <typename R> __host__ __device__ constexpr int far_bytes() {
     return sizeof(typename Src<R>::T) > 24 ? (int)sizeof(typename Src<R>::T) : 24;
 }
-// bytes per staged near source: the record, or the 32-byte PD record (x, x, y, y), (m, m, i, 0)
+// bytes per staged near source: the record, or the 32-byte PD record (x, x, y, y), (m, m, i, box)
 template <typename R> __host__ __device__ constexpr int src_bytes() {
     return sizeof(typename Src<R>::T) > 32 ? (int)sizeof(typename Src<R>::T) : 32;
 }

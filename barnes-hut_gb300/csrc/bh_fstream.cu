@@ -14,11 +14,12 @@
 //     into the group frame) into the warp's staging as packed (x, x, y, y) + (M, M) entries,
 //     WFAR at a time, and swept; each pass's plain FP32 sum enters the running total through a
 //     Kahan-compensated addition (BH_PREC_FP32_KAHAN) or a plain one (BH_PREC_FP32);
-//   * near field: the near boxes' 32-byte packed records (x, x, y, y), (m, m, index, 0) are copied
-//     box piece by box piece into the warp's staging by bulk asynchronous copies (TMA), WSRC
-//     sources per pass, double-buffered on two mbarriers so the copy of pass p + 1 overlaps the
-//     sweep of pass p; the lanes shift each staged source from its box frame into the group
-//     frame in place before the sweep.
+//   * near field: the near boxes' 32-byte packed records (x, x, y, y), (m, m, index, box) are
+//     copied box piece by box piece into the warp's staging by bulk asynchronous copies (TMA),
+//     WSRC sources per pass, double-buffered on two mbarriers so the copy of pass p + 1 overlaps
+//     the sweep of pass p; the lanes shift each staged source from its box frame into the group
+//     frame in place before the sweep, the shift following from the box coordinates that the
+//     record carries.
 // Each lane owns FORCE_R targets as two packed pairs (one f32x2 instruction serves two targets);
 // the lanes form slices that split every staged list; slice partials are reduced through the
 // warp's staging before the FP64 write-back and the fused tick.
@@ -40,17 +41,18 @@ constexpr int WDESC = 64;   // near descriptors per batch (per warp)
 constexpr int W_SRC = 0;                             // 2 x WSRC x 32 bytes
 constexpr int W_FARXY = 0;                           // WFAR x float4 (x, x, y, y), aliases W_SRC
 constexpr int W_FARM = W_FARXY + WFAR * 16;          // WFAR x float2 (M, M), aliases W_SRC
-constexpr int W_SHIFT = W_SRC + 2 * WSRC * 32;       // (WDESC + 1) x float2
-constexpr int W_NBOX = W_SHIFT + (WDESC + 1) * 8;    // (WDESC + 1) x int
+constexpr int W_NBOX = W_SRC + 2 * WSRC * 32;        // (WDESC + 1) x int
 constexpr int W_NPRE = W_NBOX + (WDESC + 1) * 4;     // (WDESC + 1) x int
 constexpr int NRUN = MAX_TG * MAX_TG;                // target runs (boxes) of a work item
 constexpr int W_RUN = W_NPRE + (WDESC + 1) * 4;      // 2 x (NRUN + 1) x int
 constexpr int W_MBAR = (W_RUN + 2 * (NRUN + 1) * 4 + 7) / 8 * 8;  // 2 x uint64
 constexpr int W_BYTES = (W_MBAR + 16 + 127) / 128 * 128;
 constexpr size_t FS_SMEM = (size_t)FW * W_BYTES;
-static_assert(W_FARM + WFAR * 8 <= W_SHIFT, "far staging must fit in the near-source buffers");
-static_assert(2 * 32 * NR * sizeof(float) <= (size_t)W_SHIFT, "slice partials alias the source buffers");
+static_assert(W_FARM + WFAR * 8 <= W_NBOX, "far staging must fit in the near-source buffers");
+static_assert(2 * 32 * NR * sizeof(float) <= (size_t)W_NBOX, "slice partials alias the source buffers");
 static_assert(32 * NR >= STREAM_CHUNK, "a warp must cover every target of a work item");
+constexpr int FDB = 2;      // far entries per lane decoded together (loads in flight)
+static_assert(WFAR % (32 * FDB) == 0, "far staging passes are whole rounds of FDB entries per lane");
 static_assert((WSRC * 32) % 16 == 0 && W_BYTES % 128 == 0, "bulk-copy destinations must be 16-byte aligned");
 
 template <bool KAHAN, int MINB>
@@ -61,7 +63,6 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
     float4 *farxy = reinterpret_cast<float4 *>(ws + W_FARXY);
     float2 *farm = reinterpret_cast<float2 *>(ws + W_FARM);
     unsigned char *srcb = ws + W_SRC;
-    float2 *nshift = reinterpret_cast<float2 *>(ws + W_SHIFT);
     int *nbox = reinterpret_cast<int *>(ws + W_NBOX);
     int *npre = reinterpret_cast<int *>(ws + W_NPRE);
     int *rstart = reinterpret_cast<int *>(ws + W_RUN);  // first particle of target run r
@@ -234,16 +235,35 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         // ---- far field: the group's accepted cells
         for (int f0 = 0; f0 < cnt.x; f0 += WFAR) {
             const int nf = min(WFAR, cnt.x - f0);
-            for (int k = lane; k < nf; k += 32) {
-                const unsigned code = (unsigned)lf[f0 + k];
-                const int l = (int)(code >> 28), loc = (int)(code & 0x0FFFFFFFu);
-                const int gl = sd.lvg[l];
-                const int ci = loc / gl, cj = loc - ci * gl;
-                const float4 rr = d.rec[sd.coff + sd.lvoff[l] + loc];
-                const float rx = __fadd_rn(__fmul_rn((float)((ci << l) - gx0), step_f), rr.x);
-                const float ry = __fadd_rn(__fmul_rn((float)((cj << l) - gy0), step_f), rr.y);
-                farxy[k] = make_float4(rx, rx, ry, ry);
-                farm[k] = make_float2(rr.z, rr.z);
+            // FDB entries per lane at a time: their codes, then their records, then the staging
+            for (int u0 = 0; u0 < WFAR / 32; u0 += FDB) {
+                unsigned code[FDB];
+                float4 rr[FDB];
+#pragma unroll
+                for (int u = 0; u < FDB; u++) {
+                    const int k = lane + 32 * (u0 + u);
+                    code[u] = k < nf ? (unsigned)lf[f0 + k] : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < FDB; u++) {
+                    if (lane + 32 * (u0 + u) < nf) {
+                        const int l = (int)(code[u] >> 28);
+                        const int ci = (int)((code[u] >> 14) & 0x3FFFu), cj = (int)(code[u] & 0x3FFFu);
+                        rr[u] = d.rec[sd.coff + sd.lvoff[l] + (long long)ci * sd.lvg[l] + cj];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < FDB; u++) {
+                    const int k = lane + 32 * (u0 + u);
+                    if (k < nf) {
+                        const int l = (int)(code[u] >> 28);
+                        const int ci = (int)((code[u] >> 14) & 0x3FFFu), cj = (int)(code[u] & 0x3FFFu);
+                        const float rx = __fadd_rn(__fmul_rn((float)((ci << l) - gx0), step_f), rr[u].x);
+                        const float ry = __fadd_rn(__fmul_rn((float)((cj << l) - gy0), step_f), rr[u].y);
+                        farxy[k] = make_float4(rx, rx, ry, ry);
+                        farm[k] = make_float2(rr[u].z, rr[u].z);
+                    }
+                }
             }
             __syncwarp();
             far_sweep(nf, true);
@@ -263,10 +283,9 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
             int nn = min(WDESC, cnt.y - b0);
             if (sub < 0) {
                 for (int k = lane; k <= nn; k += 32) {
-                    const int4 e = ln[2 * (b0 + k)];
+                    const int2 e = *reinterpret_cast<const int2 *>(ln + 2 * (b0 + k));
                     nbox[k] = e.x;
                     npre[k] = e.y;
-                    nshift[k] = make_float2(__int_as_float(e.z), __int_as_float(e.w));
                 }
                 __syncwarp();
             } else {
@@ -321,7 +340,6 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                         const int q = nkeep + __popc(mk & lt);
                         nbox[q] = e0.x;
                         npre[q] = base + inc - c;
-                        nshift[q] = make_float2(__int_as_float(e0.z), __int_as_float(e0.w));
                     } else if (acc) {
                         const int q = nacc + __popc(ma & lt);
                         const float rx = __int_as_float(e1.z), ry = __int_as_float(e1.w), m = __int_as_float(e1.y);
@@ -356,7 +374,6 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
             };
             if (npass > 0) issue(0);
             if (npass > 1) issue(1);
-            int kfirst = 0;  // first descriptor overlapping the current pass (warp-uniform)
             for (int p = 0; p < npass; p++) {
                 const int s0 = pbeg + p * WSRC, ns = min(WSRC, pend - s0);
                 const int buf = p & 1;
@@ -371,22 +388,20 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                     tma_ok = false;
                     break;
                 }
-                // shift the staged sources into the group frame in place: lane-strided over the
-                // pass, each lane following its sources' boxes forward through the descriptors
+                // shift the staged sources into the group frame in place, lane-strided over the
+                // pass: the shift of box (kx, ky) is (kx - gx0, ky - gy0) x step, as in the lists
                 float4 *s4 = reinterpret_cast<float4 *>(srcb + buf * (WSRC * 32));
-                {
-                    int k = kfirst;
-                    for (int j = lane; j < ns; j += 32) {
-                        while (k + 1 < nn && npre[k + 1] <= s0 + j) k++;
-                        const float2 sh = nshift[k];
-                        float4 v = s4[2 * j];
-                        v.x = __fadd_rn(sh.x, v.x);
-                        v.y = v.x;
-                        v.z = __fadd_rn(sh.y, v.z);
-                        v.w = v.z;
-                        s4[2 * j] = v;
-                    }
-                    while (kfirst + 1 < nn && npre[kfirst + 1] <= s0 + ns) kfirst++;  // next pass
+#pragma unroll 3
+                for (int j = lane; j < ns; j += 32) {
+                    float4 v = s4[2 * j];
+                    const int code = __float_as_int(s4[2 * j + 1].w);
+                    const float shx = __fmul_rn((float)((code >> 16) - gx0), step_f);
+                    const float shy = __fmul_rn((float)((code & 0xffff) - gy0), step_f);
+                    v.x = __fadd_rn(shx, v.x);
+                    v.y = v.x;
+                    v.z = __fadd_rn(shy, v.z);
+                    v.w = v.z;
+                    s4[2 * j] = v;
                 }
                 __syncwarp();
                 if (active) {
@@ -410,6 +425,7 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
             }
             __syncwarp();  // the descriptors are rewritten by the next batch
         }
+
 
         // ---- reduce slice partials (through the source buffers) and write
         if (active) {

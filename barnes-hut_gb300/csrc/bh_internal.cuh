@@ -41,7 +41,7 @@ constexpr int FORCE_R = 4;                                   // targets per thre
 constexpr int TARGET_CHUNK = FORCE_THREADS * FORCE_R;        // targets per work item
 constexpr int FRONTIER_CAP = 512;                            // traversal frontier per level
 constexpr int STREAM_CHUNK = 128;  // targets per work item of the list-streaming force kernel
-constexpr int LIST_MAX_G = 16384;  // far-list codes hold (level, cell) in 4 + 28 bits
+constexpr int LIST_MAX_G = 16384;  // far-list codes hold (level, column, row) in 4 + 14 + 14 bits
 constexpr int ITEM_BUCKETS = 32;   // log2 cost buckets of the heaviest-first item order
 
 struct SysDesc {
@@ -90,8 +90,9 @@ struct DevPlan {
     int *PID[2];
     double *AX, *AY;  // accelerations, box-sorted order
     float4 *P;
-    float4 *PD;  // per box-sorted particle: (x, x, y, y), (m, m, index, 0) -- the packed
-                 // near-field record, staged into shared memory by bulk copies
+    float4 *PD;  // per box-sorted particle: (x, x, y, y), (m, m, index, kx << 16 | ky) -- the
+                 // packed near-field record (offsets from the box origin; box coordinates),
+                 // staged into shared memory by bulk copies
     int *key, *slot, *skey;
     int *counts, *box_start, *tile_sums;
     int *qcounts;  // per box, particles in each quadrant (x half * 2 + y half); a box's particles
@@ -101,7 +102,7 @@ struct DevPlan {
     float4 *rec, *rec2;
     // interaction lists of every target group (list-streaming path), in fixed per-group slots
     // (SysDesc lfcap far codes, lncap + 1 near descriptors), counts in lcnt (x far, y near):
-    //   far code: level << 28 | cell index within the level;
+    //   far code: level << 28 | cell column << 14 | cell row (columns, rows < LIST_MAX_G);
     //   near descriptor: two int4 -- (first particle, exclusive prefix of the boxes' particle
     //   counts, shift of the box origin from the group origin as float bits x, y) and (box index
     //   in the system, mass, centre of mass in the group frame x, y as float bits); descriptor

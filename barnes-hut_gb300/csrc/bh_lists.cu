@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(LW * 32) k_lists(DevPlan d) {
                     const int ntot = __shfl_sync(0xffffffffu, inc, 31);
                     if (kind == 1) {
                         const int pos = nfar + __popc(mf & lt_mask);
-                        if (pos < sd.lfcap) far_out[pos] = (int)(((unsigned)l << 28) | (unsigned)loc[u]);
+                        if (pos < sd.lfcap) far_out[pos] = (int)(((unsigned)l << 28) | ((unsigned)ci << 14) | (unsigned)cj);
                     } else if (kind == 2) {
                         const int pos = nnear + __popc(mn & lt_mask);
                         if (pos < sd.lncap) fn[pos] = loc[u];

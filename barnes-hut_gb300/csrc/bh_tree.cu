@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
         const float mf = __double2float_rn(m);
         d.P[dst] = make_float4(ox, oy, mf, __int_as_float(dst));
         d.PD[2 * (long long)dst] = make_float4(ox, ox, oy, oy);
-        d.PD[2 * (long long)dst + 1] = make_float4(mf, mf, __int_as_float(dst), 0.f);
+        d.PD[2 * (long long)dst + 1] = make_float4(mf, mf, __int_as_float(dst), __int_as_float((kx << 16) | ky));
         d.skey[dst] = key;
     }
 }
