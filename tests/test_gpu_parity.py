@@ -221,6 +221,31 @@ def test_refined_lists_vs_fp64_oracle(TG, dense_min, quad_min):
     assert plan.error_flags() == 0
 
 
+@pytest.mark.parametrize("TG,G,dense_min", [(4, 128, 8), (8, 96, 4)])
+def test_sparse_boxes_many_descriptors_per_pass(TG, G, dense_min):
+    """One or two particles per box: a staging pass of the list-streaming kernel spans more than
+    a warp's worth (32) of near-box descriptors, on group lists and on refined lists alike.  Pair
+    counts exact, forces within 1e-5 of the oracle, and every bounded copy wait completes."""
+    from barneshut.gb300 import workloads
+    from oracle import oracle
+
+    x, y, m, vx, vy = workloads.cluster_mixture(20000, seed=35)
+    eps = 1e-3
+    plan = make_plan(20000, G, grav_constant=1.0, tick_seconds=1e-5, softening=eps, cutoff_r2=0.0,
+                     theta=0.5, group_dim=TG, precision=1, dense_min=dense_min, quad_min=-1)
+    plan.load(x, y, m, vx, vy)
+    plan.create_tree()
+    plan.summarize()
+    plan.evaluate()
+    out = plan.store()
+    assert plan.error_flags() == 0
+    nn, nf = plan.pair_counts()
+    ax, ay, on, of = oracle.theta_evaluate(x, y, m, G, TG=TG, theta=0.5, eps2=eps * eps, cutoff=0.0,
+                                           dense_min=dense_min, quad_min=0)
+    assert (nn, nf) == (on, of)
+    assert oracle.rel_rms(out["ax"].cpu().numpy(), out["ay"].cpu().numpy(), ax, ay) <= 1e-5
+
+
 def test_theta_error_vs_direct_sum():
     from barneshut.gb300 import workloads
     from oracle import oracle
