@@ -46,7 +46,8 @@ constexpr int W_NPRE = W_NBOX + (WDESC + 1) * 4;     // (WDESC + 1) x int
 constexpr int NRUN = MAX_TG * MAX_TG;                // target runs (boxes) of a work item
 constexpr int W_RUN = W_NPRE + (WDESC + 1) * 4;      // 2 x (NRUN + 1) x int
 constexpr int W_MBAR = (W_RUN + 2 * (NRUN + 1) * 4 + 7) / 8 * 8;  // 2 x uint64
-constexpr int W_BYTES = (W_MBAR + 16 + 127) / 128 * 128;
+constexpr int W_CNT = W_MBAR + 16;                   // 2 x uint64: the warp's near, far pair counts
+constexpr int W_BYTES = (W_CNT + 16 + 127) / 128 * 128;
 constexpr size_t FS_SMEM = (size_t)FW * W_BYTES;
 static_assert(W_FARM + WFAR * 8 <= W_NBOX, "far staging must fit in the near-source buffers");
 static_assert(2 * 32 * NR * sizeof(float) <= (size_t)W_NBOX, "slice partials alias the source buffers");
@@ -73,10 +74,11 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
     const int nxt = (d.glob->epoch + 1) & 1;
     const double *Xs = d.X[nxt], *Ys = d.Y[nxt];
     const long long nitems = d.sitem_off[d.NG_total];
-    unsigned long long npairs = 0, fpairs = 0;  // counted by lane 0
+    unsigned long long *wcnt = reinterpret_cast<unsigned long long *>(ws + W_CNT);  // lane 0 counts
     uint32_t phases = 0u;  // bit b: parity of buffer b's current mbarrier phase
     bool tma_ok = true;  // warp-uniform; cleared (and flagged) when a copy wait times out
     if (lane == 0) {
+        wcnt[0] = wcnt[1] = 0ull;
         tc::mbar_init(&mbar[0], 1);
         tc::mbar_init(&mbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                     }
                 }
             }
-            fpairs += (unsigned long long)T * nf;
+            if (lane == 0) wcnt[1] += (unsigned long long)T * nf;
             __syncwarp();  // the staging is rewritten next
         };
 
@@ -419,7 +421,7 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                         }
                     }
                 }
-                npairs += (unsigned long long)T * ns;
+                if (lane == 0) wcnt[0] += (unsigned long long)T * ns;
                 __syncwarp();  // every lane is done with this buffer
                 if (p + 2 < npass) issue(p + 2);
             }
@@ -474,8 +476,8 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         __syncwarp();  // the staging and the column table are reused by the next item
     }
     if (lane == 0) {
-        atomicAdd(&d.glob->near_pairs, npairs);
-        atomicAdd(&d.glob->far_pairs, fpairs);
+        atomicAdd(&d.glob->near_pairs, wcnt[0]);
+        atomicAdd(&d.glob->far_pairs, wcnt[1]);
     }
 }
 
