@@ -550,18 +550,19 @@ extern "C" int bh_step_graph(bh_plan *p, int nsteps, void *stream) {
 
 extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     if (!p || !count) return BH_ERR_INVALID;
-    // prologue, 3 box-scan phases, work items (count, 3 scan phases, fill),
-    // pyramid levels, records; with particles also bbox, bbox
-    // finalize, place, scatter, leaf moments, force (and before it the list build and the
-    // two kernels of the heaviest-first item order); list streaming also builds its own work
-    // items (count, 3 scan phases, fill)
+    // prologue, 3 box-scan phases, pyramid levels, records; with particles also bbox, bbox
+    // finalize, place, scatter, leaf moments, force (and before it, when streaming, the list
+    // build and the two kernels of the heaviest-first item order); work items (count, 3 scan
+    // phases, fill) for the walk or the learned correction, and for list streaming
     // pyramid: one launch per level while its cells exceed 256, then one for the remaining levels
     int pyr = 0;
     for (int l = 1; l < p->Lmax; l++) {
         pyr++;
         if (p->lvl[(size_t)l * (p->nsys + 1) + p->nsys] <= 256) break;
     }
-    *count = 1 + 3 + 5 + pyr + 1 + (p->n_total > 0 ? 6 : 0) + (p->stream ? 5 : 0) + (p->stream && p->n_total > 0 ? 3 : 0);
+    const bool walk_items = !p->stream || (p->params.flags & BH_FLAG_LEARNED);
+    *count = 1 + 3 + (walk_items ? 5 : 0) + pyr + 1 + (p->n_total > 0 ? 6 : 0) + (p->stream ? 5 : 0) +
+             (p->stream && p->n_total > 0 ? 3 : 0);
     return BH_OK;
 }
 
@@ -702,6 +703,8 @@ extern "C" int bh_learned_pairs(bh_plan *p, double theta_hi, double theta_lo, in
     if (!(theta_hi > theta_lo) || !(theta_lo > 0.0) || item_stride < 1 || item_offset < 0 ||
         tpi < 1 || capacity < 0 || !feats || !targets || !counter)
         return fail(p, BH_ERR_INVALID, "bad learned_pairs arguments");
+    // a streaming plan without the learned correction builds no walk items in its step
+    if (p->dev.stream && !p->dev.learned) CK(p, launch_walk_items(p->dev, (cudaStream_t)stream), "work items");
     CK(p, launch_learned_pairs(p->dev, theta_hi, theta_lo, max_level, item_offset, item_stride, tpi,
                                feats, targets, counter, capacity, (cudaStream_t)stream),
        "learned pairs");

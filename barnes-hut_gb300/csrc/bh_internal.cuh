@@ -288,6 +288,7 @@ cudaError_t launch_bbox(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_place(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_scan(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_items(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_walk_items(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st);

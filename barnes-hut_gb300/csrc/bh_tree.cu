@@ -560,13 +560,26 @@ cudaError_t launch_place(const DevPlan &d, cudaStream_t st) {
 cudaError_t launch_scan(const DevPlan &d, cudaStream_t st) {
     return scan_excl(d.counts, d.box_start, d.B_total, d.tile_sums, st);
 }
-cudaError_t launch_items(const DevPlan &d, cudaStream_t st) {
+// Work items of the walk kernel and of the learned correction (group, target chunk).
+cudaError_t launch_walk_items(const DevPlan &d, cudaStream_t st) {
     unsigned g = grid_for(d.NG_total, TPB, 152LL * 8);
     k_group_items<<<g, TPB, 0, st>>>(d);
     cudaError_t e = scan_excl(d.item_cnt, d.item_off, d.NG_total, d.tile_sums, st);
     if (e != cudaSuccess) return e;
     k_fill_items<<<g, TPB, 0, st>>>(d);
+    return cudaGetLastError();
+}
+// The step's work items: the walk items where the walk or the learned correction runs, the
+// list-streaming items where the lists are streamed (a streaming plan builds walk items only
+// with the learned correction, or on demand for bh_learned_pairs).
+cudaError_t launch_items(const DevPlan &d, cudaStream_t st) {
+    cudaError_t e;
+    if (!d.stream || d.learned) {
+        e = launch_walk_items(d, st);
+        if (e != cudaSuccess) return e;
+    }
     if (d.stream) {
+        unsigned g = grid_for(d.NG_total, TPB, 152LL * 8);
         k_sitem_count<<<g, TPB, 0, st>>>(d);
         e = scan_excl(d.sitem_cnt, d.sitem_off, d.NG_total, d.tile_sums, st);
         if (e != cudaSuccess) return e;
