@@ -101,7 +101,9 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         const SysDyn &dy = d.dyn[s];
         const long long lg = g - sd.goff;
         const int TG = sd.TG, G = sd.G;
-        const int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
+        const int tgs = __ffs(TG) - 1;  // TG is a power of two
+        // a system has fewer than 2^31 groups (G <= LIST_MAX_G)
+        const int gi = (int)lg / sd.NGs, gj = (int)lg - gi * sd.NGs;
         const int gx0 = gi * TG, gy0 = gj * TG;
         // the item's targets: runs of box-sorted particles, one per box of the group (column-major;
         // a box outside the item's set is an empty run; a quadrant item's box run is the quadrant)
@@ -113,7 +115,7 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                 const int b = b0 + lane;
                 int st = 0, len = 0;
                 if (b < nrun) {
-                    const int cx = b / TG, cy = b - cx * TG;
+                    const int cx = b >> tgs, cy = b & (TG - 1);
                     if (gx0 + cx < G && gy0 + cy < G) {
                         const long long bb = sd.boff + (long long)(gx0 + cx) * G + gy0 + cy;
                         st = d.box_start[bb];
@@ -158,7 +160,8 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         const bool active = lane < nslice * nthr;
         const int slice = active ? lane / nthr : 0, tl = active ? lane % nthr : 0;
         // sorted index of the lane's target r (recomputed in the epilogue rather than kept live)
-        auto target_index = [&](int r) {
+        // (the run is the target's box within the group, column-major)
+        auto target_index = [&](int r, int &run) {
             const int v = tl * NR + r;
             const int u = c0 + (v < T ? v : 0);
             int lo = 0, hi = nrun;  // the run r with rpre[r] <= u < rpre[r + 1]
@@ -166,17 +169,17 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                 const int mid = (lo + hi) >> 1;
                 if (rpre[mid] <= u) lo = mid; else hi = mid;
             }
+            run = lo;
             return rstart[lo] + (u - rpre[lo]);
         };
         float tx[NR], ty[NR];
 #pragma unroll
         for (int r = 0; r < NR; r++) {
-            const int ti = target_index(r);
+            int run;
+            const int ti = target_index(r, run);
             const float4 p = d.P[ti];
-            const int lb = d.skey[ti] - (int)sd.boff;
-            const int kx = lb / G, ky = lb - kx * G;
-            tx[r] = __fadd_rn(__fmul_rn((float)(kx - gx0), step_f), p.x);
-            ty[r] = __fadd_rn(__fmul_rn((float)(ky - gy0), step_f), p.y);
+            tx[r] = __fadd_rn(__fmul_rn((float)(run >> tgs), step_f), p.x);
+            ty[r] = __fadd_rn(__fmul_rn((float)(run & (TG - 1)), step_f), p.y);
         }
         // negated target coordinates, near accumulators, far sums and compensations, in pairs
         f2_t ntx2[NR / 2], nty2[NR / 2], nax2[NR / 2], nay2[NR / 2];
@@ -296,7 +299,7 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                 // that rectangle's origin) is swept as a far entry; the others stay near and are
                 // re-prefixed
                 const int bsel = qbox >= 0 ? qbox : sub;
-                const int bcx = bsel / TG, bcy = bsel - bcx * TG;
+                const int bcx = bsel >> tgs, bcy = bsel & (TG - 1);
                 float oxb, oyb, wr;  // rectangle origin in the group frame, edge
                 if (qbox >= 0) {
                     const float half_f = 0.5f * step_f;
@@ -456,7 +459,8 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                     sx += o[0];
                     sy += o[1];
                 }
-                const int t = target_index(r);
+                int run;
+                const int t = target_index(r, run);
                 double ax = d.gconst * (double)sx, ay = d.gconst * (double)sy;
                 if (accumulate) {
                     ax += d.AX[t];
