@@ -41,7 +41,7 @@ EXPORTS = (
     "bh_pair_counts", "bh_box_moments", "bh_grid_info", "bh_direct_sample", "bh_diagnostics",
     "bh_kernels_per_step", "bh_mlp_param_count", "bh_mlp_image_bytes", "bh_mlp_pack",
     "bh_mlp_forward", "bh_mlp_train_batch", "bh_mlp_adam", "bh_set_correction", "bh_learned_pairs",
-    "bh_direct_sum_noalloc", "bh_generate",
+    "bh_direct_sum_noalloc", "bh_generate", "bh_graph_kernel_nodes",
 )
 BH_GEN_UNIFORM, BH_GEN_GAUSS, BH_GEN_CLUSTER = 0, 1, 2
 BH_NOALLOC_MAX_TARGETS = 4096
@@ -117,6 +117,7 @@ def load_library(path=None):
     L.bh_direct_sample.argtypes = [vp, i, vp, ll, vp, vp, vp]
     L.bh_diagnostics.argtypes = [vp, i, i, vp, vp]
     L.bh_kernels_per_step.argtypes = [vp, pi]
+    L.bh_graph_kernel_nodes.argtypes = [vp, pi]
     L.bh_set_correction.argtypes = [vp, vp, vp]
     L.bh_direct_sum_noalloc.argtypes = [vp, vp, vp, ll, vp, ll, d, d, vp, vp, vp]
     L.bh_learned_pairs.argtypes = [vp, d, d, i, ll, ll, i, vp, vp, vp, ll, vp]
@@ -315,6 +316,12 @@ class Plan:
     def kernels_per_step(self):
         c = ctypes.c_int()
         self._check(self.L.bh_kernels_per_step(self.h, ctypes.byref(c)))
+        return c.value
+
+    def graph_kernel_nodes(self):
+        """Kernel nodes of the step graph captured by the last step_graph call."""
+        c = ctypes.c_int()
+        self._check(self.L.bh_graph_kernel_nodes(self.h, ctypes.byref(c)))
         return c.value
 
     def pair_counts(self):

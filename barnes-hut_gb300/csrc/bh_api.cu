@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 #include <new>
 #include <vector>
 
@@ -42,6 +43,7 @@ struct bh_plan {
     bool acc_stale = true;  // next bh_evaluate overwrites instead of accumulating
     // graph cache
     cudaGraphExec_t gexec = nullptr;
+    int gkernels = -1;  // kernel nodes of the captured step graph
     int gsteps = 0;
     cudaStream_t gstream = nullptr;
     // learned correction (caller-owned device buffers)
@@ -537,6 +539,23 @@ extern "C" int bh_step_graph(bh_plan *p, int nsteps, void *stream) {
         cudaError_t e = cudaStreamEndCapture(p->gstream, &g);
         if (er) return er;
         if (e != cudaSuccess) return cuda_fail(p, e, "end capture");
+        size_t nn = 0;
+        e = cudaGraphGetNodes(g, nullptr, &nn);
+        if (e == cudaSuccess) {
+            std::vector<cudaGraphNode_t> nodes(nn);
+            e = cudaGraphGetNodes(g, nodes.data(), &nn);
+            int nk = 0;
+            for (size_t k = 0; e == cudaSuccess && k < nn; k++) {
+                cudaGraphNodeType t;
+                e = cudaGraphNodeGetType(nodes[k], &t);
+                if (t == cudaGraphNodeTypeKernel) nk++;
+            }
+            p->gkernels = nk;
+        }
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            return cuda_fail(p, e, "graph nodes");
+        }
         e = cudaGraphInstantiate(&p->gexec, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return cuda_fail(p, e, "graph instantiate");
@@ -563,6 +582,13 @@ extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     const bool walk_items = !p->stream || (p->params.flags & BH_FLAG_LEARNED);
     *count = 1 + 3 + (walk_items ? 5 : 0) + pyr + 1 + (p->n_total > 0 ? 6 : 0) + (p->stream ? 5 : 0) +
              (p->stream && p->n_total > 0 ? 3 : 0);
+    return BH_OK;
+}
+
+extern "C" int bh_graph_kernel_nodes(const bh_plan *p, int *count) {
+    if (!p || !count) return BH_ERR_INVALID;
+    if (p->gkernels < 0) return BH_ERR_INVALID;  // no step graph captured yet
+    *count = p->gkernels;
     return BH_OK;
 }
 

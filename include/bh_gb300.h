@@ -176,6 +176,11 @@ int bh_step_graph(bh_plan *plan, int nsteps, void *stream);
  * singlegpu.py:41-99). */
 int bh_kernels_per_step(const bh_plan *plan, int *count);
 
+/* Kernel nodes of the step graph bh_step_graph captured last (its nsteps
+ * rounds); BH_ERR_INVALID before the first capture.  Host only; no reference
+ * counterpart. */
+int bh_graph_kernel_nodes(const bh_plan *plan, int *count);
+
 /* Synchronise the stream and read (then clear) the device error flags. */
 int bh_error_flags(bh_plan *plan, unsigned *flags, void *stream);
 

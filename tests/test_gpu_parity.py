@@ -353,6 +353,32 @@ def test_graph_replay_equals_eager():
     assert_same_run(a.store(), b.store())
 
 
+@pytest.mark.parametrize("case", ["stream", "stream_quad", "walk", "flat", "batched"])
+def test_kernels_per_step_matches_graph(case):
+    """bh_kernels_per_step (the launch count the benchmark reports) equals the kernel nodes of
+    the captured step graph, nsteps rounds at a time."""
+    from barneshut.gb300 import workloads
+
+    N = native()
+    x, y, m, vx, vy = workloads.cluster_mixture(30000, seed=71)
+    kw = dict(grav_constant=1.0, tick_seconds=1e-5, softening=1e-3, cutoff_r2=0.0, theta=0.5)
+    n, G = [30000], [32]
+    if case == "stream_quad":
+        kw.update(group_dim=2, dense_min=16, quad_min=32)
+    elif case == "walk":
+        kw.update(flags=N.BH_FLAG_WALK)
+    elif case == "flat":
+        kw.update(theta=0.0, softening=0.0, cutoff_r2=1e-5)
+    elif case == "batched":
+        n, G = [20000, 10000], [24, 4]
+    plan = make_plan(n, G, **kw)
+    plan.load(x, y, m, vx, vy)
+    for nsteps in (1, 3):
+        plan.step_graph(nsteps)
+        assert plan.graph_kernel_nodes() == nsteps * plan.kernels_per_step()
+    assert plan.error_flags() == 0
+
+
 # ---------------------------------------------------------------- samplers
 def test_direct_sample_matches_oracle():
     from barneshut.gb300 import workloads
