@@ -97,3 +97,24 @@ def test_missing_library_fails_loudly(monkeypatch):
     monkeypatch.setattr(native, "_lib", None)
     with pytest.raises(native.NativeLibraryError):
         native.load_library("/nonexistent/libbh_gb300.so")
+
+
+def test_launch_count_host_logic(lib):
+    """bh_kernels_per_step is host-only: a list-streaming plan builds no walk work items unless
+    it carries the learned correction; a walking plan builds them (5 kernels: count, 3 scan
+    phases, fill).  No step graph exists before the first capture."""
+    from barneshut.gb300 import native
+
+    def count(**kw):
+        rc, h = _create(lib, [100000], [64], theta=0.5, softening=1e-3, cutoff_r2=0.0, **kw)
+        assert rc == 0
+        c = ctypes.c_int()
+        assert lib.bh_kernels_per_step(h, ctypes.byref(c)) == 0
+        g = ctypes.c_int()
+        assert lib.bh_graph_kernel_nodes(h, ctypes.byref(g)) == native.BH_ERR_INVALID
+        assert lib.bh_plan_destroy(h) == 0
+        return c.value
+
+    stream = count()
+    assert count(flags=native.BH_FLAG_WALK) == stream + 5 - 8  # walk items in, stream items and lists out
+    assert count(flags=native.BH_FLAG_LEARNED) == stream + 5
