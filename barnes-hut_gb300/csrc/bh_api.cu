@@ -26,12 +26,13 @@ struct bh_plan {
     std::vector<long long> poff, boff, coff, goff, lvl;
     int Lmax = 1;
     long long n_total = 0, B_total = 0, C_total = 0, NG_total = 0;
+    long long org_total = 0;  // entries of the box-origin tables (2 G per system)
     // workspace layout (byte offsets)
     size_t ws_bytes = 0;
     size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
     size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_tiles, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
-        o_rec2, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk, o_qcnt;
+        o_rec2, o_org, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk, o_qcnt;
     bool stream = false;  // theta-mode interaction lists built once per group and streamed
     int chunk = TARGET_CHUNK;
     int dense_min = BH_STREAM_DENSE_MIN;
@@ -165,6 +166,8 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
         }
         d.TG = TG;
         d.NGs = (G + TG - 1) / TG;
+        d.ooff = p->org_total;
+        p->org_total += 2LL * G;
         d.boff = p->boff[s];
         d.coff = p->coff[s];
         d.goff = p->goff[s];
@@ -272,6 +275,7 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_mom = take(48 * C);
     p->o_rec = take(16 * C);
     p->o_rec2 = take(16 * C);
+    p->o_org = take(8 * (size_t)p->org_total);
     p->ws_bytes = o;
     *out = p;
     return BH_OK;
@@ -338,6 +342,7 @@ static void fill_dev(bh_plan *p) {
     d.mom = (double *)(w + p->o_mom);
     d.rec = (float4 *)(w + p->o_rec);
     d.rec2 = (float4 *)(w + p->o_rec2);
+    d.org = (double *)(w + p->o_org);
     d.lfar = (int *)(w + p->o_lfar);
     d.lnear = (int4 *)(w + p->o_lnear);
     d.lcnt = (int2 *)(w + p->o_lcnt);

@@ -54,6 +54,7 @@ struct SysDesc {
     long long lvoff[MAX_LEVELS]; // first cell of each level, relative to coff
     long long lfoff, lnoff;      // first far / near list slot of the system's groups
     int lfcap, lncap;            // far / near list slots per group
+    long long ooff;              // first entry of the system's box-origin table (G x, then G y)
 };
 
 struct SysDyn {
@@ -98,6 +99,7 @@ struct DevPlan {
     int *qcounts;  // per box, particles in each quadrant (x half * 2 + y half); a box's particles
                    // are stored quadrant by quadrant
     int *item_cnt, *item_off, *item_group;  // force work items (group, target chunk)
+    double *org;  // per system: box origins mn + k step along x (k < G), then along y, FP64
     double *mom;
     float4 *rec, *rec2;
     // interaction lists of every target group (list-streaming path), in fixed per-group slots

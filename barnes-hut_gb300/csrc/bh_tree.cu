@@ -108,11 +108,8 @@ __global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
 
 // One thread per system: the square bounding box (helpers/grid.py:10-26), its
 // box edge step = edge / G (base.py:233) and 1 / step, once per step.
-__global__ void k_bbox_finalize(DevPlan d) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.nsys) return;
+__device__ void bbox_finalize_sys(const DevPlan &d, int s) {
     SysDyn &dy = d.dyn[s];
-    if (d.sys[s].n == 0) return;
     double mnx = unord_bits(dy.bbmin[0]), mny = unord_bits(dy.bbmin[1]);
     double mxx = unord_bits(dy.bbmax[0]), mxy = unord_bits(dy.bbmax[1]);
     double step;
@@ -134,6 +131,23 @@ __global__ void k_bbox_finalize(DevPlan d) {
         dy.key_tol = tol < 0.25 ? (float)tol : 1.f;
     } else {
         dy.key_tol = 1.f;  // the FP64 key for every particle
+    }
+}
+
+// One CTA per system: thread 0 squares the bounding box and derives the grid; then the CTA
+// tabulates the box origins mn + k step (FP64), which the scatter reads instead of forming
+// them per particle on the slow FP64 pipe.
+__global__ void k_bbox_finalize(DevPlan d) {
+    const int s = blockIdx.x;
+    SysDyn &dy = d.dyn[s];
+    if (d.sys[s].n == 0) return;
+    if (threadIdx.x == 0) bbox_finalize_sys(d, s);
+    __syncthreads();
+    const int G = d.sys[s].G;
+    double *org = d.org + d.sys[s].ooff;
+    for (int k = threadIdx.x; k < G; k += blockDim.x) {
+        org[k] = box_origin(dy.minx, k, dy.step);
+        org[G + k] = box_origin(dy.miny, k, dy.step);
     }
 }
 
@@ -410,8 +424,9 @@ __global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
         d.VY[nxt][dst] = d.VY[cur][i];
         d.M[nxt][dst] = m;
         d.PID[nxt][dst] = d.PID[cur][i];
-        float ox = __double2float_rn(__dsub_rn(x, box_origin(dy.minx, kx, dy.step)));
-        float oy = __double2float_rn(__dsub_rn(y, box_origin(dy.miny, ky, dy.step)));
+        const double *org = d.org + sd.ooff;  // box origins (k_bbox_finalize)
+        float ox = __double2float_rn(__dsub_rn(x, org[kx]));
+        float oy = __double2float_rn(__dsub_rn(y, org[sd.G + ky]));
         const float mf = __double2float_rn(m);
         d.P[dst] = make_float4(ox, oy, mf, __int_as_float(dst));
         d.PD[2 * (long long)dst] = make_float4(ox, ox, oy, oy);
@@ -553,7 +568,7 @@ cudaError_t launch_bbox(const DevPlan &d, cudaStream_t st) {
 }
 cudaError_t launch_place(const DevPlan &d, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_bbox_finalize<<<(d.nsys + 127) / 128, 128, 0, st>>>(d);
+    k_bbox_finalize<<<d.nsys, 128, 0, st>>>(d);
     k_place<<<grid_for(d.n_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
