@@ -32,7 +32,7 @@ namespace bh {
 constexpr int NR = FORCE_R;
 constexpr int FW = 4;       // warps per CTA
 constexpr int WFAR = 128;   // far entries per staging pass (per warp)
-constexpr int WSRC = 80;    // near sources per bulk-copy pass (per warp, per buffer)
+constexpr int WSRC = 88;    // near sources per bulk-copy pass (per warp, per buffer)
 constexpr int WDESC = 64;   // near descriptors per batch (per warp)
 
 // per-warp shared-memory carve-up (bytes).  The far phase of an item ends before its near phase
