@@ -174,6 +174,23 @@ __device__ __forceinline__ int box_key1(double p, double mn, double step, int G)
 // Same key, computed as floor((p - mn) * inv_step).  The product differs from the correctly
 // rounded quotient by at most ~3 ulp, so the floors can differ only when the quotient lies
 // within ~3 ulp of an integer (< 1e-10 for G <= 32768); only then is the IEEE division taken.
+// FP64 -> FP32 rounded to nearest, ties to even (the IEEE 754 narrowing conversion), on the
+// integer pipes: bit-identical to __double2float_rn
+// whenever the result is a normal float (a mantissa carry rounds into the exponent, and past the
+// largest float into infinity, as IEEE rounding does); zero, subnormal and out-of-range inputs
+// take __double2float_rn.  GB300 executes that conversion on its slow FP64 pipe.
+__device__ __forceinline__ float f64_to_f32_rn(double p) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(p);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;  // biased float exponent
+    if (e < 1 || e > 254) return __double2float_rn(p);
+    // the float fraction: hi's 20 fraction bits and lo's top 3; the 29 dropped bits round it
+    const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1FFFFFFFu, half = 0x10000000u;
+    const unsigned up = (rest > half || (rest == half && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float(((hi & 0x80000000u) | ((unsigned)e << 23) | m) + up);
+}
+
 __device__ __forceinline__ int box_key1_fast(double p, double mn, double step, double inv, int G) {
     if (!(step > 0.0)) return 0;
     double d = __dsub_rn(p, mn);
@@ -192,7 +209,7 @@ __device__ __forceinline__ int box_key1_fast(double p, double mn, double step, d
 // FP64 key costs about nine FP64 operations per coordinate.
 __device__ __forceinline__ int box_key1_f32(double p, double mn, double step, double inv, float mn_f,
                                             float inv_f, float tol, int G) {
-    const float q = __fmul_rn(__fsub_rn(__double2float_rn(p), mn_f), inv_f);
+    const float q = __fmul_rn(__fsub_rn(f64_to_f32_rn(p), mn_f), inv_f);
     const float k = floorf(q);
     const float fr = q - k;
     if (!(tol < 0.25f) || fr < tol || fr > 1.f - tol) return box_key1_fast(p, mn, step, inv, G);
@@ -215,7 +232,7 @@ __device__ __forceinline__ int half_key1_fast(double p, double mn, double step, 
 // The same from the float estimate (2 q_f carries twice box_key1_f32's error bound).
 __device__ __forceinline__ int half_key1_f32(double p, double mn, double step, double inv, float mn_f,
                                              float inv_f, float tol, int G) {
-    const float q = 2.f * __fmul_rn(__fsub_rn(__double2float_rn(p), mn_f), inv_f);
+    const float q = 2.f * __fmul_rn(__fsub_rn(f64_to_f32_rn(p), mn_f), inv_f);
     const float k = floorf(q);
     const float fr = q - k;
     const float tol2 = 2.f * tol;

@@ -425,9 +425,9 @@ __global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
         d.M[nxt][dst] = m;
         d.PID[nxt][dst] = d.PID[cur][i];
         const double *org = d.org + sd.ooff;  // box origins (k_bbox_finalize)
-        float ox = __double2float_rn(__dsub_rn(x, org[kx]));
-        float oy = __double2float_rn(__dsub_rn(y, org[sd.G + ky]));
-        const float mf = __double2float_rn(m);
+        float ox = f64_to_f32_rn(__dsub_rn(x, org[kx]));
+        float oy = f64_to_f32_rn(__dsub_rn(y, org[sd.G + ky]));
+        const float mf = f64_to_f32_rn(m);
         d.P[dst] = make_float4(ox, oy, mf, __int_as_float(dst));
         d.PD[2 * (long long)dst] = make_float4(ox, ox, oy, oy);
         d.PD[2 * (long long)dst + 1] = make_float4(mf, mf, __int_as_float(dst), __int_as_float((kx << 16) | ky));
@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(TPB) k_records(DevPlan d) {
         double M = q[0];
         if (M > 0.0) {
             double cx = q[1] / M, cy = q[2] / M;
-            d.rec[c] = make_float4(__double2float_rn(cx), __double2float_rn(cy), __double2float_rn(M), 0.f);
+            d.rec[c] = make_float4(f64_to_f32_rn(cx), f64_to_f32_rn(cy), f64_to_f32_rn(M), 0.f);
             int s = find_seg(d.coff_tab, d.nsys, c);
             const SysDesc &sd = d.sys[s];
             long long loc = c - sd.coff;
@@ -546,8 +546,8 @@ __global__ void __launch_bounds__(TPB) k_records(DevPlan d) {
             double sz = (double)(1 << l) * d.dyn[s].step;
             double nrm = 1.0 / (M * sz * sz);
             double ixx = q[3] - q[1] * cx, ixy = q[4] - q[1] * cy, iyy = q[5] - q[2] * cy;
-            d.rec2[c] = make_float4(__double2float_rn(ixx * nrm), __double2float_rn(ixy * nrm),
-                                    __double2float_rn(iyy * nrm), 0.f);
+            d.rec2[c] = make_float4(f64_to_f32_rn(ixx * nrm), f64_to_f32_rn(ixy * nrm),
+                                    f64_to_f32_rn(iyy * nrm), 0.f);
         } else {
             d.rec[c] = make_float4(0.f, 0.f, 0.f, 0.f);
             d.rec2[c] = make_float4(0.f, 0.f, 0.f, 0.f);
