@@ -405,33 +405,67 @@ __global__ void __launch_bounds__(TPB) k_sitem_fill(DevPlan d) {
 // per-sorted-particle key.
 __global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
     const int cur = d.glob->epoch & 1, nxt = cur ^ 1;
-    long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < d.n_total; i += stride) {
-        const int key4 = d.key[i];
-        const int key = key4 >> 2, quad = key4 & 3;
-        const int4 qc = reinterpret_cast<const int4 *>(d.qcounts)[key];
-        const int qpre = (quad > 0 ? qc.x : 0) + (quad > 1 ? qc.y : 0) + (quad > 2 ? qc.z : 0);
-        int dst = d.box_start[key] + qpre + d.slot[i];
-        int s = find_seg(d.boff_tab, d.nsys, key);
-        const SysDesc &sd = d.sys[s];
-        const SysDyn &dy = d.dyn[s];
-        int lb = (int)(key - sd.boff);
-        int kx = lb / sd.G, ky = lb - kx * sd.G;
-        double x = d.X[cur][i], y = d.Y[cur][i], m = d.M[cur][i];
-        d.X[nxt][dst] = x;
-        d.Y[nxt][dst] = y;
-        d.VX[nxt][dst] = d.VX[cur][i];
-        d.VY[nxt][dst] = d.VY[cur][i];
-        d.M[nxt][dst] = m;
-        d.PID[nxt][dst] = d.PID[cur][i];
-        const double *org = d.org + sd.ooff;  // box origins (k_bbox_finalize)
-        float ox = f64_to_f32_rn(__dsub_rn(x, org[kx]));
-        float oy = f64_to_f32_rn(__dsub_rn(y, org[sd.G + ky]));
-        const float mf = f64_to_f32_rn(m);
-        d.P[dst] = make_float4(ox, oy, mf, __int_as_float(dst));
-        d.PD[2 * (long long)dst] = make_float4(ox, ox, oy, oy);
-        d.PD[2 * (long long)dst + 1] = make_float4(mf, mf, __int_as_float(dst), __int_as_float((kx << 16) | ky));
-        d.skey[dst] = key;
+    // SU particles per thread per round, each stage's loads issued for all of them before the
+    // next stage uses them (the chain key -> box start and quadrant counts -> destination, and
+    // the state loads, would otherwise run one particle at a time)
+    constexpr int SU = 4;
+    const long long n = d.n_total, stride = (long long)gridDim.x * blockDim.x;
+    for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += SU * stride) {
+        int key4[SU], dst[SU];
+#pragma unroll
+        for (int u = 0; u < SU; u++) {
+            const long long i = i0 + u * stride;
+            key4[u] = i < n ? d.key[i] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < SU; u++) {
+            const long long i = i0 + u * stride;
+            dst[u] = 0;
+            if (i < n) {
+                const int key = key4[u] >> 2, quad = key4[u] & 3;
+                const int4 qc = reinterpret_cast<const int4 *>(d.qcounts)[key];
+                const int qpre = (quad > 0 ? qc.x : 0) + (quad > 1 ? qc.y : 0) + (quad > 2 ? qc.z : 0);
+                dst[u] = d.box_start[key] + qpre + d.slot[i];
+            }
+        }
+        double x[SU], y[SU], m[SU], vx[SU], vy[SU];
+        int pid[SU];
+#pragma unroll
+        for (int u = 0; u < SU; u++) {
+            const long long i = i0 + u * stride;
+            if (i < n) {
+                x[u] = d.X[cur][i];
+                y[u] = d.Y[cur][i];
+                m[u] = d.M[cur][i];
+                vx[u] = d.VX[cur][i];
+                vy[u] = d.VY[cur][i];
+                pid[u] = d.PID[cur][i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < SU; u++) {
+            const long long i = i0 + u * stride;
+            if (i >= n) continue;
+            const int key = key4[u] >> 2, t = dst[u];
+            const int s = find_seg(d.boff_tab, d.nsys, key);
+            const SysDesc &sd = d.sys[s];
+            const int lb = (int)(key - sd.boff);
+            const int kx = lb / sd.G, ky = lb - kx * sd.G;
+            d.X[nxt][t] = x[u];
+            d.Y[nxt][t] = y[u];
+            d.VX[nxt][t] = vx[u];
+            d.VY[nxt][t] = vy[u];
+            d.M[nxt][t] = m[u];
+            d.PID[nxt][t] = pid[u];
+            const double *org = d.org + sd.ooff;  // box origins (k_bbox_finalize)
+            const float ox = f64_to_f32_rn(__dsub_rn(x[u], org[kx]));
+            const float oy = f64_to_f32_rn(__dsub_rn(y[u], org[sd.G + ky]));
+            const float mf = f64_to_f32_rn(m[u]);
+            d.P[t] = make_float4(ox, oy, mf, __int_as_float(t));
+            d.PD[2 * (long long)t] = make_float4(ox, ox, oy, oy);
+            d.PD[2 * (long long)t + 1] = make_float4(mf, mf, __int_as_float(t), __int_as_float((kx << 16) | ky));
+            d.skey[t] = key;
+        }
     }
 }
 
