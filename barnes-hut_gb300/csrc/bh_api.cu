@@ -734,7 +734,9 @@ extern "C" int bh_learned_pairs(bh_plan *p, double theta_hi, double theta_lo, in
     if (!(theta_hi > theta_lo) || !(theta_lo > 0.0) || item_stride < 1 || item_offset < 0 ||
         tpi < 1 || capacity < 0 || !feats || !targets || !counter)
         return fail(p, BH_ERR_INVALID, "bad learned_pairs arguments");
-    // a streaming plan without the learned correction builds no walk items in its step
+    // a plan without the learned correction builds neither the cell records' second moments nor
+    // (when streaming) the walk items in its step
+    if (!p->dev.learned) CK(p, launch_records(p->dev, true, (cudaStream_t)stream), "cell records");
     if (p->dev.stream && !p->dev.learned) CK(p, launch_walk_items(p->dev, (cudaStream_t)stream), "work items");
     CK(p, launch_learned_pairs(p->dev, theta_hi, theta_lo, max_level, item_offset, item_stride, tpi,
                                feats, targets, counter, capacity, (cudaStream_t)stream),

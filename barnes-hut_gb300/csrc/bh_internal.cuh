@@ -26,7 +26,7 @@
 //   * mom: FP64 moments (M, Sx, Sy, Sxx, Sxy, Syy about the cell origin) for
 //     every pyramid cell; rec / rec2: float records the force kernel reads
 //     (centre of mass relative to the cell origin, mass; normalised second
-//     moments about the centre of mass).
+//     moments about the centre of mass, formed only for the learned correction).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -308,6 +308,7 @@ cudaError_t launch_place(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_scan(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_items(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_walk_items(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_records(const DevPlan &d, bool second, cudaStream_t st);
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st);

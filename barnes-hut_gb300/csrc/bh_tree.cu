@@ -564,7 +564,7 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_pyramid_tail(DevPlan d, int l0
 
 // Float records: centre of mass relative to the cell origin and mass; second
 // moments about the centre of mass normalised by M s^2 (s = cell edge).
-__global__ void __launch_bounds__(TPB) k_records(DevPlan d) {
+__global__ void __launch_bounds__(TPB) k_records(DevPlan d, int second) {
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < d.C_total; c += stride) {
         const double *q = d.mom + 6 * c;
@@ -572,6 +572,7 @@ __global__ void __launch_bounds__(TPB) k_records(DevPlan d) {
         if (M > 0.0) {
             double cx = q[1] / M, cy = q[2] / M;
             d.rec[c] = make_float4(f64_to_f32_rn(cx), f64_to_f32_rn(cy), f64_to_f32_rn(M), 0.f);
+            if (!second) continue;
             int s = find_seg(d.coff_tab, d.nsys, c);
             const SysDesc &sd = d.sys[s];
             long long loc = c - sd.coff;
@@ -584,7 +585,7 @@ __global__ void __launch_bounds__(TPB) k_records(DevPlan d) {
                                     f64_to_f32_rn(iyy * nrm), 0.f);
         } else {
             d.rec[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-            d.rec2[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (second) d.rec2[c] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
     }
 }
@@ -652,7 +653,11 @@ cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st) {
         }
         k_pyramid_level<<<grid_for(d.lvl_cells[l], TPB, 152LL * 4), TPB, 0, st>>>(d, l);
     }
-    k_records<<<grid_for(d.C_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
+    // the normalised second moments feed only the learned correction
+    return launch_records(d, d.learned != 0, st);
+}
+cudaError_t launch_records(const DevPlan &d, bool second, cudaStream_t st) {
+    k_records<<<grid_for(d.C_total, TPB, 152LL * 8), TPB, 0, st>>>(d, second ? 1 : 0);
     return cudaGetLastError();
 }
 
