@@ -100,3 +100,23 @@ def test_dropin_checkpoint_resume(tmp_path):
     second.read_input_file(str(ckpt))
     second.run()
     _check_against_reference(z, *_final_positions(second))
+
+
+def test_cli_run_2d(tmp_path):
+    """bin/run_2d.py with the reference's arguments (run_2d.py:28-61): one warm-up run, one
+    timed run with --check; the Timer report names the reference's phases."""
+    import subprocess
+    import sys
+
+    from barneshut.gb300 import particle_io
+
+    z = np.load(f"{GOLDEN}/ref_c1_uniform10k.npz")
+    inp = tmp_path / "c1.bin"
+    particle_io.write_particles(str(inp), z["x0"], z["y0"], z["m"], z["vx0"], z["vy0"])
+    cmd = [sys.executable, f"{ROOT}/barnes-hut_gb300/bin/run_2d.py", str(inp), "1", "1",
+           _ini(tmp_path, 2, skip_timestep=True), "--check", "--sleep", "0"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "avg relative" in r.stdout and "warmup done" in r.stdout
+    for phase in ("grid_creation", "summarization", "evaluation", "end-to-end"):
+        assert phase in r.stdout, (phase, r.stdout[-2000:])
