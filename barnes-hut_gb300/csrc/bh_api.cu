@@ -257,7 +257,7 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_icnt = take(4 * (size_t)p->NG_total);
     p->o_ioff = take(4 * ((size_t)p->NG_total + 1));
     p->o_igrp = take(4 * ((size_t)p->NG_total + N / p->chunk + 1));
-    p->o_lfar = take(4 * (size_t)lf_total);
+    p->o_lfar = take(16 * (size_t)lf_total);
     p->o_lnear = take(16 * (size_t)ln_total);
     p->o_lcnt = take(p->stream ? 8 * (size_t)p->NG_total : 0);
     // target sets: a sparse set per group, each dense box, each quadrant of a quadrant box; a
@@ -343,7 +343,7 @@ static void fill_dev(bh_plan *p) {
     d.rec = (float4 *)(w + p->o_rec);
     d.rec2 = (float4 *)(w + p->o_rec2);
     d.org = (double *)(w + p->o_org);
-    d.lfar = (int *)(w + p->o_lfar);
+    d.lfar = (float4 *)(w + p->o_lfar);
     d.lnear = (int4 *)(w + p->o_lnear);
     d.lcnt = (int2 *)(w + p->o_lcnt);
     d.item_order = (int *)(w + p->o_iord);

@@ -10,9 +10,8 @@
 // a piece of its remainder, sitem_range; pulled from a device queue); the warps of a CTA share
 // nothing but the CTA's shared memory carve-up, so there is no CTA-wide barrier and a warp
 // waiting on memory leaves the SM to the other warps.  Per item:
-//   * far field: the group's far codes are decoded (level, cell -> record; centre of mass shifted
-//     into the group frame) into the warp's staging as packed (x, x, y, y) + (M, M) entries,
-//     WFAR at a time, and swept; each pass's plain FP32 sum enters the running total through a
+//   * far field: the group's far entries (centre of mass in the group frame, mass) are widened
+//     into the warp's staging as packed (x, x, y, y) + (M, M) entries, WFAR at a time, and swept; each pass's plain FP32 sum enters the running total through a
 //     Kahan-compensated addition (BH_PREC_FP32_KAHAN) or a plain one (BH_PREC_FP32);
 //   * near field: the near boxes' 32-byte packed records (x, x, y, y), (m, m, index, box) are
 //     copied box piece by box piece into the warp's staging by bulk asynchronous copies (TMA),
@@ -52,8 +51,7 @@ constexpr size_t FS_SMEM = (size_t)FW * W_BYTES;
 static_assert(W_FARM + WFAR * 8 <= W_NBOX, "far staging must fit in the near-source buffers");
 static_assert(2 * 32 * NR * sizeof(float) <= (size_t)W_NBOX, "slice partials alias the source buffers");
 static_assert(32 * NR >= STREAM_CHUNK, "a warp must cover every target of a work item");
-constexpr int FDB = 2;      // far entries per lane decoded together (loads in flight)
-static_assert(WFAR % (32 * FDB) == 0, "far staging passes are whole rounds of FDB entries per lane");
+static_assert(WFAR % 32 == 0, "far staging passes are whole lane rounds");
 static_assert((WSRC * 32) % 16 == 0 && W_BYTES % 128 == 0, "bulk-copy destinations must be 16-byte aligned");
 
 template <bool KAHAN, int MINB>
@@ -194,7 +192,7 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
             fsx2[k] = fsy2[k] = fcx2[k] = fcy2[k] = f2_pack(0.f, 0.f);
         }
         const int2 cnt = d.lcnt[g];
-        const int *lf = d.lfar + sd.lfoff + lg * sd.lfcap;
+        const float4 *lf = d.lfar + sd.lfoff + lg * sd.lfcap;
         const int4 *ln = d.lnear + sd.lnoff + lg * 2 * (sd.lncap + 1);
 
         // sweep nf staged far entries; the pass's plain FP32 sum enters the running total through
@@ -240,34 +238,14 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         // ---- far field: the group's accepted cells
         for (int f0 = 0; f0 < cnt.x; f0 += WFAR) {
             const int nf = min(WFAR, cnt.x - f0);
-            // FDB entries per lane at a time: their codes, then their records, then the staging
-            for (int u0 = 0; u0 < WFAR / 32; u0 += FDB) {
-                unsigned code[FDB];
-                float4 rr[FDB];
+            // the entries (centre of mass in the group frame, mass) widen into the packed staging
 #pragma unroll
-                for (int u = 0; u < FDB; u++) {
-                    const int k = lane + 32 * (u0 + u);
-                    code[u] = k < nf ? (unsigned)lf[f0 + k] : 0u;
-                }
-#pragma unroll
-                for (int u = 0; u < FDB; u++) {
-                    if (lane + 32 * (u0 + u) < nf) {
-                        const int l = (int)(code[u] >> 28);
-                        const int ci = (int)((code[u] >> 14) & 0x3FFFu), cj = (int)(code[u] & 0x3FFFu);
-                        rr[u] = d.rec[sd.coff + sd.lvoff[l] + (long long)ci * sd.lvg[l] + cj];
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < FDB; u++) {
-                    const int k = lane + 32 * (u0 + u);
-                    if (k < nf) {
-                        const int l = (int)(code[u] >> 28);
-                        const int ci = (int)((code[u] >> 14) & 0x3FFFu), cj = (int)(code[u] & 0x3FFFu);
-                        const float rx = __fadd_rn(__fmul_rn((float)((ci << l) - gx0), step_f), rr[u].x);
-                        const float ry = __fadd_rn(__fmul_rn((float)((cj << l) - gy0), step_f), rr[u].y);
-                        farxy[k] = make_float4(rx, rx, ry, ry);
-                        farm[k] = make_float2(rr[u].z, rr[u].z);
-                    }
+            for (int u = 0; u < WFAR / 32; u++) {
+                const int k = lane + 32 * u;
+                if (k < nf) {
+                    const float4 e = lf[f0 + k];
+                    farxy[k] = make_float4(e.x, e.x, e.y, e.y);
+                    farm[k] = make_float2(e.z, e.z);
                 }
             }
             __syncwarp();

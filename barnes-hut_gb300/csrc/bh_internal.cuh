@@ -41,7 +41,7 @@ constexpr int FORCE_R = 4;                                   // targets per thre
 constexpr int TARGET_CHUNK = FORCE_THREADS * FORCE_R;        // targets per work item
 constexpr int FRONTIER_CAP = 512;                            // traversal frontier per level
 constexpr int STREAM_CHUNK = 128;  // targets per work item of the list-streaming force kernel
-constexpr int LIST_MAX_G = 16384;  // far-list codes hold (level, column, row) in 4 + 14 + 14 bits
+constexpr int LIST_MAX_G = 16384;  // largest G of the list-streaming path (32-bit group indices)
 constexpr int ITEM_BUCKETS = 32;   // log2 cost buckets of the heaviest-first item order
 
 struct SysDesc {
@@ -103,13 +103,14 @@ struct DevPlan {
     double *mom;
     float4 *rec, *rec2;
     // interaction lists of every target group (list-streaming path), in fixed per-group slots
-    // (SysDesc lfcap far codes, lncap + 1 near descriptors), counts in lcnt (x far, y near):
-    //   far code: level << 28 | cell column << 14 | cell row (columns, rows < LIST_MAX_G);
+    // (SysDesc lfcap far entries, lncap + 1 near descriptors), counts in lcnt (x far, y near):
+    //   far entry: the accepted cell's centre of mass in the group frame and its mass, float4
+    //   (x, y, M, 0), formed with the opening test's own arithmetic;
     //   near descriptor: two int4 -- (first particle, exclusive prefix of the boxes' particle
     //   counts, shift of the box origin from the group origin as float bits x, y) and (box index
     //   in the system, mass, centre of mass in the group frame x, y as float bits); descriptor
     //   [count] carries the total in .y of its first int4
-    int *lfar;
+    float4 *lfar;
     int4 *lnear;
     int2 *lcnt;
     // list-streaming work items (per group: its sparse boxes together, then every dense box or

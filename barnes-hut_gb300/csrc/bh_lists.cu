@@ -12,8 +12,8 @@
 // entries in frontier order, so list order is deterministic and matches the walking force
 // kernel's; the test is the same FP32 arithmetic, so both paths accept the same cells.
 //
-// Output per group g of system s: far codes (level << 28 | cell index within the level) at
-// lfar[s.lfoff + lg * s.lfcap ..]; near descriptors -- (first particle, exclusive prefix of the
+// Output per group g of system s: far entries (the accepted cell's centre of mass in the group
+// frame, as the opening test computed it, and its mass) at lfar[s.lfoff + lg * s.lfcap ..]; near descriptors -- (first particle, exclusive prefix of the
 // boxes' particle counts, box-origin shift in the group frame) and (box index, mass, centre of
 // mass in the group frame) -- at lnear[s.lnoff + lg * 2 * (s.lncap + 1) ..] with the total in
 // descriptor [count]; lcnt[g] = (far count, near count).  The slots are
@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(LW * 32) k_lists(DevPlan d) {
         const int gx1 = min(sd.G, gx0 + TG), gy1 = min(sd.G, gy0 + TG);
         const float step_f = __double2float_rn(dy.step);
         const float W_f = __fmul_rn((float)TG, step_f);
-        int *far_out = d.lfar + sd.lfoff + lg * sd.lfcap;
+        float4 *far_out = d.lfar + sd.lfoff + lg * sd.lfcap;
         int4 *near_out = d.lnear + sd.lnoff + lg * 2 * (sd.lncap + 1);
         int nfar = 0, nnear = 0, nfr = 1, cur = 0;
         bool ovf = false;
@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(LW * 32) k_lists(DevPlan d) {
 #pragma unroll
                 for (int u = 0; u < LU; u++) {  // classify and append in frontier order
                     int kind = 0, ci = 0, cj = 0;
+                    float rx = 0.f, ry = 0.f;  // centre of mass in the group frame
                     if (loc[u] >= 0 && rr[u].z > 0.f) {
                         ci = loc[u] / gl;
                         cj = loc[u] - ci * gl;
@@ -88,8 +89,8 @@ __global__ void __launch_bounds__(LW * 32) k_lists(DevPlan d) {
                         const bool overlap = lo_x < gx1 && hi_x > gx0 && lo_y < gy1 && hi_y > gy0;
                         bool accept = false;
                         if (!overlap) {
-                            const float rx = __fadd_rn(__fmul_rn((float)(lo_x - gx0), step_f), rr[u].x);
-                            const float ry = __fadd_rn(__fmul_rn((float)(lo_y - gy0), step_f), rr[u].y);
+                            rx = __fadd_rn(__fmul_rn((float)(lo_x - gx0), step_f), rr[u].x);
+                            ry = __fadd_rn(__fmul_rn((float)(lo_y - gy0), step_f), rr[u].y);
                             const float dxo = fmaxf(0.f, fmaxf(-rx, __fsub_rn(rx, W_f)));
                             const float dyo = fmaxf(0.f, fmaxf(-ry, __fsub_rn(ry, W_f)));
                             const float d2 = __fadd_rn(__fmul_rn(dxo, dxo), __fmul_rn(dyo, dyo));
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(LW * 32) k_lists(DevPlan d) {
                     const int ntot = __shfl_sync(0xffffffffu, inc, 31);
                     if (kind == 1) {
                         const int pos = nfar + __popc(mf & lt_mask);
-                        if (pos < sd.lfcap) far_out[pos] = (int)(((unsigned)l << 28) | ((unsigned)ci << 14) | (unsigned)cj);
+                        if (pos < sd.lfcap) far_out[pos] = make_float4(rx, ry, rr[u].z, 0.f);
                     } else if (kind == 2) {
                         const int pos = nnear + __popc(mn & lt_mask);
                         if (pos < sd.lncap) fn[pos] = loc[u];
