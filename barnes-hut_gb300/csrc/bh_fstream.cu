@@ -11,8 +11,9 @@
 // nothing but the CTA's shared memory carve-up, so there is no CTA-wide barrier and a warp
 // waiting on memory leaves the SM to the other warps.  Per item:
 //   * far field: the group's far entries (centre of mass in the group frame, mass) are widened
-//     into the warp's staging as packed (x, x, y, y) + (M, M) entries, WFAR at a time, and swept; each pass's plain FP32 sum enters the running total through a
-//     Kahan-compensated addition (BH_PREC_FP32_KAHAN) or a plain one (BH_PREC_FP32);
+//     into the warp's staging as packed (x, x, y, y) + (M, M) entries, WFAR at a time, and
+//     swept; each pass's plain FP32 sum enters the running total through a Kahan-compensated
+//     addition (BH_PREC_FP32_KAHAN) or a plain one (BH_PREC_FP32);
 //   * near field: the near boxes' 32-byte packed records (x, x, y, y), (m, m, index, box) are
 //     copied box piece by box piece into the warp's staging by bulk asynchronous copies (TMA),
 //     WSRC sources per pass, double-buffered on two mbarriers so the copy of pass p + 1 overlaps
