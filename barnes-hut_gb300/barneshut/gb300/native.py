@@ -41,7 +41,8 @@ EXPORTS = (
     "bh_pair_counts", "bh_box_moments", "bh_grid_info", "bh_direct_sample", "bh_diagnostics",
     "bh_kernels_per_step", "bh_mlp_param_count", "bh_mlp_image_bytes", "bh_mlp_pack",
     "bh_mlp_forward", "bh_mlp_train_batch", "bh_mlp_adam", "bh_set_correction", "bh_learned_pairs",
-    "bh_direct_sum_noalloc", "bh_generate", "bh_graph_kernel_nodes",
+    "bh_direct_sum_noalloc", "bh_generate", "bh_graph_kernel_nodes", "bh_set_kernel_timing",
+    "bh_force_kernel_ms",
 )
 BH_GEN_UNIFORM, BH_GEN_GAUSS, BH_GEN_CLUSTER = 0, 1, 2
 BH_NOALLOC_MAX_TARGETS = 4096
@@ -118,6 +119,8 @@ def load_library(path=None):
     L.bh_diagnostics.argtypes = [vp, i, i, vp, vp]
     L.bh_kernels_per_step.argtypes = [vp, pi]
     L.bh_graph_kernel_nodes.argtypes = [vp, pi]
+    L.bh_set_kernel_timing.argtypes = [vp, i]
+    L.bh_force_kernel_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
     L.bh_set_correction.argtypes = [vp, vp, vp]
     L.bh_direct_sum_noalloc.argtypes = [vp, vp, vp, ll, vp, ll, d, d, vp, vp, vp]
     L.bh_learned_pairs.argtypes = [vp, d, d, i, ll, ll, i, vp, vp, vp, ll, vp]
@@ -323,6 +326,16 @@ class Plan:
         c = ctypes.c_int()
         self._check(self.L.bh_graph_kernel_nodes(self.h, ctypes.byref(c)))
         return c.value
+
+    def set_kernel_timing(self, enable=True):
+        """Record CUDA events around the force kernel of every later eager evaluate()."""
+        self._check(self.L.bh_set_kernel_timing(self.h, 1 if enable else 0))
+
+    def force_kernel_ms(self):
+        """Duration of the force kernel of the last timed evaluate() (waits for it)."""
+        v = ctypes.c_float()
+        self._check(self.L.bh_force_kernel_ms(self.h, ctypes.byref(v)))
+        return v.value
 
     def pair_counts(self):
         a, b = ctypes.c_longlong(), ctypes.c_longlong()

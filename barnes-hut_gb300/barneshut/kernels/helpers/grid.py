@@ -1,6 +1,6 @@
 """Host-side grid helpers with the semantics of
-python-bh/barneshut/kernels/helpers/grid.py:5-48 (used for grid sizing and by
-callers of the reference helpers; the device computes the per-step box)."""
+python-bh/barneshut/kernels/helpers/grid.py:5-26 (grid sizing and the square box; the
+device computes the per-step box)."""
 import math
 
 import numpy as np
@@ -31,22 +31,3 @@ def get_bounding_box(points):
     assert (max_x - min_x) - (max_y - min_y) < 0.00001
     return (min_x, min_y), (max_x, max_y)
 
-
-def get_neighbor_cells(point, grid_dim):
-    """Chebyshev-1 neighbours of box (x, y) inside the grid, x-major order."""
-    x, y = point
-    cells = []
-    for i in range(max(0, x - 1), min(grid_dim - 1, x + 1) + 1):
-        for j in range(max(0, y - 1), min(grid_dim - 1, y + 1) + 1):
-            if (i, j) != (x, y):
-                cells.append((i, j))
-    return cells
-
-
-def remove_bottom_left_neighbors(point, neighbors):
-    """Drop the four neighbours that precede (x, y) in x-major order's mutual
-    update: (x-1, y-1), (x-1, y), (x, y-1), (x+1, y-1)."""
-    x, y = point
-    drop = {(x - 1, y - 1), (x - 1, y), (x, y - 1), (x + 1, y - 1)}
-    neighbors[:] = [c for c in neighbors if c not in drop]
-    return neighbors

@@ -39,11 +39,15 @@ struct bh_plan {
     int quad_min = BH_STREAM_QUAD_MIN;
     void *ws = nullptr;
     int device = -1;
+    int nsm = 1;  // streaming multiprocessors of `device`
     DevPlan dev;
     bool has_tree = false;
     bool acc_stale = true;  // next bh_evaluate overwrites instead of accumulating
     // graph cache
     cudaGraphExec_t gexec = nullptr;
+    cudaEvent_t tev[2] = {nullptr, nullptr};  // bh_set_kernel_timing: around the force kernel
+    bool timing = false;
+    bool tev_recorded = false;
     int gkernels = -1;  // kernel nodes of the captured step graph
     int gsteps = 0;
     cudaStream_t gstream = nullptr;
@@ -189,12 +193,15 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->quad_min = pr.quad_min > 0 ? pr.quad_min : (pr.quad_min == 0 ? BH_STREAM_QUAD_MIN : 0);
     long long lf_total = 0, ln_total = 0;
     if (p->stream) {
-        // a level's accepted cells are a subset of its frontier (at most FRONTIER_CAP cells), and
-        // the near boxes a subset of the leaf level's frontier
+        // a level's accepted cells are a subset of its frontier, and the near boxes a subset of
+        // the leaf level's frontier; a frontier holds the children of the cells rejected one level
+        // up, at most 4 (TG/2 + 2/theta + 2)^2 (the bound checked against FRONTIER_CAP above)
         for (int s = 0; s < nsys; s++) {
             SysDesc &d = p->sys[s];
+            const double fb = 4.0 * std::pow(d.TG / 2.0 + 2.0 / pr.theta + 2.0, 2.0);
+            const long long lvcap = std::min<long long>(FRONTIER_CAP, (long long)std::ceil(fb));
             long long cap = 0;
-            for (int l = 0; l < d.L; l++) cap += std::min<long long>(FRONTIER_CAP, (long long)d.lvg[l] * d.lvg[l]);
+            for (int l = 0; l < d.L; l++) cap += std::min<long long>(lvcap, (long long)d.lvg[l] * d.lvg[l]);
             d.lfcap = (int)cap;
             // a near leaf is rejected for the group rectangle, so its centre of mass lies within
             // 1/theta box edges of it: at most floor(1/theta) + 1 boxes away (one more for rounding)
@@ -285,6 +292,8 @@ extern "C" int bh_plan_destroy(bh_plan *p) {
     if (!p) return BH_ERR_INVALID;
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     if (p->gstream) cudaStreamDestroy(p->gstream);
+    for (cudaEvent_t e : p->tev)
+        if (e) cudaEventDestroy(e);
     delete p;
     return BH_OK;
 }
@@ -355,6 +364,7 @@ static void fill_dev(bh_plan *p) {
     d.dense_min = p->dense_min;
     d.quad_min = p->quad_min;
     d.item_bucket = (int *)(w + p->o_ibkt);
+    d.nsm = p->nsm;
     d.stream = p->stream ? 1 : 0;
     d.chunk = p->chunk;
     const bh_params &pr = p->params;
@@ -379,6 +389,8 @@ extern "C" int bh_bind(bh_plan *p, void *workspace, size_t bytes, void *stream) 
     if (((uintptr_t)workspace) & 255) return fail(p, BH_ERR_WORKSPACE, "workspace not 256-byte aligned");
     cudaStream_t st = (cudaStream_t)stream;
     CK(p, cudaGetDevice(&p->device), "cudaGetDevice");
+    CK(p, cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, p->device), "SM count");
+    if (p->nsm < 1) p->nsm = 1;
     CK(p, force_init(), "force kernel attributes");
     CK(p, learned_init(), "learned kernel attributes");
     p->ws = workspace;
@@ -480,7 +492,9 @@ extern "C" int bh_evaluate(bh_plan *p, void *stream) {
     if (r) return r;
     if (!p->has_tree) return fail(p, BH_ERR_INVALID, "evaluate before create_tree");
     if (p->dev.learned && !p->mlp_img) return fail(p, BH_ERR_INVALID, "BH_FLAG_LEARNED without bh_set_correction");
-    CK(p, launch_force(p->dev, false, !p->acc_stale, (cudaStream_t)stream), "evaluate");
+    CK(p, launch_force(p->dev, false, !p->acc_stale, (cudaStream_t)stream, p->timing ? p->tev : nullptr),
+       "evaluate");
+    if (p->timing) p->tev_recorded = true;
     if (p->dev.learned)
         CK(p, launch_learned_correct(p->dev, p->params.correction_theta, p->mlp_img, p->mlp_params,
                                      false, (cudaStream_t)stream), "learned correction");
@@ -569,6 +583,24 @@ extern "C" int bh_step_graph(bh_plan *p, int nsteps, void *stream) {
     CK(p, cudaGraphLaunch(p->gexec, st), "graph launch");
     p->has_tree = true;
     p->acc_stale = true;
+    return BH_OK;
+}
+
+extern "C" int bh_set_kernel_timing(bh_plan *p, int enable) {
+    if (!p) return BH_ERR_INVALID;
+    if (enable)
+        for (cudaEvent_t &e : p->tev)
+            if (!e) CK(p, cudaEventCreate(&e), "timing event");
+    p->timing = enable != 0;
+    p->tev_recorded = false;
+    return BH_OK;
+}
+
+extern "C" int bh_force_kernel_ms(bh_plan *p, float *ms) {
+    if (!p || !ms) return BH_ERR_INVALID;
+    if (!p->tev_recorded) return fail(p, BH_ERR_INVALID, "no timed bh_evaluate since bh_set_kernel_timing");
+    CK(p, cudaEventSynchronize(p->tev[1]), "timing sync");
+    CK(p, cudaEventElapsedTime(ms, p->tev[0], p->tev[1]), "elapsed time");
     return BH_OK;
 }
 

@@ -624,7 +624,7 @@ static cudaError_t launch_force_t(const DevPlan &d, bool tick, bool accumulate, 
     auto k = k_force<R, NR, KAHAN, TEST, EXACT, MINB>;
     size_t sm = force_smem<R>();
     long long items_max = d.NG_total + d.n_total / d.chunk + 1;
-    long long grid = 152LL * MINB;
+    long long grid = (long long)d.nsm * MINB;
     if (grid > items_max) grid = items_max;
     if (grid < 1) grid = 1;
     cudaError_t e = cudaMemsetAsync(&d.glob->item_next, 0, sizeof(unsigned), st);
@@ -657,29 +657,34 @@ cudaError_t force_init() {
     return init_force_t<float, FORCE_R, false, false, false>();
 }
 
-cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
+cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st,
+                         const cudaEvent_t *ev) {
     if (d.n_total == 0) return cudaSuccess;
     if (d.stream) {  // prebuilt interaction lists, streamed (bh_lists.cu, bh_fstream.cu)
         cudaError_t e = launch_lists(d, st);
         if (e != cudaSuccess) return e;
-        return launch_fstream(d, tick, accumulate, st);
+        return launch_fstream(d, tick, accumulate, st, ev);
     }
+    cudaError_t e = cudaSuccess;
+    if (ev && (e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
     const bool test = d.cutoff > 0.0 || d.eps2 == 0.0;
     const bool exact = d.cutoff > 0.0;
     if (d.prec == 2) {
-        if (test) return launch_force_t<double, FORCE_R, false, true, false>(d, tick, accumulate, st);
-        return launch_force_t<double, FORCE_R, false, false, false>(d, tick, accumulate, st);
+        if (test) e = launch_force_t<double, FORCE_R, false, true, false>(d, tick, accumulate, st);
+        else e = launch_force_t<double, FORCE_R, false, false, false>(d, tick, accumulate, st);
+    } else if (d.prec == 1) {
+        if (exact) e = launch_force_t<float, FORCE_R, true, true, true>(d, tick, accumulate, st);
+        else if (test) e = launch_force_t<float, FORCE_R, true, true, false>(d, tick, accumulate, st);
+        else if (d.tune == 1) e = launch_force_t<float, FORCE_R, true, false, false, 6>(d, tick, accumulate, st);
+        else e = launch_force_t<float, FORCE_R, true, false, false>(d, tick, accumulate, st);
+    } else {
+        if (exact) e = launch_force_t<float, FORCE_R, false, true, true>(d, tick, accumulate, st);
+        else if (test) e = launch_force_t<float, FORCE_R, false, true, false>(d, tick, accumulate, st);
+        else if (d.tune == 1) e = launch_force_t<float, FORCE_R, false, false, false, 6>(d, tick, accumulate, st);
+        else e = launch_force_t<float, FORCE_R, false, false, false>(d, tick, accumulate, st);
     }
-    if (d.prec == 1) {
-        if (exact) return launch_force_t<float, FORCE_R, true, true, true>(d, tick, accumulate, st);
-        if (test) return launch_force_t<float, FORCE_R, true, true, false>(d, tick, accumulate, st);
-        if (d.tune == 1) return launch_force_t<float, FORCE_R, true, false, false, 6>(d, tick, accumulate, st);
-        return launch_force_t<float, FORCE_R, true, false, false>(d, tick, accumulate, st);
-    }
-    if (exact) return launch_force_t<float, FORCE_R, false, true, true>(d, tick, accumulate, st);
-    if (test) return launch_force_t<float, FORCE_R, false, true, false>(d, tick, accumulate, st);
-    if (d.tune == 1) return launch_force_t<float, FORCE_R, false, false, false, 6>(d, tick, accumulate, st);
-    return launch_force_t<float, FORCE_R, false, false, false>(d, tick, accumulate, st);
+    if (e != cudaSuccess) return e;
+    return ev ? cudaEventRecord(ev[1], st) : cudaSuccess;
 }
 
 }  // namespace bh

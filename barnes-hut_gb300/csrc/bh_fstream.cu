@@ -465,16 +465,19 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
 }
 
 template <bool KAHAN, int MINB>
-static cudaError_t launch_fstream_t(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
+static cudaError_t launch_fstream_t(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st,
+                                    const cudaEvent_t *ev) {
     long long items_max = d.NG_total + d.n_total / d.dense_min +
                           (d.quad_min > 0 ? 4 * (d.n_total / d.quad_min) : 0) + d.n_total / STREAM_ITEM_DIV + 1;
-    long long grid = 152LL * MINB;
+    long long grid = (long long)d.nsm * MINB;
     if (grid * FW > items_max) grid = (items_max + FW - 1) / FW;
     if (grid < 1) grid = 1;
     cudaError_t e = cudaMemsetAsync(&d.glob->item_next, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
+    if (ev && (e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
     k_fstream<KAHAN, MINB><<<(unsigned)grid, FW * 32, FS_SMEM, st>>>(d, tick ? 1 : 0, accumulate ? 1 : 0);
-    return cudaGetLastError();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return ev ? cudaEventRecord(ev[1], st) : cudaSuccess;
 }
 
 template <bool KAHAN, int MINB>
@@ -491,13 +494,14 @@ cudaError_t fstream_init() {
     return init_fstream_t<false, 6>();
 }
 
-cudaError_t launch_fstream(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st) {
+cudaError_t launch_fstream(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st,
+                           const cudaEvent_t *ev) {
     if (d.n_total == 0) return cudaSuccess;
     if (d.prec == 1)
-        return d.tune == 1 ? launch_fstream_t<true, 6>(d, tick, accumulate, st)
-                           : launch_fstream_t<true, 8>(d, tick, accumulate, st);
-    return d.tune == 1 ? launch_fstream_t<false, 6>(d, tick, accumulate, st)
-                       : launch_fstream_t<false, 8>(d, tick, accumulate, st);
+        return d.tune == 1 ? launch_fstream_t<true, 6>(d, tick, accumulate, st, ev)
+                           : launch_fstream_t<true, 8>(d, tick, accumulate, st, ev);
+    return d.tune == 1 ? launch_fstream_t<false, 6>(d, tick, accumulate, st, ev)
+                       : launch_fstream_t<false, 8>(d, tick, accumulate, st, ev);
 }
 
 }  // namespace bh

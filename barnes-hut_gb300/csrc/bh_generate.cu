@@ -113,7 +113,8 @@ extern "C" int bh_generate(int distribution, long long n, unsigned long long see
     if (n == 0) return BH_OK;
     if (!x || !y || !m || !vx || !vy) return bh::bh_set_thread_error(BH_ERR_INVALID, "bh_generate: null array");
     long long blocks = (n + 255) / 256;
-    if (blocks > 152LL * 16) blocks = 152LL * 16;
+    const long long cap = bh::device_sm_count() * 16LL;
+    if (blocks > cap) blocks = cap;
     bh::k_generate<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(distribution, n, seed, x, y, m, vx, vy);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return bh::bh_set_thread_error(BH_ERR_CUDA, cudaGetErrorString(e));

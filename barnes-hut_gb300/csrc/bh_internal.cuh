@@ -123,6 +123,8 @@ struct DevPlan {
                    // work items and near lists (0: none)
     int *item_order;  // list-streaming work items, heaviest cost bucket first
     int *item_bucket;  // ITEM_BUCKETS counts + ITEM_BUCKETS cursors
+    int nsm;     // streaming multiprocessors of the plan's device (queried at bh_bind): sizes the
+                 // persistent and grid-stride launches
     int stream;  // 1: lists are built by k_lists and streamed by k_fstream
     int chunk;   // targets per work item (TARGET_CHUNK, or STREAM_CHUNK when stream)
     // parameters
@@ -248,6 +250,16 @@ __device__ __forceinline__ int box_item_kind(int nb, int dense_min, int quad_min
     return nb >= dense_min ? 1 : 0;
 }
 
+// Streaming multiprocessors of the current device (the runtime caches the attribute); grid-stride
+// launches that have no plan size their grids with it.
+inline int device_sm_count() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+        return 1;
+    return n;
+}
+
 // Origin of leaf box k along one axis: mn + k * step, FP64, no contraction.
 __device__ __forceinline__ double box_origin(double mn, int k, double step) {
     return __dadd_rn(mn, __dmul_rn((double)k, step));
@@ -312,9 +324,12 @@ cudaError_t launch_walk_items(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_records(const DevPlan &d, bool second, cudaStream_t st);
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st);
-cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st);
+// ev (optional): two events recorded on st right before and after the force kernel proper
+cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st,
+                         const cudaEvent_t *ev = nullptr);
 cudaError_t launch_lists(const DevPlan &d, cudaStream_t st);
-cudaError_t launch_fstream(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st);
+cudaError_t launch_fstream(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st,
+                           const cudaEvent_t *ev = nullptr);
 cudaError_t fstream_init();
 cudaError_t force_init();
 cudaError_t launch_tick(const DevPlan &d, cudaStream_t st);

@@ -461,7 +461,7 @@ cudaError_t launch_learned_correct(const DevPlan &d, double theta_lo, const uint
     cudaError_t e = cudaMemsetAsync(&d.glob->item_next2, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     long long items_max = d.NG_total + d.n_total / d.chunk + 1;
-    long long grid = 152LL * 2;
+    long long grid = (long long)d.nsm * 2;
     if (grid > items_max) grid = items_max;
     k_learned_correct<<<(unsigned)grid, LT, LSmem::TOTAL + 1024, st>>>(
         d, (float)(theta_lo * theta_lo), img, params, tick ? 1 : 0);
@@ -473,7 +473,7 @@ cudaError_t launch_learned_pairs(const DevPlan &d, double theta_hi, double theta
                                  float *feats, float *targets, unsigned *counter, long long capacity,
                                  cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_learned_pairs<<<152 * 4, LT, PSmem::TOTAL + 16, st>>>(
+    k_learned_pairs<<<d.nsm * 4, LT, PSmem::TOTAL + 16, st>>>(
         d, (float)(theta_hi * theta_hi), (float)(theta_lo * theta_lo), max_level, item_offset,
         item_stride, tpi, feats, targets, counter, capacity);
     return cudaGetLastError();

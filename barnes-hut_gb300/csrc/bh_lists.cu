@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(256) k_item_order(DevPlan d) {
 
 cudaError_t launch_lists(const DevPlan &d, cudaStream_t st) {
     if (d.NG_total == 0) return cudaSuccess;
-    long long grid = 152LL * 8;  // 64 registers x 128 threads: 8 CTAs per SM
+    long long grid = (long long)d.nsm * 8;  // 64 registers x 128 threads: 8 CTAs per SM
     if (grid * LW > d.NG_total) grid = (d.NG_total + LW - 1) / LW;
     k_lists<<<(unsigned)grid, LW * 32, 0, st>>>(d);
     cudaError_t e = cudaGetLastError();
@@ -270,7 +270,7 @@ cudaError_t launch_lists(const DevPlan &d, cudaStream_t st) {
     long long items_max = d.NG_total + d.n_total / d.dense_min +
                           (d.quad_min > 0 ? 4 * (d.n_total / d.quad_min) : 0) + d.n_total / STREAM_ITEM_DIV + 1;  // >= items
     long long ig = (items_max + 255) / 256;
-    if (ig > 152LL * 8) ig = 152LL * 8;
+    if (ig > (long long)d.nsm * 8) ig = (long long)d.nsm * 8;
     k_item_hist<<<(unsigned)ig, 256, 0, st>>>(d);
     k_item_order<<<(unsigned)ig, 256, 0, st>>>(d);
     return cudaGetLastError();

@@ -5,10 +5,10 @@ namespace bh {
 
 constexpr int MT = 256;
 
-static inline unsigned grid_of(long long n, int tpb) {
+static inline unsigned grid_of(long long n, int tpb, int nsm) {
     long long b = (n + tpb - 1) / tpb;
     if (b < 1) b = 1;
-    if (b > 152LL * 16) b = 152LL * 16;
+    if (b > nsm * 16LL) b = nsm * 16LL;
     return (unsigned)b;
 }
 
@@ -183,34 +183,34 @@ __global__ void k_box_com(DevPlan d, int sys, double *out) {
 }
 
 cudaError_t launch_box_com(const DevPlan &d, int sys, double *out, cudaStream_t st) {
-    k_box_com<<<152 * 4, MT, 0, st>>>(d, sys, out);
+    k_box_com<<<d.nsm * 4, MT, 0, st>>>(d, sys, out);
     return cudaGetLastError();
 }
 
 cudaError_t launch_load(const DevPlan &d, const double *x, const double *y, const double *m,
                         const double *vx, const double *vy, long long rs, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_load<<<grid_of(d.n_total, MT), MT, 0, st>>>(d, x, y, m, vx, vy, rs);
+    k_load<<<grid_of(d.n_total, MT, d.nsm), MT, 0, st>>>(d, x, y, m, vx, vy, rs);
     return cudaGetLastError();
 }
 
 cudaError_t launch_store(const DevPlan &d, int has_tree, double *rec, double *x, double *y,
                          double *vx, double *vy, double *ax, double *ay, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_store<<<grid_of(d.n_total, MT), MT, 0, st>>>(d, rec, x, y, vx, vy, ax, ay, has_tree);
+    k_store<<<grid_of(d.n_total, MT, d.nsm), MT, 0, st>>>(d, rec, x, y, vx, vy, ax, ay, has_tree);
     return cudaGetLastError();
 }
 
 cudaError_t launch_tick(const DevPlan &d, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_tick<<<grid_of(d.n_total, MT), MT, 0, st>>>(d);
+    k_tick<<<grid_of(d.n_total, MT, d.nsm), MT, 0, st>>>(d);
     return cudaGetLastError();
 }
 
 cudaError_t launch_direct(const DevPlan &d, int sys, const long long *targets, long long nt,
                           double *ax, double *ay, cudaStream_t st) {
     if (d.n_total == 0 || nt == 0) return cudaSuccess;
-    k_inverse_pid<<<grid_of(d.n_total, MT), MT, 0, st>>>(d);
+    k_inverse_pid<<<grid_of(d.n_total, MT, d.nsm), MT, 0, st>>>(d);
     for (long long t0 = 0; t0 < nt; t0 += (1LL << 30)) {
         long long c = nt - t0 < (1LL << 30) ? nt - t0 : (1LL << 30);
         k_direct<<<(unsigned)c, MT, 0, st>>>(d, sys, targets + t0, ax + t0, ay + t0);
@@ -221,7 +221,7 @@ cudaError_t launch_direct(const DevPlan &d, int sys, const long long *targets, l
 cudaError_t launch_diag(const DevPlan &d, int sys, int want_pot, double *out, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(out, 0, 4 * sizeof(double), st);
     if (e != cudaSuccess) return e;
-    k_diag<<<152 * 2, MT, 0, st>>>(d, sys, want_pot, out);
+    k_diag<<<d.nsm * 2, MT, 0, st>>>(d, sys, want_pot, out);
     return cudaGetLastError();
 }
 

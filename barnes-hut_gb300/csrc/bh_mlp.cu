@@ -402,7 +402,8 @@ cudaError_t mlp_infer(const float *feats, int fs, long long P, const uint8_t *im
                       const float *params, float *out, unsigned *err, cudaStream_t st) {
     if (P <= 0) return cudaSuccess;
     long long tiles = (P + MT - 1) / MT;
-    int grid = (int)(tiles < 152 * 4 ? tiles : 152 * 4);
+    const long long cap = device_sm_count() * 4LL;
+    int grid = (int)(tiles < cap ? tiles : cap);
     k_mlp_infer<<<grid, MT, MlpSmemInfer::TOTAL + 1024, st>>>(feats, fs, P, img, params, out, err);
     return cudaGetLastError();
 }
@@ -412,7 +413,8 @@ cudaError_t mlp_train(const float *feats, int fs, const float *targets, long lon
                       unsigned *err, cudaStream_t st) {
     if (P <= 0) return cudaSuccess;
     long long tiles = (P + MT - 1) / MT;
-    int grid = (int)(tiles < 152 ? tiles : 152);
+    const long long cap = device_sm_count();
+    int grid = (int)(tiles < cap ? tiles : cap);
     k_mlp_train<<<grid, MT, MlpSmemTrain::TOTAL + 1024, st>>>(feats, fs, targets, P, img, params,
                                                             grad, loss, err);
     return cudaGetLastError();

@@ -7,6 +7,8 @@
 // device arrays (positions and masses in any order, target indices, outputs) and keeps its
 // scratch -- the per-chunk partial sums of every target -- in the file-scope array below,
 // which every GPU that loads the library holds until the process exits.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "../../include/bh_gb300.h"
@@ -80,24 +82,74 @@ __global__ void k_direct_finish(const long long *targets, long long nt, long lon
     ay[k] = gconst * b;
 }
 
-// Device address of the scratch array, looked up once per device with that device current.
-constexpr int NA_MAX_DEVICES = 64;
+// Device address of the scratch array.  The address belongs to one CUDA context (the module is
+// loaded once per context), so it is looked up once per context, with that context current, and
+// cached under the context's ID -- unique for the life of the process, so a context created after
+// cudaDeviceReset, or a framework's own driver-API context on the same device, never finds an
+// address that belongs to another context.
+constexpr int NA_CACHE = 64;
 static std::mutex g_na_mutex;
-static double *g_na_ptr[NA_MAX_DEVICES];
+static unsigned long long g_na_ctx[NA_CACHE];
+static double *g_na_ptr[NA_CACHE];
+static int g_na_next;
+
+// The two driver calls are resolved through the runtime, so the library needs no link against
+// the driver library (it loads on machines without a GPU driver, for its host-side checks).
+typedef CUresult (*ctx_get_current_fn)(CUcontext *);
+typedef CUresult (*ctx_get_id_fn)(CUcontext, unsigned long long *);
+static ctx_get_current_fn g_ctx_get_current;
+static ctx_get_id_fn g_ctx_get_id;
+
+static cudaError_t noalloc_driver_calls() {
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (g_ctx_get_current && g_ctx_get_id) return cudaSuccess;
+    void *a = nullptr, *b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa);
+    if (e != cudaSuccess) return e;
+    e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb);
+    if (e != cudaSuccess) return e;
+    if (qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b)
+        return cudaErrorSymbolNotFound;
+    g_ctx_get_current = (ctx_get_current_fn)a;
+    g_ctx_get_id = (ctx_get_id_fn)b;
+    return cudaSuccess;
+}
 
 static cudaError_t noalloc_scratch(double **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= NA_MAX_DEVICES) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_ptr[dev]) {
-        double *p = nullptr;
-        e = cudaGetSymbolAddress((void **)&p, g_noalloc_partials);
+    cudaError_t de = noalloc_driver_calls();
+    if (de != cudaSuccess) return de;
+    ctx_get_current_fn cuCtxGetCurrent = g_ctx_get_current;
+    ctx_get_id_fn cuCtxGetId = g_ctx_get_id;
+    CUcontext ctx = nullptr;
+    CUresult r = cuCtxGetCurrent(&ctx);
+    if (r == CUDA_ERROR_NOT_INITIALIZED)
+        ctx = nullptr;
+    else if (r != CUDA_SUCCESS)
+        return cudaErrorDeviceUninitialized;
+    double *p = nullptr;
+    if (!ctx) {  // no context current yet: the runtime's lookup makes the primary context current
+        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_partials);
         if (e != cudaSuccess) return e;
-        g_na_ptr[dev] = p;
+        if (cuCtxGetCurrent(&ctx) != CUDA_SUCCESS || !ctx) return cudaErrorDeviceUninitialized;
     }
-    *out = g_na_ptr[dev];
+    unsigned long long id = 0;
+    if (cuCtxGetId(ctx, &id) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    for (int i = 0; i < NA_CACHE; i++)
+        if (g_na_ptr[i] && g_na_ctx[i] == id) {
+            *out = g_na_ptr[i];
+            return cudaSuccess;
+        }
+    if (!p) {
+        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_partials);
+        if (e != cudaSuccess) return e;
+    }
+    const int slot = g_na_next;  // oldest entry out first once the table is full
+    g_na_next = (g_na_next + 1) % NA_CACHE;
+    g_na_ctx[slot] = id;
+    g_na_ptr[slot] = p;
+    *out = p;
     return cudaSuccess;
 }
 

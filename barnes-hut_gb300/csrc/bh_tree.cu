@@ -13,7 +13,7 @@ namespace bh {
 constexpr int TPB = 256;
 constexpr int SCAN_TILE = 4096;  // counts per scan tile (256 threads x 16)
 
-static inline unsigned grid_for(long long n, int tpb, long long cap = 152LL * 16) {
+static inline unsigned grid_for(long long n, int tpb, long long cap) {
     long long b = (n + tpb - 1) / tpb;
     if (b < 1) b = 1;
     if (b > cap) b = cap;
@@ -593,18 +593,18 @@ __global__ void __launch_bounds__(TPB) k_records(DevPlan d, int second) {
 // ------------------------------------------------------------------ launches
 cudaError_t launch_prologue(const DevPlan &d, cudaStream_t st) {
     long long n = d.B_total > d.nsys ? d.B_total : d.nsys;
-    k_prologue<<<grid_for(n, TPB), TPB, 0, st>>>(d);
+    k_prologue<<<grid_for(n, TPB, d.nsm * 16LL), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
 cudaError_t launch_bbox(const DevPlan &d, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_bbox<<<grid_for(d.n_total, TPB * 16, 152LL * 8), TPB, 0, st>>>(d);
+    k_bbox<<<grid_for(d.n_total, TPB * 16, d.nsm * 8LL), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
 cudaError_t launch_place(const DevPlan &d, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
     k_bbox_finalize<<<d.nsys, 128, 0, st>>>(d);
-    k_place<<<grid_for(d.n_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
+    k_place<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
 cudaError_t launch_scan(const DevPlan &d, cudaStream_t st) {
@@ -612,7 +612,7 @@ cudaError_t launch_scan(const DevPlan &d, cudaStream_t st) {
 }
 // Work items of the walk kernel and of the learned correction (group, target chunk).
 cudaError_t launch_walk_items(const DevPlan &d, cudaStream_t st) {
-    unsigned g = grid_for(d.NG_total, TPB, 152LL * 8);
+    unsigned g = grid_for(d.NG_total, TPB, d.nsm * 8LL);
     k_group_items<<<g, TPB, 0, st>>>(d);
     cudaError_t e = scan_excl(d.item_cnt, d.item_off, d.NG_total, d.tile_sums, st);
     if (e != cudaSuccess) return e;
@@ -629,7 +629,7 @@ cudaError_t launch_items(const DevPlan &d, cudaStream_t st) {
         if (e != cudaSuccess) return e;
     }
     if (d.stream) {
-        unsigned g = grid_for(d.NG_total, TPB, 152LL * 8);
+        unsigned g = grid_for(d.NG_total, TPB, d.nsm * 8LL);
         k_sitem_count<<<g, TPB, 0, st>>>(d);
         e = scan_excl(d.sitem_cnt, d.sitem_off, d.NG_total, d.tile_sums, st);
         if (e != cudaSuccess) return e;
@@ -639,11 +639,11 @@ cudaError_t launch_items(const DevPlan &d, cudaStream_t st) {
 }
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_scatter<<<grid_for(d.n_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
+    k_scatter<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st) {
-    if (d.n_total > 0) k_leaf_moments<<<grid_for(d.n_total, TPB, 152LL * 8), TPB, 0, st>>>(d);
+    if (d.n_total > 0) k_leaf_moments<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     for (int l = 1; l < d.Lmax; l++) {
         // the level's cell count over all systems is known on the host: one thread per cell
         // while the level is large, then one CTA for all the remaining (small) levels
@@ -651,13 +651,13 @@ cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st) {
             k_pyramid_tail<<<1, TAIL_THREADS, 0, st>>>(d, l);
             break;
         }
-        k_pyramid_level<<<grid_for(d.lvl_cells[l], TPB, 152LL * 4), TPB, 0, st>>>(d, l);
+        k_pyramid_level<<<grid_for(d.lvl_cells[l], TPB, d.nsm * 4LL), TPB, 0, st>>>(d, l);
     }
     // the normalised second moments feed only the learned correction
     return launch_records(d, d.learned != 0, st);
 }
 cudaError_t launch_records(const DevPlan &d, bool second, cudaStream_t st) {
-    k_records<<<grid_for(d.C_total, TPB, 152LL * 8), TPB, 0, st>>>(d, second ? 1 : 0);
+    k_records<<<grid_for(d.C_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d, second ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -169,19 +169,93 @@ def fp32_peak_tflops(torch, dev):
         torch.backends.cuda.matmul.allow_tf32 = prev
 
 
-def cpu_baseline(args, x, y, m, G):
+def cpu_baseline(x, y, m, G, full_limit_s=240.0):
+    """The reference CPU algorithm -- the oracle's restatement of sequential.py and
+    com_concat_dedup (evaluation.py:73-109), FP64, OpenMP over target boxes on every host core --
+    on the bench's own input.  First a bounded sample: the O(N) phases (bounding box, keys, the
+    structured sort, COMs) in full and the evaluation of 1,024 non-empty boxes at a fixed stride,
+    scaled to all boxes to estimate a step.  Then, when that estimate is within full_limit_s, one
+    full step (every non-empty box evaluated), whose measured time is the reported baseline."""
     from oracle import oracle
 
     threads = os.cpu_count() or 1
-    r = oracle.reference_sample_time(x, y, m, G, args.ref_sample_boxes, threads)
-    return {"value": len(x) / r["step_s"], "unit": "particle-steps/s", "cores": threads,
-            "kind": "port",
-            "sample": (f"reference CPU algorithm (oracle/bh_oracle.c restatement of sequential.py + "
-                       f"com_concat_dedup, FP64, OpenMP) on the same N={len(x)} input: O(N) phases "
-                       f"in full ({r['setup_s']:.2f} s) + evaluation of {r['sampled']} of "
-                       f"{r['nonempty']} non-empty boxes ({r['sample_s']:.2f} s), extrapolated to "
-                       f"{r['step_s']:.1f} s/step"),
-            "step_seconds": r["step_s"]}
+    est = oracle.reference_sample_time(x, y, m, G, 1024, threads)
+    out = {"unit": "particle-steps/s", "cores": threads, "kind": "port",
+           "estimate_s": est["step_s"], "estimate_sample": f"{est['sampled']} of {est['nonempty']} boxes"}
+    if est["step_s"] <= full_limit_s:
+        full = oracle.reference_sample_time(x, y, m, G, 1 << 40, threads)
+        step_s = full["setup_s"] + full["sample_s"]
+        out.update(value=len(x) / step_s, step_seconds=step_s, measured="full step",
+                   sample=(f"one full reference CPU step measured on the same N={len(x)} input: O(N) "
+                           f"phases {full['setup_s']:.2f} s + evaluation of all {full['nonempty']} "
+                           f"non-empty boxes {full['sample_s']:.1f} s (the sampled estimate, "
+                           f"{est['sampled']} boxes scaled up, was {est['step_s']:.1f} s)"))
+    else:
+        out.update(value=len(x) / est["step_s"], step_seconds=est["step_s"], measured="estimate",
+                   sample=(f"reference CPU step estimated on the same N={len(x)} input: O(N) phases "
+                           f"in full ({est['setup_s']:.2f} s) + evaluation of {est['sampled']} of "
+                           f"{est['nonempty']} non-empty boxes ({est['sample_s']:.2f} s), scaled to "
+                           f"{est['step_s']:.1f} s/step (a full step exceeds {full_limit_s:.0f} s)"))
+    return out
+
+
+def cpu_estimator_check(n=1 << 20, G=256, seed=1):
+    """The sampled estimate of a reference CPU step against a full measured step at N = 1,048,576
+    on 256 x 256 boxes (a few seconds on the host): how far the scaled sample is from the truth."""
+    from barneshut.gb300 import workloads
+    from oracle import oracle
+
+    x, y, m, _, _ = workloads.cluster_mixture(n, seed=seed)
+    threads = os.cpu_count() or 1
+    est = oracle.reference_sample_time(x, y, m, G, 1024, threads)
+    full = oracle.reference_sample_time(x, y, m, G, 1 << 40, threads)
+    full_s = full["setup_s"] + full["sample_s"]
+    return {"n": n, "grid": G, "cores": threads, "full_step_s": full_s, "estimated_step_s": est["step_s"],
+            "estimate_over_full": est["step_s"] / full_s}
+
+
+def flat_same_config(torch, dev, batch, host, reps=2):
+    """The reference's own algorithm on the GPU at the bench's N = 4,194,304 / 512 x 512 input:
+    flat far field (every non-neighbour box through its centre of mass), 3 x 3 near field, the
+    CPU path's r^2 <= 1e-5 cutoff, no softening, FP32 pairs with Kahan far field.  Step time
+    (create_tree + summarize + evaluate + tick, CUDA events) and relative RMS force error on
+    16,384 seeded targets against the FP64 restatement of the reference evaluation."""
+    from barneshut.gb300 import native, workloads
+    from oracle import oracle
+
+    n = batch[0].numel()
+    prm = native.make_params(1.0, DT, 0.0, 1e-5, 0.0, 0, native.BH_PREC_FP32_KAHAN)
+    plan = native.Plan([n], [GRID], prm, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    plan.load(*batch)
+    plan.step(1)  # warm-up
+    ms = []
+    for _ in range(reps):
+        plan.load(*batch)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.step(1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    plan.load(*batch)
+    plan.create_tree()
+    plan.summarize()
+    plan.evaluate()
+    o = plan.store()
+    near, far = plan.pair_counts()
+    flags = plan.error_flags(raise_on_error=False)
+    plan.close()
+    t = workloads.precision_subsample(n, 16384, seed=SEED)
+    x, y, m = host
+    rax, ray = oracle.gpu_evaluate(x, y, m, GRID, gconst=1.0, cutoff=1e-5, targets=t)
+    ax, ay = o["ax"].cpu().numpy()[t], o["ay"].cpu().numpy()[t]
+    ms_step = sorted(ms)[len(ms) // 2]
+    return {"workload": "reference algorithm: flat far field, r^2 <= 1e-5 cutoff, no softening, "
+                        "FP32+Kahan pairs",
+            "ms_per_step": ms_step, "particle_steps_per_s": n / (ms_step / 1e3),
+            "rel_rms_vs_reference_cpu_algorithm": oracle.rel_rms(ax, ay, rax[t], ray[t]),
+            "targets": len(t), "pairs_near": near, "pairs_far": far, "device_error_flags": flags}
 
 
 def batched_benchmark(torch, dev, nsys=512, steps=50, warmup=3):
@@ -454,29 +528,48 @@ def e2e_pipelined_ms(torch, plan, host_in, dev, steps):
 
 
 def run_reference(args, ws, rank):
+    """The reference arm: the reference's CPU algorithm (the oracle's restatement of
+    sequential.py + com_concat_dedup, FP64, OpenMP over target boxes on every host core) on the
+    same N = 4,194,304 / 512 x 512 input.  A full step takes minutes on the host, so each of the
+    W + K steps is a bounded sample of one: the O(N) phases (bounding box, keys, the structured
+    sort, COMs) in full and the evaluation of `--ref-sample-boxes` non-empty boxes at a fixed
+    stride, step k starting one box further along the stride (the K timed steps evaluate K
+    disjoint box samples).  ms_per_step is the measured time of those sampled steps; value is
+    N / (O(N) time + evaluation time scaled to all non-empty boxes), averaged over the K steps.
+    Under torchrun only rank 0 runs."""
     if rank != 0:
         return
     from barneshut.gb300 import workloads
+    from oracle import oracle
 
     x, y, m, vx, vy = workloads.cluster_mixture(args.n, seed=SEED)
-    vals = []
-    t0 = time.time()
-    steps = max(1, min(args.steps, 3))
-    for _ in range(steps):
-        vals.append(cpu_baseline(args, x, y, m, args.grid))
-    val = sum(v["value"] for v in vals) / len(vals)
-    cb = dict(vals[-1])
-    cb["value"] = val
+    threads = os.cpu_count() or 1
+    K, W = max(1, args.steps), max(0, args.warmup)
+    for k in range(W):
+        oracle.reference_sample_time(x, y, m, args.grid, args.ref_sample_boxes, threads, offset=k)
+    t0 = time.perf_counter()
+    runs = [oracle.reference_sample_time(x, y, m, args.grid, args.ref_sample_boxes, threads,
+                                         offset=W + k) for k in range(K)]
+    timed = time.perf_counter() - t0
+    est_s = sum(r["step_s"] for r in runs) / K
+    val = args.n / est_s
+    r0 = runs[0]
+    sample = (f"each step: O(N) phases in full (mean {sum(r['setup_s'] for r in runs) / K:.2f} s) + "
+              f"evaluation of {r0['sampled']} of {r0['nonempty']} non-empty boxes (mean "
+              f"{sum(r['sample_s'] for r in runs) / K:.2f} s), K disjoint box samples; value = N / "
+              f"(O(N) time + evaluation time x {r0['nonempty']}/{r0['sampled']}) = N / {est_s:.1f} s")
     line = {"metric": METRIC, "value": val, "unit": "particle-steps/s", "n_gpus": args.gpus,
-            "steps": steps, "warmup": 0, "ms_per_step": 1e3 * args.n / val,
+            "steps": K, "warmup": W, "ms_per_step": 1e3 * timed / K,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD + " (reference flat far field; no theta in the reference)",
+            "config": {"workload": WORKLOAD + " (reference algorithm: flat far field, r^2 <= 1e-5 "
+                                              "cutoff; the reference has no opening angle)",
                        "n": args.n, "grid": args.grid},
-            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": threads,
+                             "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "wall_s": time.time() - t0}
+            "estimated_full_step_s": est_s}
     print(json.dumps(line), flush=True)
 
 
@@ -554,6 +647,8 @@ def main():
 
     # ---- phases (CUDA events): load, create_tree, summarize, force (dominant kernel)
     ph = {"load": [], "create_tree": [], "summarize": [], "force": []}
+    kern = []
+    plan.set_kernel_timing(True)
     for _ in range(max(3, min(K, 10))):
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
         ev[0].record(stream)
@@ -568,9 +663,11 @@ def main():
         torch.cuda.synchronize()
         for k, (a, b) in zip(ph, zip(ev[:-1], ev[1:])):
             ph[k].append(a.elapsed_time(b))
+        kern.append(plan.force_kernel_ms())
+    plan.set_kernel_timing(False)
     phases_ms = {k: sorted(v)[len(v) // 2] for k, v in ph.items()}
     near2, far2 = plan.pair_counts()
-    t_force = phases_ms["force"] / 1e3
+    t_kernel = sum(kern) / len(kern) / 1e3  # the force kernel alone, mean over the launches
     flops_force = 12.0 * near2 + 20.0 * far2
     peak = fp32_peak_tflops(torch, dev)
 
@@ -618,13 +715,17 @@ def main():
         side["precision"] = precision_study(torch, dev, batch)
         side["learned"] = learned_benchmark(torch, dev, batch, t_dev / K, acc)
 
+    if not args.quick and rank == 0:
+        side["flat_same_config"] = flat_same_config(torch, dev, batch, (x, y, m))
+        side["cpu_estimator_check"] = cpu_estimator_check()
     cpu = None
     if rank == 0:
-        cpu = cpu_baseline(args, x, y, m, args.grid)
+        cpu = cpu_baseline(x, y, m, args.grid, full_limit_s=0.0 if args.quick else 240.0)
 
     if rank == 0:
         peaks = measured_peaks()
-        achieved = flops_force / t_force / 1e12
+        achieved = flops_force / t_kernel / 1e12
+        nominal = 152 * 128 * 2 * (clk.get("sm_max_mhz") or 2070.0) * 1e6 / 1e12
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws,
             "steps": K, "warmup": W, "ms_per_step": 1e3 * t_dev / K, "higher_is_better": True,
@@ -634,16 +735,22 @@ def main():
                        "l2": "state ~400 MB > 129 MB L2 (no flush needed)",
                        "parallelism": f"{ws} independent replica(s)"},
             "gpu_launches": (kernels_per_step + 1) * K,  # + the bh_load kernel of each step
-            "roofline": {"bound": "fp32", "kernel": "k_force (near + far pair loop)",
+            "roofline": {"bound": "fp32", "kernel": "k_fstream (list-streaming force kernel, tick fused)",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": K_FSTREAM_TRAFFIC,
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
-                                           "k_fstream launch at this workload "
-                                           "(profiles/k_fstream_cluster4M_theta05.md)",
-                         "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off",
+                                           "k_fstream launch at this workload (committed summary)",
+                         "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off "
+                                        "(MEASURED_PEAKS.json has no FP32 figure)",
+                         "nominal_peak": nominal, "frac_of_nominal": achieved / nominal,
                          "algorithmic": f"12 flop x {near2} near + 20 flop x {far2} far pairs",
-                         "kernel_ms": 1e3 * t_force},
+                         "kernel_ms": 1e3 * t_kernel,
+                         "kernel_ms_source": "CUDA events around the force kernel alone "
+                                             "(bh_set_kernel_timing), mean of the phase launches",
+                         "force_phase_ms": phases_ms["force"]},
             "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "cpu_baseline_detail": {k: cpu[k] for k in ("measured", "step_seconds", "estimate_s",
+                                                       "estimate_sample")},
             "e2e": e2e,
             "clocks": clk,
             "accuracy": acc,

@@ -200,6 +200,15 @@ int bh_box_moments(bh_plan *plan, int sys, double *out, void *stream);
  * (base.py:211-239). */
 int bh_grid_info(bh_plan *plan, int sys, double *out, void *stream);
 
+/* Kernel timing, no reference counterpart (the reference's Timer measures whole phases,
+ * timer/timer.py).  With enable != 0, each later eager bh_evaluate records two CUDA events on
+ * its stream, right before and after the force kernel proper (after the interaction lists and
+ * the work-item order of the list-streaming path); bh_force_kernel_ms waits for the second
+ * event and returns the last such launch's duration in milliseconds.  Graph replays
+ * (bh_step_graph) and bh_step record nothing. */
+int bh_set_kernel_timing(bh_plan *plan, int enable);
+int bh_force_kernel_ms(bh_plan *plan, float *ms);
+
 /* FP64 direct sum on the device for nt targets (indices into the
  * concatenated pid order, device array) of system `sys`, no cutoff, the
  * plan's softening: a_t = G sum_{j != t} m_j (x_j - x_t) / (r^2 + eps^2).
@@ -220,8 +229,11 @@ int bh_direct_sample(bh_plan *plan, int sys, const long long *targets, long long
  * device array of BH_NOALLOC_MAX_TARGETS x BH_NOALLOC_CHUNKS x 2 doubles (4 MiB)
  * that every GPU loading the library holds until the process exits; more
  * than BH_NOALLOC_MAX_TARGETS targets is rejected with BH_ERR_INVALID.  The
- * first call on a device looks up that array's device address (once, with
- * the device current); make that first call before any stream capture.  All
+ * array's device address belongs to one CUDA context: the first call in a
+ * context (the current one, or the device's primary context if none is
+ * current) looks it up with that context current and caches it under the
+ * context's process-unique ID, so a context made after cudaDeviceReset looks
+ * it up again; make the first call in a context before any stream capture.  All
  * calls share the array: calls that overlap on the GPU (e.g. on two streams)
  * race and must be ordered by the caller.  bh_last_error(NULL) describes a
  * failure. */

@@ -33,6 +33,8 @@
  *                         acceptance test is evaluated in float exactly as the
  *                         CUDA kernel evaluates it, so both sides build the same
  *                         interaction lists; the pair arithmetic here is FP64.
+ *   8. oref_gpu_evaluate  the reference GPU evaluation (flat far field over every
+ *                         box, no cutoff): kernels/grid_decomposition/gpu/grid.py:15-268
  *
  * Build: gcc -O2 -fopenmp -ffp-contract=off -fPIC -shared (no FMA contraction:
  * the reference is plain IEEE double arithmetic).
@@ -312,7 +314,8 @@ int oref_reference_evaluate(long long n, const double *x, const double *y, const
  * Timed, bounded sample of one reference CPU step on a large system (the CPU
  * baseline).  Runs the O(N) phases in full (bounding box, keys, the sort by
  * (gx, gy, px, ...), per-box COM) and the com_concat_dedup evaluation for
- * `nsample` non-empty target boxes drawn with a fixed stride, with OpenMP over
+ * `nsample` non-empty target boxes drawn with a fixed stride (starting at `offset` within the
+ * stride, so successive calls with offsets 0, 1, 2, ... sample disjoint boxes), with OpenMP over
  * the sampled boxes.  Each sampled box does the reference's work: build its
  * COM list over all boxes, the far field against it, the four dedup
  * neighbours with mutual update, and the self interaction.
@@ -330,7 +333,7 @@ static double wall_seconds(void)
 }
 
 void oref_reference_sample_time(long long n, const double *x, const double *y, const double *m,
-                                int G, long long nsample, int nthreads, double *out)
+                                int G, long long nsample, long long offset, int nthreads, double *out)
 {
     double t0 = wall_seconds();
     double bb[5];
@@ -378,7 +381,7 @@ void oref_reference_sample_time(long long n, const double *x, const double *y, c
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : sink)
 #endif
     for (long long q = 0; q < nsample; q++) {
-        long long b = ne[q * strd];
+        long long b = ne[(q * strd + (strd > 1 ? offset % strd : 0)) % (nonempty ? nonempty : 1)];
         int bx = (int)(b / G), by = (int)(b % G);
         long long s0 = start[b], na = start[b + 1] - s0;
         double *f1 = (double *)calloc(2 * (size_t)na, sizeof(double));
@@ -630,6 +633,8 @@ void oref_moments(long long n, const double *x, const double *y, const double *m
  * non-empty leaf box as a monopole.  Pairs whose unsoftened r^2 <= cutoff are
  * skipped (cutoff = 1e-5 reproduces cpu_numba.py; 0 skips coincident points).
  * Output ax/ay in pid order.  counts[0..1] = near / far pair interactions.
+ * mask (optional, one byte per particle): forces are computed only for targets whose byte is
+ * non-zero (the others keep their ax/ay); the pair counts always cover every target.
  */
 /*
  * dense_min > 0 (theta mode): the targets of a box holding at least dense_min particles use
@@ -644,7 +649,7 @@ void oref_moments(long long n, const double *x, const double *y, const double *m
 int oref_theta_evaluate(long long n, const double *x, const double *y, const double *m, int G,
                         int TG, double theta, double eps2, double cutoff, double gconst,
                         double *ax, double *ay, long long *counts, int nthreads, int dense_min,
-                        int quad_min)
+                        int quad_min, const unsigned char *mask)
 {
     if (n <= 0) return 0;
     double bb[5];
@@ -832,6 +837,7 @@ int oref_theta_evaluate(long long n, const double *x, const double *y, const dou
                     for (long long k = bstart[bb0]; k < bstart[bb0 + 1]; k++) {
                         long long t = order[k];
                         if (kind == 2 && quad[t] != part) continue;
+                        if (mask && !mask[t]) continue;
                         double xt = x[t], yt = y[t], sx = 0.0, sy = 0.0;
                         for (long long q = 0; q < nacc; q++) {
                             long long cell = bfar[q];
@@ -897,4 +903,108 @@ int oref_theta_evaluate(long long n, const double *x, const double *y, const dou
     free(bstart);
     free(order);
     return G;
+}
+
+/* ------------------------------------------------------------------ 8 -- */
+/*
+ * The reference GPU evaluation (python-bh kernels/grid_decomposition/gpu/grid.py), FP64:
+ *   keys      g_place_particles (:15-50): min(floor((p - min) / step), G - 1)
+ *   COMs      g_summarize (:78-114): sum of p * m and m over the box; (0, 0, 0) for an empty box
+ *   evaluate  g_evaluate_boxes (:116-157) with d_self_self_grav (:211-229), d_self_other_grav
+ *             (:231-248), d_self_COM_grav (:250-268): for every target, a loop over all G x G
+ *             boxes in (gx, gy) order -- its own box pair by pair skipping only itself (j != i),
+ *             the 8 neighbours pair by pair, every other box (empty ones included) through its
+ *             COM -- with f = (G m_i m_j) / (dist * dist), dist = sqrt(dx^2 + dy^2), and
+ *             a -= f * dx / m_i, dx = x_i - x_j.  No cutoff, no softening.
+ * The reference GPU path divides by zero for two particles at the same position (and for a
+ * particle at exactly (0, 0) against an empty box's zero COM), which gives NaN; skip_zero != 0
+ * drops every pair with dist == 0 instead (the rule of this project's CUDA path).  cutoff >= 0
+ * also drops pairs with dx^2 + dy^2 <= cutoff (1e-5 gives the CPU path's physics: used to pin
+ * this restatement against the reference CPU path's golden vectors).  mask: see
+ * oref_theta_evaluate.  Output ax/ay in pid order.
+ */
+static inline void gpu_pair(double xi, double yi, double mi, double ox, double oy, double mj,
+                            double G, double cutoff, int skip_zero, double *ax, double *ay)
+{
+    double xdif = xi - ox, ydif = yi - oy;
+    double r2 = xdif * xdif + ydif * ydif;
+    if (cutoff >= 0.0 && !(r2 > cutoff)) return;
+    double dist = sqrt(r2);
+    if (skip_zero && dist == 0.0) return;
+    double f = (G * mi * mj) / (dist * dist);
+    *ax = *ax - (f * xdif / mi);
+    *ay = *ay - (f * ydif / mi);
+}
+
+void oref_gpu_evaluate(long long n, const double *x, const double *y, const double *m, int G,
+                       double gconst, double cutoff, int skip_zero, const unsigned char *mask,
+                       double *ax, double *ay, int nthreads)
+{
+    if (n <= 0) return;
+    double bb[5];
+    oref_bbox(n, x, y, G, bb);
+    int *kx = (int *)malloc(sizeof(int) * (size_t)n), *ky = (int *)malloc(sizeof(int) * (size_t)n);
+    for (long long i = 0; i < n; i++) {
+        double qx = floor((x[i] - bb[0]) / bb[4]), qy = floor((y[i] - bb[1]) / bb[4]);
+        kx[i] = (int)(qx < (double)(G - 1) ? qx : (double)(G - 1));
+        ky[i] = (int)(qy < (double)(G - 1) ? qy : (double)(G - 1));
+    }
+    long long B = (long long)G * G;
+    long long *bstart = (long long *)calloc((size_t)B + 1, sizeof(long long));
+    long long *order = (long long *)malloc(sizeof(long long) * (size_t)n);
+    for (long long i = 0; i < n; i++) bstart[(long long)kx[i] * G + ky[i] + 1]++;
+    for (long long b = 0; b < B; b++) bstart[b + 1] += bstart[b];
+    {
+        long long *cur = (long long *)malloc(sizeof(long long) * (size_t)B);
+        memcpy(cur, bstart, sizeof(long long) * (size_t)B);
+        for (long long i = 0; i < n; i++) order[cur[(long long)kx[i] * G + ky[i]]++] = i;
+        free(cur);
+    }
+    double *com = (double *)calloc(3 * (size_t)B, sizeof(double));
+    for (long long b = 0; b < B; b++) {
+        if (bstart[b + 1] == bstart[b]) continue;
+        double M = 0.0, sx = 0.0, sy = 0.0;
+        for (long long k = bstart[b]; k < bstart[b + 1]; k++) {
+            long long j = order[k];
+            sx += x[j] * m[j];
+            sy += y[j] * m[j];
+            M += m[j];
+        }
+        if (M != 0.0) {
+            com[3 * b] = sx / M;
+            com[3 * b + 1] = sy / M;
+            com[3 * b + 2] = M;
+        }
+    }
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+    for (long long i = 0; i < n; i++) {
+        if (mask && !mask[i]) continue;
+        const int bx = kx[i], by = ky[i];
+        const double xi = x[i], yi = y[i], mi = m[i];
+        double sx = 0.0, sy = 0.0;
+        for (int gx = 0; gx < G; gx++)
+            for (int gy = 0; gy < G; gy++) {
+                long long c = (long long)gx * G + gy;
+                if (abs(gx - bx) <= 1 && abs(gy - by) <= 1) {
+                    for (long long k = bstart[c]; k < bstart[c + 1]; k++) {
+                        long long j = order[k];
+                        if (j == i) continue;
+                        gpu_pair(xi, yi, mi, x[j], y[j], m[j], gconst, cutoff, skip_zero, &sx, &sy);
+                    }
+                } else {
+                    gpu_pair(xi, yi, mi, com[3 * c], com[3 * c + 1], com[3 * c + 2], gconst, cutoff,
+                             skip_zero, &sx, &sy);
+                }
+            }
+        ax[i] = sx;
+        ay[i] = sy;
+    }
+    free(kx);
+    free(ky);
+    free(bstart);
+    free(order);
+    free(com);
 }

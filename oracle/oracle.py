@@ -66,9 +66,11 @@ def lib():
         L.oref_pyramid_cells.argtypes = [i]
         L.oref_pyramid_cells.restype = ll
         L.oref_moments.argtypes = [ll, pd, pd, pd, i, pd, pi, pi, pd, pf]
-        L.oref_theta_evaluate.argtypes = [ll, pd, pd, pd, i, i, d, d, d, d, pd, pd, pll, i, i, i]
+        L.oref_theta_evaluate.argtypes = [ll, pd, pd, pd, i, i, d, d, d, d, pd, pd, pll, i, i, i,
+                                          ctypes.c_void_p]
         L.oref_theta_evaluate.restype = i
-        L.oref_reference_sample_time.argtypes = [ll, pd, pd, pd, i, ll, i, pd]
+        L.oref_gpu_evaluate.argtypes = [ll, pd, pd, pd, i, d, d, i, ctypes.c_void_p, pd, pd, i]
+        L.oref_reference_sample_time.argtypes = [ll, pd, pd, pd, i, ll, ll, i, pd]
         _lib = L
     return _lib
 
@@ -176,29 +178,56 @@ def moments(x, y, m, G):
     return dict(mom=mom, rec=rec, bbox=bb, kx=kx, ky=ky)
 
 
+def _mask(n, targets):
+    if targets is None:
+        return None
+    mk = np.zeros(n, np.uint8)
+    mk[np.asarray(targets, dtype=np.int64)] = 1
+    return mk
+
+
 def theta_evaluate(x, y, m, G, TG=1, theta=0.5, eps2=0.0, cutoff=0.0, gconst=1.0, nthreads=0,
-                   dense_min=0, quad_min=0):
+                   dense_min=0, quad_min=0, targets=None):
     """FP64 opening-angle evaluation (theta <= 0: the reference's flat mode).  dense_min > 0:
     boxes with at least dense_min particles use per-box refined lists; quad_min > 0: boxes with
-    at least quad_min particles use per-quadrant refined lists (see bh_oracle.c).
-    Returns (ax, ay, n_near_pairs, n_far_pairs)."""
+    at least quad_min particles use per-quadrant refined lists (see bh_oracle.c).  targets (pid
+    indices): compute forces only for these (the others stay 0); pair counts cover all targets.
+    Returns (ax, ay, n_near_pairs, n_far_pairs) with ax/ay over all n particles."""
     x, y, m = _d(x), _d(y), _d(m)
     n = len(x)
     ax, ay = np.zeros(n), np.zeros(n)
     cnt = np.zeros(2, np.int64)
+    mk = _mask(n, targets)
     lib().oref_theta_evaluate(n, _p(x), _p(y), _p(m), int(G), int(TG), float(theta),
                               float(eps2), float(cutoff), float(gconst), _p(ax), _p(ay),
-                              _p(cnt, ctypes.c_longlong), int(nthreads), int(dense_min), int(quad_min))
+                              _p(cnt, ctypes.c_longlong), int(nthreads), int(dense_min), int(quad_min),
+                              None if mk is None else mk.ctypes.data)
     return ax, ay, int(cnt[0]), int(cnt[1])
 
 
-def reference_sample_time(x, y, m, G, nsample, nthreads=0):
-    """Time a bounded sample of one reference CPU step (see bh_oracle.c).
-    Returns dict(setup_s, sample_s, nonempty, sampled, step_s)."""
+def gpu_evaluate(x, y, m, G, gconst=1.0, cutoff=-1.0, skip_zero=False, targets=None, nthreads=0):
+    """The reference GPU path's evaluation (gpu/grid.py: flat far field over every box, j != i,
+    no cutoff).  skip_zero: drop pairs at distance 0 (which give NaN in the reference GPU path)
+    as this project's CUDA path does; cutoff >= 0: also drop pairs with r^2 <= cutoff (1e-5: the
+    CPU path's physics).  targets: compute only these (the others stay 0).  Returns (ax, ay)."""
+    x, y, m = _d(x), _d(y), _d(m)
+    n = len(x)
+    ax, ay = np.zeros(n), np.zeros(n)
+    mk = _mask(n, targets)
+    lib().oref_gpu_evaluate(n, _p(x), _p(y), _p(m), int(G), float(gconst), float(cutoff),
+                            int(bool(skip_zero)), None if mk is None else mk.ctypes.data,
+                            _p(ax), _p(ay), int(nthreads))
+    return ax, ay
+
+
+def reference_sample_time(x, y, m, G, nsample, nthreads=0, offset=0):
+    """Time a bounded sample of one reference CPU step (see bh_oracle.c); nsample >= the
+    non-empty boxes times the whole step.  Returns dict(setup_s, sample_s, nonempty, sampled,
+    step_s), step_s = setup_s + sample_s * nonempty / sampled."""
     x, y, m = _d(x), _d(y), _d(m)
     out = np.zeros(6)
     lib().oref_reference_sample_time(len(x), _p(x), _p(y), _p(m), int(G), int(nsample),
-                                     int(nthreads), _p(out))
+                                     int(offset), int(nthreads), _p(out))
     return dict(setup_s=out[0], sample_s=out[1], nonempty=int(out[2]), sampled=int(out[3]),
                 step_s=out[4])
 

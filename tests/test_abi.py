@@ -118,3 +118,33 @@ def test_launch_count_host_logic(lib):
     stream = count()
     assert count(flags=native.BH_FLAG_WALK) == stream + 5 - 8  # walk items in, stream items and lists out
     assert count(flags=native.BH_FLAG_LEARNED) == stream + 5
+
+
+def _workspace(lib, n, G, **kw):
+    rc, h = _create(lib, [n], [G], theta=0.5, softening=1e-4, cutoff_r2=0.0, **kw)
+    assert rc == 0
+    sz = ctypes.c_size_t()
+    assert lib.bh_workspace_size(h, ctypes.byref(sz)) == 0
+    assert lib.bh_plan_destroy(h) == 0
+    return sz.value
+
+
+def test_workspace_budget(lib):
+    """Workspace of the list-streaming plans: the far-list slots dominate at small target groups
+    (one 16-byte slot per cell a level's frontier can hold, 4 (TG/2 + 2/theta + 2)^2 at most,
+    per level and group).  Budgets: N = 4,194,304 on 512 x 512 boxes, theta = 0.5 -- 1.25 GB with
+    4 x 4 groups (the benchmark's tile), 6.1 GB with single-box groups; N = 16,777,216 on
+    16384 x 16384 boxes needs 364 GB with 8 x 8 groups, more than one GPU holds; such grids take
+    the pyramid walk (BH_FLAG_WALK), which keeps no lists: 38 GB, mostly the 358M pyramid cells'
+    moments and records (80 B each)."""
+    from barneshut.gb300 import native
+
+    n4m = 1 << 22
+    assert _workspace(lib, n4m, 512, group_dim=4) <= 1.25e9
+    assert _workspace(lib, n4m, 512, group_dim=1) <= 6.1e9
+    sizes = [_workspace(lib, n4m, 512, group_dim=t) for t in (1, 2, 4, 8)]
+    assert sizes == sorted(sizes, reverse=True)
+    big = _workspace(lib, 1 << 24, 16384, group_dim=8)
+    assert 3.0e11 < big <= 3.7e11
+    walk = _workspace(lib, 1 << 24, 16384, group_dim=8, flags=native.BH_FLAG_WALK)
+    assert walk <= 3.9e10

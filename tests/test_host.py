@@ -5,8 +5,7 @@ import numpy as np
 import pytest
 
 from barneshut.gb300 import particle_io, workloads
-from barneshut.kernels.helpers import (get_bounding_box, get_neighbor_cells, next_perfect_square,
-                                       remove_bottom_left_neighbors)
+from barneshut.kernels.helpers import get_bounding_box, next_perfect_square
 
 
 def test_next_perfect_square():
@@ -20,15 +19,6 @@ def test_bounding_box_is_square():
     pts = np.array([[0.0, 0.0], [2.0, 1.0], [1.0, 0.5]])
     (a, b), (c, d) = get_bounding_box(pts)
     assert (a, b, c, d) == (0.0, 0.0, 2.0, 2.0)
-
-
-def test_neighbours_and_dedup():
-    nb = get_neighbor_cells((0, 0), 4)
-    assert nb == [(0, 1), (1, 0), (1, 1)]
-    nb = get_neighbor_cells((2, 2), 4)
-    assert len(nb) == 8
-    kept = remove_bottom_left_neighbors((2, 2), list(nb))
-    assert kept == [(1, 3), (2, 3), (3, 2), (3, 3)]
 
 
 def test_particle_file_roundtrip(tmp_path):

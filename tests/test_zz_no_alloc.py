@@ -71,3 +71,23 @@ def test_noalloc_rejects_too_many_targets():
                                  _p(out), None)
     assert rc == native.BH_ERR_INVALID
     assert b"BH_NOALLOC_MAX_TARGETS" in L.bh_last_error(None)
+
+
+def test_noalloc_small_n_ragged_targets():
+    """Fewer particles (40) than source chunks (64), so most chunks are empty; target indices
+    outside [0, n) come back as NaN, as bh_direct_sample reports them; nt = 5 is not a multiple
+    of the finishing kernel's block.  Checked against the FP64 oracle's direct sum."""
+    from barneshut.gb300 import native, workloads
+    from oracle import oracle
+
+    L = native.load_library()
+    n = 40
+    x, y, m, _, _ = workloads.uniform(n, seed=321)
+    X, Y, M = (torch.as_tensor(a, device="cuda") for a in (x, y, m))
+    targets = np.array([-1, 0, 39, 40, 17])
+    ax, ay = noalloc(L, X, Y, M, targets, 2.0, 1e-2)
+    ok = (targets >= 0) & (targets < n)
+    assert np.all(np.isnan(ax[~ok])) and np.all(np.isnan(ay[~ok]))
+    rx, ry = oracle.direct(x, y, m, gconst=2.0, eps2=1e-4, cutoff=-1.0, targets=targets[ok])
+    np.testing.assert_allclose(ax[ok], rx, rtol=1e-11, atol=0)
+    np.testing.assert_allclose(ay[ok], ry, rtol=1e-11, atol=0)
