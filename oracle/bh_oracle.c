@@ -570,6 +570,8 @@ static void shift_moments(const double *c, double dx, double dy, double *p)
  * {cx_off, cy_off, M, 0} where cx_off = (float)(Sx/M) is the centre of mass
  * relative to the cell origin (zeros for an empty cell).
  */
+static void build_pyramid(int G, double step, double *mom, float *rec);
+
 void oref_moments(long long n, const double *x, const double *y, const double *m, int G,
                   const double *bb, const int *kx, const int *ky, double *mom, float *rec)
 {
@@ -588,6 +590,15 @@ void oref_moments(long long n, const double *x, const double *y, const double *m
         q[4] += mm * dx * dy;
         q[5] += mm * dy * dy;
     }
+    build_pyramid(G, step, mom, rec);
+}
+
+/* Levels above the leaves (each cell the sum of its up to four children, shifted to its origin)
+ * and the float records, from the leaf moments in mom[0 .. G*G*6). */
+static void build_pyramid(int G, double step, double *mom, float *rec)
+{
+    long long ncell = oref_pyramid_cells(G);
+    memset(mom + 6 * (size_t)G * (size_t)G, 0, sizeof(double) * 6 * (size_t)(ncell - (long long)G * G));
     long long off = 0, poff;
     int g = G, l = 0;
     while (g > 1) {
@@ -646,14 +657,71 @@ void oref_moments(long long n, const double *x, const double *y, const double *m
  * quadrant is the low bit of its FP64 key at twice the box resolution).  dense_min <= 0 and
  * quad_min <= 0 keep the group lists for every target (the walking force kernel).
  */
+static int theta_eval_core(long long n, const double *x, const double *y, const double *m, int G,
+                           int TG, double theta, double eps2, double cutoff, double gconst,
+                           double *ax, double *ay, long long *counts, int nthreads, int dense_min,
+                           int quad_min, const unsigned char *mask, const double *bb_in,
+                           const double *leaf_in);
+
 int oref_theta_evaluate(long long n, const double *x, const double *y, const double *m, int G,
                         int TG, double theta, double eps2, double cutoff, double gconst,
                         double *ax, double *ay, long long *counts, int nthreads, int dense_min,
                         int quad_min, const unsigned char *mask)
 {
+    return theta_eval_core(n, x, y, m, G, TG, theta, eps2, cutoff, gconst, ax, ay, counts, nthreads,
+                           dense_min, quad_min, mask, NULL, NULL);
+}
+
+/*
+ * The same evaluation on a part of a system (one rank's slab of boxes plus the halo boxes its
+ * near field reaches), with the grid and the far field of the whole system given: bb_in[5] the
+ * whole system's square box (oref_bbox layout) and leaf_in[G*G*6] its leaf moments (M, Sx, Sy,
+ * Sxx, Sxy, Syy about each box origin).  Pass the targets to evaluate in mask; the particles
+ * present must include every near box of those targets.  Pair counts cover the masked targets
+ * only.
+ */
+int oref_theta_evaluate_part(long long n, const double *x, const double *y, const double *m, int G,
+                             int TG, double theta, double eps2, double cutoff, double gconst,
+                             double *ax, double *ay, long long *counts, int nthreads, int dense_min,
+                             int quad_min, const unsigned char *mask, const double *bb_in,
+                             const double *leaf_in)
+{
+    return theta_eval_core(n, x, y, m, G, TG, theta, eps2, cutoff, gconst, ax, ay, counts, nthreads,
+                           dense_min, quad_min, mask, bb_in, leaf_in);
+}
+
+/* Leaf moments of boxes (M, Sx, Sy, Sxx, Sxy, Syy about each box origin, FP64, particles summed
+ * in index order) of the given particles on the grid bb (oref_bbox layout).  out[G*G*6]. */
+void oref_leaf_moments(long long n, const double *x, const double *y, const double *m, int G,
+                       const double *bb, double *out)
+{
+    memset(out, 0, sizeof(double) * 6 * (size_t)G * (size_t)G);
+    for (long long i = 0; i < n; i++) {
+        int kx = ref_key1(x[i], bb[0], bb[4], G), ky = ref_key1(y[i], bb[1], bb[4], G);
+        double ox = bb[0] + (double)kx * bb[4], oy = bb[1] + (double)ky * bb[4];
+        double dx = x[i] - ox, dy = y[i] - oy, mm = m[i];
+        double *q = out + 6 * ((long long)kx * G + ky);
+        q[0] += mm;
+        q[1] += mm * dx;
+        q[2] += mm * dy;
+        q[3] += mm * dx * dx;
+        q[4] += mm * dx * dy;
+        q[5] += mm * dy * dy;
+    }
+}
+
+static int theta_eval_core(long long n, const double *x, const double *y, const double *m, int G,
+                           int TG, double theta, double eps2, double cutoff, double gconst,
+                           double *ax, double *ay, long long *counts, int nthreads, int dense_min,
+                           int quad_min, const unsigned char *mask, const double *bb_in,
+                           const double *leaf_in)
+{
     if (n <= 0) return 0;
     double bb[5];
-    oref_bbox(n, x, y, G, bb);
+    if (bb_in)
+        memcpy(bb, bb_in, sizeof(bb));
+    else
+        oref_bbox(n, x, y, G, bb);
     int *kx = (int *)malloc(sizeof(int) * (size_t)n), *ky = (int *)malloc(sizeof(int) * (size_t)n);
     oref_keys(n, x, y, G, bb, kx, ky);
     /* quadrant of each particle within its box: the low bits of the keys at twice the box
@@ -671,7 +739,12 @@ int oref_theta_evaluate(long long n, const double *x, const double *y, const dou
     int L = oref_num_levels(G);
     double *mom = (double *)malloc(sizeof(double) * 6 * (size_t)ncell);
     float *rec = (float *)malloc(sizeof(float) * 4 * (size_t)ncell);
-    oref_moments(n, x, y, m, G, bb, kx, ky, mom, rec);
+    if (leaf_in) {
+        memcpy(mom, leaf_in, sizeof(double) * 6 * (size_t)B);
+        build_pyramid(G, bb[4], mom, rec);
+    } else {
+        oref_moments(n, x, y, m, G, bb, kx, ky, mom, rec);
+    }
     long long *lvoff = (long long *)malloc(sizeof(long long) * (size_t)(L + 1));
     int *lvg = (int *)malloc(sizeof(int) * (size_t)(L + 1));
     {
@@ -723,7 +796,9 @@ int oref_theta_evaluate(long long n, const double *x, const double *y, const dou
             for (int i = 0; i < G; i++)
                 for (int j = 0; j < G; j++) {
                     long long c = (long long)i * G + j;
-                    if (bstart[c + 1] == bstart[c]) continue;
+                    /* a part of a system knows the other boxes by their moments only */
+                    const int nonempty = bstart[c + 1] > bstart[c] || (leaf_in && mom[6 * c] > 0.0);
+                    if (!nonempty) continue;
                     if (abs(i - gx0) <= 1 && abs(j - gy0) <= 1)
                         near[nnear++] = c;
                     else
@@ -791,9 +866,12 @@ int oref_theta_evaluate(long long n, const double *x, const double *y, const dou
                 else if (!flat && dense_min > 0 && nb >= dense_min)
                     kind = 1;
                 for (int part = 0; part < (kind == 2 ? 4 : 1); part++) {
-                    long long nt_part = 0;
+                    long long nt_part = 0, nt_cnt = 0;
                     for (long long k = bstart[bb0]; k < bstart[bb0 + 1]; k++)
-                        if (kind != 2 || quad[order[k]] == part) nt_part++;
+                        if (kind != 2 || quad[order[k]] == part) {
+                            nt_part++;
+                            if (!bb_in || !mask || mask[order[k]]) nt_cnt++;
+                        }
                     if (nt_part == 0) continue;
                     const long long *nl = near;
                     long long nnl = nnear, nacc = 0;
@@ -832,8 +910,8 @@ int oref_theta_evaluate(long long n, const double *x, const double *y, const dou
                     }
                     long long nsrc = 0;
                     for (long long q = 0; q < nnl; q++) nsrc += bstart[nl[q] + 1] - bstart[nl[q]];
-                    cnt_near += nt_part * nsrc;
-                    cnt_far += nt_part * (nfar + nacc);
+                    cnt_near += nt_cnt * nsrc;
+                    cnt_far += nt_cnt * (nfar + nacc);
                     for (long long k = bstart[bb0]; k < bstart[bb0 + 1]; k++) {
                         long long t = order[k];
                         if (kind == 2 && quad[t] != part) continue;

@@ -33,10 +33,11 @@ def build(force=False):
     if (not force and os.path.exists(LIB)
             and os.path.getmtime(LIB) >= os.path.getmtime(SRC)):
         return LIB
+    tmp = f"{LIB}.{os.getpid()}.tmp"  # concurrent builders never share a temporary
     cmd = ["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
-           "-shared", "-o", LIB + ".tmp", SRC, "-lm"]
+           "-shared", "-o", tmp, SRC, "-lm"]
     subprocess.run(cmd, check=True)
-    os.replace(LIB + ".tmp", LIB)
+    os.replace(tmp, LIB)
     return LIB
 
 
@@ -69,6 +70,10 @@ def lib():
         L.oref_theta_evaluate.argtypes = [ll, pd, pd, pd, i, i, d, d, d, d, pd, pd, pll, i, i, i,
                                           ctypes.c_void_p]
         L.oref_theta_evaluate.restype = i
+        L.oref_theta_evaluate_part.argtypes = [ll, pd, pd, pd, i, i, d, d, d, d, pd, pd, pll, i,
+                                               i, i, ctypes.c_void_p, pd, pd]
+        L.oref_theta_evaluate_part.restype = i
+        L.oref_leaf_moments.argtypes = [ll, pd, pd, pd, i, pd, pd]
         L.oref_gpu_evaluate.argtypes = [ll, pd, pd, pd, i, d, d, i, ctypes.c_void_p, pd, pd, i]
         L.oref_reference_sample_time.argtypes = [ll, pd, pd, pd, i, ll, ll, i, pd]
         _lib = L
@@ -203,6 +208,34 @@ def theta_evaluate(x, y, m, G, TG=1, theta=0.5, eps2=0.0, cutoff=0.0, gconst=1.0
                               _p(cnt, ctypes.c_longlong), int(nthreads), int(dense_min), int(quad_min),
                               None if mk is None else mk.ctypes.data)
     return ax, ay, int(cnt[0]), int(cnt[1])
+
+
+def theta_evaluate_part(x, y, m, G, bb, leaf, targets, TG=1, theta=0.5, eps2=0.0, cutoff=0.0,
+                        gconst=1.0, nthreads=0, dense_min=0, quad_min=0):
+    """theta_evaluate on a part of a system (a slab of boxes and the halo boxes its near field
+    reaches) with the whole system's square box bb[5] and leaf moments leaf[G, G, 6] given.
+    targets: the local indices to evaluate.  Returns (ax, ay, n_near_pairs, n_far_pairs) over the
+    local particles (non-targets stay 0) and the targets' pair counts."""
+    x, y, m = _d(x), _d(y), _d(m)
+    n = len(x)
+    ax, ay = np.zeros(n), np.zeros(n)
+    cnt = np.zeros(2, np.int64)
+    mk = _mask(n, targets)
+    bb = _d(bb)
+    leaf = _d(leaf).reshape(-1)
+    lib().oref_theta_evaluate_part(n, _p(x), _p(y), _p(m), int(G), int(TG), float(theta),
+                                   float(eps2), float(cutoff), float(gconst), _p(ax), _p(ay),
+                                   _p(cnt, ctypes.c_longlong), int(nthreads), int(dense_min),
+                                   int(quad_min), mk.ctypes.data, _p(bb), _p(leaf))
+    return ax, ay, int(cnt[0]), int(cnt[1])
+
+
+def leaf_moments(x, y, m, G, bb):
+    """Leaf moments (M, Sx, Sy, Sxx, Sxy, Syy about each box origin), shape (G, G, 6)."""
+    x, y, m = _d(x), _d(y), _d(m)
+    out = np.zeros((G, G, 6))
+    lib().oref_leaf_moments(len(x), _p(x), _p(y), _p(m), int(G), _p(_d(bb)), _p(out))
+    return out
 
 
 def gpu_evaluate(x, y, m, G, gconst=1.0, cutoff=-1.0, skip_zero=False, targets=None, nthreads=0):
