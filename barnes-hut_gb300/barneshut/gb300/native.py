@@ -42,7 +42,7 @@ EXPORTS = (
     "bh_kernels_per_step", "bh_mlp_param_count", "bh_mlp_image_bytes", "bh_mlp_pack",
     "bh_mlp_forward", "bh_mlp_train_batch", "bh_mlp_adam", "bh_set_correction", "bh_learned_pairs",
     "bh_direct_sum_noalloc", "bh_generate", "bh_graph_kernel_nodes", "bh_set_kernel_timing",
-    "bh_force_kernel_ms",
+    "bh_force_kernel_ms", "bh_corrected_pairs", "bh_set_grid", "bh_leaf_moments", "bh_set_leaf_moments",
 )
 BH_GEN_UNIFORM, BH_GEN_GAUSS, BH_GEN_CLUSTER = 0, 1, 2
 BH_NOALLOC_MAX_TARGETS = 4096
@@ -120,6 +120,10 @@ def load_library(path=None):
     L.bh_kernels_per_step.argtypes = [vp, pi]
     L.bh_graph_kernel_nodes.argtypes = [vp, pi]
     L.bh_set_kernel_timing.argtypes = [vp, i]
+    L.bh_corrected_pairs.argtypes = [vp, pll, vp]
+    L.bh_set_grid.argtypes = [vp, i, ctypes.POINTER(d), vp]
+    L.bh_leaf_moments.argtypes = [vp, i, vp, vp]
+    L.bh_set_leaf_moments.argtypes = [vp, i, vp, vp]
     L.bh_force_kernel_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
     L.bh_set_correction.argtypes = [vp, vp, vp]
     L.bh_direct_sum_noalloc.argtypes = [vp, vp, vp, ll, vp, ll, d, d, vp, vp, vp]
@@ -327,6 +331,31 @@ class Plan:
         self._check(self.L.bh_graph_kernel_nodes(self.h, ctypes.byref(c)))
         return c.value
 
+    def set_grid(self, extents, sys=0):
+        """Fix the grid of system `sys` to the whole system's extents (min x, min y, max x,
+        max y); None returns to the plan's own bounding box."""
+        if extents is None:
+            self._check(self.L.bh_set_grid(self.h, sys, None, self._st()))
+        else:
+            e = (ctypes.c_double * 4)(*[float(v) for v in extents])
+            self._check(self.L.bh_set_grid(self.h, sys, e, self._st()))
+
+    def leaf_moments(self, sys=0):
+        """(G, G, 6) device tensor: the last summarize's leaf moments (M, Sx, Sy, Sxx, Sxy, Syy
+        about each box origin)."""
+        torch = self._torch
+        G = self.grid_info(sys)["grid_dim"]
+        out = torch.empty((G, G, 6), dtype=torch.float64, device=self.device)
+        self._check(self.L.bh_leaf_moments(self.h, sys, _ptr(out), self._st()))
+        return out
+
+    def set_leaf_moments(self, leaf, sys=0):
+        """Replace the leaf moments of system `sys` (device (G, G, 6) FP64) and rebuild the
+        pyramid above them."""
+        leaf = self._torch.as_tensor(leaf, dtype=self._torch.float64, device=self.device).contiguous()
+        self._check(self.L.bh_set_leaf_moments(self.h, sys, _ptr(leaf), self._st()))
+        self._keep = leaf  # alive until the copy has run
+
     def set_kernel_timing(self, enable=True):
         """Record CUDA events around the force kernel of every later eager evaluate()."""
         self._check(self.L.bh_set_kernel_timing(self.h, 1 if enable else 0))
@@ -341,6 +370,12 @@ class Plan:
         a, b = ctypes.c_longlong(), ctypes.c_longlong()
         self._check(self.L.bh_pair_counts(self.h, ctypes.byref(a), ctypes.byref(b), self._st()))
         return a.value, b.value
+
+    def corrected_pairs(self):
+        """(target, cell) pairs the learned correction evaluated in the last step."""
+        a = ctypes.c_longlong()
+        self._check(self.L.bh_corrected_pairs(self.h, ctypes.byref(a), self._st()))
+        return a.value
 
     def box_moments(self, sys=0):
         """(G, G, 3) device tensor of leaf (cx, cy, M) from the last summarize."""

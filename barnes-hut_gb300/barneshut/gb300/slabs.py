@@ -175,9 +175,11 @@ class SlabSystem:
 
     # -------------------------------------------------------------- create_tree
     def create_tree(self):
-        """Bounding box over all ranks, then every particle to the rank owning its box."""
+        """Bounding box over all ranks, every particle to the rank owning its box, then the
+        near-field halo from the other ranks."""
         s = self.state
         mn, mx = self.comm.extents(s[:, 0], s[:, 1])
+        self.extents = np.array([mn[0], mn[1], mx[0], mx[1]])
         self.bb = square_box(mn[0], mn[1], mx[0], mx[1], self.G)
         kx, ky = box_keys(s[:, 0], s[:, 1], self.bb, self.G)
         dest = owner_of_boxes(kx * self.G + ky, self.ranges)
@@ -188,19 +190,11 @@ class SlabSystem:
         self.box = kx * self.G + ky
         b0, b1 = self.ranges[self.comm.rank]
         assert np.all((self.box >= b0) & (self.box < b1)), "particle outside the rank's boxes"
+        self.halo = self.exchange_halo()
 
-    # ---------------------------------------------------------------- summarize
-    def summarize(self, leaf_moments):
-        """leaf_moments(x, y, m, G, bb) -> (G, G, 6) of the given particles; the whole grid's
-        moments are the sum over ranks."""
-        s = self.state
-        local = leaf_moments(s[:, 0], s[:, 1], s[:, 2], self.G, self.bb)
-        self.leaf = self.comm.sum(local.reshape(-1)).reshape(self.G, self.G, 6)
-
-    # ----------------------------------------------------------------- evaluate
     def exchange_halo(self):
         """(x, y, m) of the particles of the other ranks' boxes that this rank's near field
-        reaches, sorted by box and, within a box, by pid."""
+        reaches, in particle-id order."""
         world, rank = self.comm.world, self.comm.rank
         parts = []
         for r in range(world):
@@ -216,15 +210,31 @@ class SlabSystem:
             h = h[np.argsort(h[:, 3], kind="stable")]
         return h[:, :3]
 
+    def local_particles(self):
+        """x, y, m of the rank's own particles followed by its halo."""
+        s, h = self.state, self.halo
+        return (np.concatenate([s[:, 0], h[:, 0]]), np.concatenate([s[:, 1], h[:, 1]]),
+                np.concatenate([s[:, 2], h[:, 2]]))
+
+    # ---------------------------------------------------------------- summarize
+    def summarize(self, leaf_moments):
+        """leaf_moments(x, y, m, G, bb) -> (G, G, 6) leaf moments of the local particles; the
+        rank keeps those of its own boxes, and the whole grid's moments are their sum over
+        ranks."""
+        x, y, m = self.local_particles()
+        local = np.array(leaf_moments(x, y, m, self.G, self.bb), dtype=np.float64).reshape(-1, 6)
+        b0, b1 = self.ranges[self.comm.rank]
+        local[:b0] = 0.0
+        local[b1:] = 0.0
+        self.leaf = self.comm.sum(local.reshape(-1)).reshape(self.G, self.G, 6)
+
+    # ----------------------------------------------------------------- evaluate
     def evaluate(self, evaluator):
-        """evaluator(x, y, m, targets, bb, leaf) -> (ax, ay) for the local rows `targets`."""
-        halo = self.exchange_halo()
-        s = self.state
-        x = np.concatenate([s[:, 0], halo[:, 0]])
-        y = np.concatenate([s[:, 1], halo[:, 1]])
-        m = np.concatenate([s[:, 2], halo[:, 2]])
-        own = np.arange(len(s))
-        ax, ay = evaluator(x, y, m, own, self.bb, self.leaf)
+        """evaluator(x, y, m, targets, bb, leaf, extents) -> (ax, ay) over the local particles
+        (own then halo) of which the rows `targets` (the own ones) are used."""
+        x, y, m = self.local_particles()
+        own = np.arange(len(self.state))
+        ax, ay = evaluator(x, y, m, own, self.bb, self.leaf, self.extents)
         self.ax, self.ay = np.asarray(ax)[own], np.asarray(ay)[own]
         return self.ax, self.ay
 
@@ -235,3 +245,45 @@ class SlabSystem:
         s[:, 4] = s[:, 4] + self.ay * dt
         s[:, 0] = s[:, 0] + s[:, 3] * dt
         s[:, 1] = s[:, 1] + s[:, 4] * dt
+
+
+class PlanSlab:
+    """The CUDA step on one rank's part of a system: a plan over the rank's own and halo
+    particles whose grid is the whole system's (bh_set_grid) and whose far field comes from the
+    whole grid's leaf moments (bh_set_leaf_moments).  `leaf_moments` (for SlabSystem.summarize)
+    builds the plan and returns its leaf moments; the instance is then the evaluator."""
+
+    def __init__(self, params, device="cuda"):
+        self.params = params
+        self.device = device
+        self.plan = None
+
+    def leaf_moments(self, x, y, m, G, bb):
+        from . import native
+
+        if self.plan is not None:
+            self.plan.close()
+        n = len(x)
+        self.plan = native.Plan([n], [G], self.params, device=self.device)
+        self.plan.set_grid(self._extents)
+        z = np.zeros(n)
+        self.plan.load(x, y, m, z, z)
+        self.plan.create_tree()
+        self.plan.summarize()
+        return self.plan.leaf_moments().cpu().numpy()
+
+    def bind(self, slab):
+        """Take the whole system's extents of the step from `slab` (after its create_tree)."""
+        self._extents = slab.extents
+        return self
+
+    def __call__(self, x, y, m, targets, bb, leaf, extents):
+        self.plan.set_leaf_moments(leaf)
+        self.plan.evaluate()
+        o = self.plan.store()
+        return o["ax"].cpu().numpy(), o["ay"].cpu().numpy()
+
+    def close(self):
+        if self.plan is not None:
+            self.plan.close()
+            self.plan = None

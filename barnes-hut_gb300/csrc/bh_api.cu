@@ -654,6 +654,18 @@ extern "C" int bh_pair_counts(bh_plan *p, long long *near_pairs, long long *far_
     return BH_OK;
 }
 
+extern "C" int bh_corrected_pairs(bh_plan *p, long long *pairs, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (!pairs) return fail(p, BH_ERR_INVALID, "null pairs");
+    cudaStream_t st = (cudaStream_t)stream;
+    Globals g;
+    CK(p, cudaMemcpyAsync(&g, (char *)p->ws + p->o_glob, sizeof(g), cudaMemcpyDeviceToHost, st), "read counts");
+    CK(p, cudaStreamSynchronize(st), "sync");
+    *pairs = (long long)g.corr_pairs;
+    return BH_OK;
+}
+
 extern "C" int bh_direct_sample(bh_plan *p, int sys, const long long *targets, long long nt,
                                 double *ax, double *ay, void *stream) {
     int r = need_bound(p);
@@ -661,6 +673,50 @@ extern "C" int bh_direct_sample(bh_plan *p, int sys, const long long *targets, l
     if (sys < 0 || sys >= p->nsys) return fail(p, BH_ERR_INVALID, "system %d out of range", sys);
     if (nt < 0 || (nt > 0 && (!targets || !ax || !ay))) return fail(p, BH_ERR_INVALID, "bad targets");
     CK(p, launch_direct(p->dev, sys, targets, nt, ax, ay, (cudaStream_t)stream), "direct sample");
+    return BH_OK;
+}
+
+extern "C" int bh_set_grid(bh_plan *p, int sys, const double *ext, void *stream) {
+    if (!p || sys < 0 || sys >= p->nsys) return BH_ERR_INVALID;
+    SysDesc &d = p->sys[sys];
+    if (ext) {
+        if (!(ext[2] >= ext[0]) || !(ext[3] >= ext[1]) || !std::isfinite(ext[0]) || !std::isfinite(ext[1]) ||
+            !std::isfinite(ext[2]) || !std::isfinite(ext[3]))
+            return fail(p, BH_ERR_INVALID, "bh_set_grid: extents must be finite with max >= min");
+        d.fixed_grid = 1;
+        for (int k = 0; k < 4; k++) d.fg_ext[k] = ext[k];
+    } else {
+        d.fixed_grid = 0;
+    }
+    if (p->ws) {  // bound: update the device copy of the system table (graphs replay from it)
+        CK(p, cudaMemcpyAsync((char *)p->ws + p->o_sys + sizeof(SysDesc) * sys, &d, sizeof(SysDesc),
+                              cudaMemcpyHostToDevice, (cudaStream_t)stream), "upload grid");
+        CK(p, cudaStreamSynchronize((cudaStream_t)stream), "sync");
+    }
+    return BH_OK;
+}
+
+extern "C" int bh_leaf_moments(bh_plan *p, int sys, double *out, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (sys < 0 || sys >= p->nsys || !out) return fail(p, BH_ERR_INVALID, "bad leaf_moments args");
+    if (!p->has_tree) return fail(p, BH_ERR_INVALID, "leaf_moments before create_tree/summarize");
+    const SysDesc &d = p->sys[sys];
+    CK(p, cudaMemcpyAsync(out, (char *)p->ws + p->o_mom + 48 * d.coff, 48 * (size_t)d.G * d.G,
+                          cudaMemcpyDeviceToDevice, (cudaStream_t)stream), "copy leaf moments");
+    return BH_OK;
+}
+
+extern "C" int bh_set_leaf_moments(bh_plan *p, int sys, const double *in, void *stream) {
+    int r = need_bound(p);
+    if (r) return r;
+    if (sys < 0 || sys >= p->nsys || !in) return fail(p, BH_ERR_INVALID, "bad set_leaf_moments args");
+    if (!p->has_tree) return fail(p, BH_ERR_INVALID, "set_leaf_moments before create_tree");
+    const SysDesc &d = p->sys[sys];
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(p, cudaMemcpyAsync((char *)p->ws + p->o_mom + 48 * d.coff, in, 48 * (size_t)d.G * d.G,
+                          cudaMemcpyDeviceToDevice, st), "copy leaf moments");
+    CK(p, launch_pyramid(p->dev, st), "pyramid");
     return BH_OK;
 }
 

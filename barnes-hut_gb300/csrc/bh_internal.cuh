@@ -55,6 +55,8 @@ struct SysDesc {
     long long lfoff, lnoff;      // first far / near list slot of the system's groups
     int lfcap, lncap;            // far / near list slots per group
     long long ooff;              // first entry of the system's box-origin table (G x, then G y)
+    int fixed_grid;              // 1: the square box comes from fg_ext, not from the particles
+    double fg_ext[4];            // min x, min y, max x, max y of the whole system (bh_set_grid)
 };
 
 struct SysDyn {
@@ -73,6 +75,7 @@ struct Globals {
     unsigned long long near_pairs, far_pairs;
     unsigned int item_next;   // force work queue head (zeroed before each force launch)
     unsigned int item_next2;  // learned-correction work queue head
+    unsigned long long corr_pairs;  // (target, cell) pairs the learned correction evaluated
 };
 
 struct DevPlan {
@@ -324,6 +327,8 @@ cudaError_t launch_walk_items(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_records(const DevPlan &d, bool second, cudaStream_t st);
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st);
+// the pyramid levels above the leaves and the cell records, from the leaf moments
+cudaError_t launch_pyramid(const DevPlan &d, cudaStream_t st);
 // ev (optional): two events recorded on st right before and after the force kernel proper
 cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st,
                          const cudaEvent_t *ev = nullptr);

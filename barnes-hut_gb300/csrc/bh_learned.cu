@@ -304,6 +304,7 @@ __global__ void __launch_bounds__(LT) k_learned_correct(DevPlan d, float th2_lo,
         }
         __syncthreads();
         const long long npairs = (long long)ig.T * nb;
+        if (tid == 0) atomicAdd(&d.glob->corr_pairs, (unsigned long long)npairs);
         for (long long p0 = 0; p0 < npairs && ok; p0 += 128) {
             const long long p = p0 + tid;
             float f[16];

@@ -30,6 +30,7 @@ __global__ void k_prologue(DevPlan d) {
         d.glob->epoch += 1;
         d.glob->near_pairs = 0;
         d.glob->far_pairs = 0;
+        d.glob->corr_pairs = 0;
     }
     if (tid < d.nsys) {
         d.dyn[tid].bbmin[0] = d.dyn[tid].bbmin[1] = ~0ull;
@@ -112,6 +113,12 @@ __device__ void bbox_finalize_sys(const DevPlan &d, int s) {
     SysDyn &dy = d.dyn[s];
     double mnx = unord_bits(dy.bbmin[0]), mny = unord_bits(dy.bbmin[1]);
     double mxx = unord_bits(dy.bbmax[0]), mxy = unord_bits(dy.bbmax[1]);
+    if (d.sys[s].fixed_grid) {  // part of a larger system: the whole system's extents
+        mnx = d.sys[s].fg_ext[0];
+        mny = d.sys[s].fg_ext[1];
+        mxx = d.sys[s].fg_ext[2];
+        mxy = d.sys[s].fg_ext[3];
+    }
     double step;
     square_bbox(mnx, mny, mxx, mxy, d.sys[s].G, &step);
     dy.minx = mnx;
@@ -644,6 +651,9 @@ cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
 }
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st) {
     if (d.n_total > 0) k_leaf_moments<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
+    return launch_pyramid(d, st);
+}
+cudaError_t launch_pyramid(const DevPlan &d, cudaStream_t st) {
     for (int l = 1; l < d.Lmax; l++) {
         // the level's cell count over all systems is known on the host: one thread per cell
         // while the level is large, then one CTA for all the remaining (small) levels

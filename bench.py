@@ -349,8 +349,11 @@ def learned_benchmark(torch, dev, batch, steps=20, n_pairs=10_000_000,
             if ref is None:
                 ref = plan.direct_sample(tgt)
             err = _rel_rms_t(torch, o["ax"][idx], o["ay"][idx], *ref)
+            near, far = plan.pair_counts()
             rows.append({"kind": kind, "theta": theta, "ms_per_step": ms,
                          "particle_steps_per_s": n / (ms / 1e3), "rel_rms_vs_fp64_direct": err,
+                         "pairs_near": near, "pairs_far": far,
+                         "pairs_corrected": plan.corrected_pairs() if flags else 0,
                          "device_error_flags": plan.error_flags(raise_on_error=False)})
             plan.close()
     plain = [r for r in rows if r["kind"] == "plain"]

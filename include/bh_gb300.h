@@ -188,11 +188,29 @@ int bh_error_flags(bh_plan *plan, unsigned *flags, void *stream);
  * force kernel: near = particle-particle, far = particle-cell (synchronises). */
 int bh_pair_counts(bh_plan *plan, long long *near_pairs, long long *far_pairs, void *stream);
 
+/* (target, cell) pairs the learned correction evaluated in the last step or evaluate
+ * (synchronises); no reference counterpart. */
+int bh_corrected_pairs(bh_plan *plan, long long *pairs, void *stream);
+
 /* Leaf-box centres of mass of system `sys` from the last bh_summarize, in the
  * reference's layout: out[(gx * G + gy) * 3 + {0, 1, 2}] = (cx, cy, M), zeros
  * for an empty box (device array of G*G*3 doubles).  Replaces reading the
  * COM grid d_COMs (singlegpu.py:38,69-77; gpu/grid.py:78-114). */
 int bh_box_moments(bh_plan *plan, int sys, double *out, void *stream);
+
+/* A plan over one rank's part of a larger system (the box-slab step that replaces
+ * implementations/multigpu.py:264-310).  bh_set_grid fixes system `sys`'s grid: from the next
+ * bh_create_tree on, the square box comes from ext[4] = {min x, min y, max x, max y} of the
+ * whole system (host doubles; the all-reduce of the ranks' extents) instead of from the
+ * plan's own particles; ext = NULL returns to the plan's own box.  bh_leaf_moments copies the
+ * last summarize's leaf moments of `sys` -- per box, x-major, (M, Sx, Sy, Sxx, Sxy, Syy) about
+ * the box origin, FP64 -- into out (device, G*G*6 doubles); bh_set_leaf_moments replaces them
+ * with `in` (device, same layout: the sum over ranks of their own boxes' moments) and rebuilds
+ * the pyramid levels above the leaves and the cell records, so the next bh_evaluate takes its
+ * far field from the whole system (multigpu.py:149-155, 303-306). */
+int bh_set_grid(bh_plan *plan, int sys, const double *ext, void *stream);
+int bh_leaf_moments(bh_plan *plan, int sys, double *out, void *stream);
+int bh_set_leaf_moments(bh_plan *plan, int sys, const double *in, void *stream);
 
 /* Square bounding box of system `sys` from the last bh_create_tree into host
  * out[5] = {min_x, min_y, step, grid_dim, n} (synchronises).  Replaces the

@@ -4,8 +4,11 @@
   plain step at the same opening angle (relative RMS <= 1e-6).
 * Gain: a network trained on pairs from two seeded cluster-mixture systems,
   applied at theta = 0.8 on a third system, lowers the relative RMS force error
-  (against the FP64 direct sum on 4,096 targets) below plain theta = 0.8.  The
-  measured errors of plain 0.5, plain 0.8 and learned 0.8 are printed.
+  (against the FP64 direct sum on 4,096 targets) below plain theta = 0.8.
+* Matched error: the learned step at theta = 0.8 is at least as accurate as a
+  plain step at theta <= 0.7 (the largest such plain angle is printed), but not
+  as accurate as plain theta = 0.5.  Whether it is faster than the plain step of
+  the same accuracy is measured by the benchmark (its learned Pareto).
 """
 import numpy as np
 import pytest
@@ -72,7 +75,18 @@ def test_learned_correction_gain():
     e08 = rel_rms(ax8[idx], ay8[idx], rx, ry)
     _, axl, ayl = accel(test, G, 0.8, mlp)
     el = rel_rms(axl[idx], ayl[idx], rx, ry)
-    print(f"relative RMS force error: plain 0.5 {e05:.3e}, plain 0.8 {e08:.3e}, "
-          f"learned 0.8 {el:.3e} (training pairs {info['pairs']}, rel. MSE {info['relative_mse']:.3f}, "
-          f"quadrupole-only rel. MSE {info['quadrupole_relative_mse']:.3f})")
+    # matched error: the largest plain opening angle at least as accurate as the learned step
+    plain = {0.5: e05, 0.8: e08}
+    for th in (0.6, 0.7):
+        _, axp, ayp = accel(test, G, th)
+        plain[th] = rel_rms(axp[idx], ayp[idx], rx, ry)
+    matched = max([th for th, e in plain.items() if e <= el], default=None)
+    print(f"relative RMS force error: plain {', '.join(f'{t} {e:.3e}' for t, e in sorted(plain.items()))}; "
+          f"learned 0.8 {el:.3e}, as accurate as plain theta {matched} (training pairs {info['pairs']}, "
+          f"rel. MSE {info['relative_mse']:.3f}, quadrupole-only rel. MSE "
+          f"{info['quadrupole_relative_mse']:.3f})")
     assert el < 0.9 * e08, (e05, e08, el)
+    # the correction at theta 0.8 is worth a plain step at theta <= 0.7, not yet plain 0.5's accuracy
+    # (the step-time side of the comparison is the benchmark's learned Pareto)
+    assert matched is not None and matched <= 0.7, (plain, el)
+    assert el > e05, (e05, el)

@@ -73,7 +73,7 @@ def _worker(rank, ws, port, case, out_dir):
         comm = slabs.SlabComm("cpu")
         sysl = slabs.SlabSystem(state, G, comm, theta=theta, group_dim=TG)
 
-        def evaluator(xa, ya, ma, targets, bb, leaf):
+        def evaluator(xa, ya, ma, targets, bb, leaf, extents):
             ax, ay, _, _ = oracle.theta_evaluate_part(xa, ya, ma, G, bb, leaf, targets, TG=TG,
                                                       theta=theta, eps2=eps2, cutoff=cut,
                                                       dense_min=dmin, quad_min=qmin)
