@@ -23,15 +23,15 @@ struct bh_plan {
     bh_params params;
     int nsys = 0;
     std::vector<SysDesc> sys;
-    std::vector<long long> poff, boff, coff, goff, lvl;
+    std::vector<long long> poff, boff, coff, goff, toff, lvl;
     int Lmax = 1;
     long long n_total = 0, B_total = 0, C_total = 0, NG_total = 0;
     long long org_total = 0;  // entries of the box-origin tables (2 G per system)
     // workspace layout (byte offsets)
     size_t ws_bytes = 0;
-    size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_lvl;
+    size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_toff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
-    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_tiles, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
+    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_sst, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
         o_rec2, o_org, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk, o_qcnt;
     bool stream = false;  // theta-mode interaction lists built once per group and streamed
     int chunk = TARGET_CHUNK;
@@ -135,6 +135,7 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->boff.assign(nsys + 1, 0);
     p->coff.assign(nsys + 1, 0);
     p->goff.assign(nsys + 1, 0);
+    p->toff.assign(nsys + 1, 0);
     for (int s = 0; s < nsys; s++) {
         if (n[s] < 0 || n[s] > (1LL << 30)) return bad("particle count out of range [0, 2^30]");
         int G = grid_dim && grid_dim[s] > 0 ? grid_dim[s] : bh_grid_dim(n[s], 1000);
@@ -175,10 +176,13 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
         d.boff = p->boff[s];
         d.coff = p->coff[s];
         d.goff = p->goff[s];
+        d.tps = (G + SUM_TILE - 1) / SUM_TILE;
+        d.toff = p->toff[s];
         p->poff[s + 1] = p->poff[s] + n[s];
         p->boff[s + 1] = p->boff[s] + (long long)G * G;
         p->coff[s + 1] = p->coff[s] + cells;
         p->goff[s + 1] = p->goff[s] + (long long)d.NGs * d.NGs;
+        p->toff[s + 1] = p->toff[s] + (long long)d.tps * d.tps;
         if (L > p->Lmax) p->Lmax = L;
     }
     p->n_total = p->poff[nsys];
@@ -241,6 +245,7 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_boff = take(sizeof(long long) * (nsys + 1));
     p->o_coff = take(sizeof(long long) * (nsys + 1));
     p->o_goff = take(sizeof(long long) * (nsys + 1));
+    p->o_toff = take(sizeof(long long) * (nsys + 1));
     p->o_lvl = take(sizeof(long long) * p->lvl.size());
     for (int b = 0; b < 2; b++) {
         p->o_X[b] = take(8 * N);
@@ -260,7 +265,7 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_counts = take(4 * B);
     p->o_qcnt = take(16 * B);
     p->o_bstart = take(4 * (B + 1));
-    p->o_tiles = take(4 * (B / 4096 + 2));
+    p->o_sst = take(8 * (B / SCAN_TILE + 2 + (size_t)p->NG_total / SCAN_TILE + 2 + (size_t)p->NG_total / SITEM_TILE + 2));
     p->o_icnt = take(4 * (size_t)p->NG_total);
     p->o_ioff = take(4 * ((size_t)p->NG_total + 1));
     p->o_igrp = take(4 * ((size_t)p->NG_total + N / p->chunk + 1));
@@ -324,6 +329,8 @@ static void fill_dev(bh_plan *p) {
     d.boff_tab = (const long long *)(w + p->o_boff);
     d.coff_tab = (const long long *)(w + p->o_coff);
     d.goff_tab = (const long long *)(w + p->o_goff);
+    d.toff_tab = (const long long *)(w + p->o_toff);
+    d.T_total = p->toff[p->nsys];
     d.lvl_tab = (const long long *)(w + p->o_lvl);
     for (int l = 0; l < p->Lmax && l < MAX_LEVELS; l++) d.lvl_cells[l] = p->lvl[(size_t)l * (p->nsys + 1) + p->nsys];
     for (int b = 0; b < 2; b++) {
@@ -344,7 +351,9 @@ static void fill_dev(bh_plan *p) {
     d.counts = (int *)(w + p->o_counts);
     d.qcounts = (int *)(w + p->o_qcnt);
     d.box_start = (int *)(w + p->o_bstart);
-    d.tile_sums = (int *)(w + p->o_tiles);
+    d.sst_box = (unsigned long long *)(w + p->o_sst);
+    d.sst_witem = d.sst_box + p->B_total / SCAN_TILE + 2;
+    d.sst_sitem = d.sst_witem + p->NG_total / SCAN_TILE + 2;
     d.item_cnt = (int *)(w + p->o_icnt);
     d.item_off = (int *)(w + p->o_ioff);
     d.item_group = (int *)(w + p->o_igrp);
@@ -401,6 +410,7 @@ extern "C" int bh_bind(bh_plan *p, void *workspace, size_t bytes, void *stream) 
     CK(p, cudaMemcpyAsync(w + p->o_boff, p->boff.data(), 8 * (p->nsys + 1), cudaMemcpyHostToDevice, st), "upload boff");
     CK(p, cudaMemcpyAsync(w + p->o_coff, p->coff.data(), 8 * (p->nsys + 1), cudaMemcpyHostToDevice, st), "upload coff");
     CK(p, cudaMemcpyAsync(w + p->o_goff, p->goff.data(), 8 * (p->nsys + 1), cudaMemcpyHostToDevice, st), "upload goff");
+    CK(p, cudaMemcpyAsync(w + p->o_toff, p->toff.data(), 8 * (p->nsys + 1), cudaMemcpyHostToDevice, st), "upload toff");
     CK(p, cudaMemcpyAsync(w + p->o_lvl, p->lvl.data(), 8 * p->lvl.size(), cudaMemcpyHostToDevice, st), "upload lvl");
     CK(p, cudaMemsetAsync(w + p->o_dyn, 0, sizeof(SysDyn) * p->nsys, st), "zero dyn");
     CK(p, cudaMemsetAsync(w + p->o_glob, 0, sizeof(Globals), st), "zero globals");
@@ -606,18 +616,12 @@ extern "C" int bh_force_kernel_ms(bh_plan *p, float *ms) {
 
 extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     if (!p || !count) return BH_ERR_INVALID;
-    // prologue, 3 box-scan phases, pyramid levels, records; with particles also bbox, bbox
-    // finalize, place, scatter, leaf moments, force (and before it, when streaming, the list
-    // build and the two kernels of the heaviest-first item order); work items (count, 3 scan
-    // phases, fill) for the walk or the learned correction, and for list streaming
-    // pyramid: one launch per level while its cells exceed 256, then one for the remaining levels
-    int pyr = 0;
-    for (int l = 1; l < p->Lmax; l++) {
-        pyr++;
-        if (p->lvl[(size_t)l * (p->nsys + 1) + p->nsys] <= 256) break;
-    }
+    // prologue, box scan, summarize; with particles also bbox (which finalises the box), place,
+    // scatter, force (and before it, when streaming, the list build and the two kernels of the
+    // heaviest-first item order); work items: count, scan, fill for the walk or the learned
+    // correction, one kernel for list streaming
     const bool walk_items = !p->stream || (p->params.flags & BH_FLAG_LEARNED);
-    *count = 1 + 3 + (walk_items ? 5 : 0) + pyr + 1 + (p->n_total > 0 ? 6 : 0) + (p->stream ? 5 : 0) +
+    *count = 1 + 1 + (walk_items ? 3 : 0) + 1 + (p->n_total > 0 ? 4 : 0) + (p->stream ? 1 : 0) +
              (p->stream && p->n_total > 0 ? 3 : 0);
     return BH_OK;
 }

@@ -458,12 +458,16 @@ k_force(DevPlan d, int tick, int accumulate) {
                     bx = (int)(b / G);
                     byy = (int)(b - (long long)bx * G);
                     long long gb = sd.boff + b;
-                    if (d.box_start[gb + 1] > d.box_start[gb]) {
-                        if (abs(bx - gx0) <= 1 && abs(byy - gy0) <= 1) {
+                    // near boxes by their particles, far boxes by their moments (a plan over one
+                    // rank's part of a system holds the other boxes' moments, not their particles)
+                    if (abs(bx - gx0) <= 1 && abs(byy - gy0) <= 1) {
+                        if (d.box_start[gb + 1] > d.box_start[gb]) {
                             kind = 2;
                             id = (int)gb;
-                        } else {
-                            float4 rr = d.rec[sd.coff + b];
+                        }
+                    } else {
+                        float4 rr = d.rec[sd.coff + b];
+                        if (rr.z > 0.f) {
                             rx = __fadd_rn(__fmul_rn((float)(bx - gx0), step_f), rr.x);
                             ry = __fadd_rn(__fmul_rn((float)(byy - gy0), step_f), rr.y);
                             M = rr.z;

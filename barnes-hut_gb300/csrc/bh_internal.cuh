@@ -40,6 +40,9 @@ constexpr int FORCE_THREADS = 128;
 constexpr int FORCE_R = 4;                                   // targets per thread (FP32)
 constexpr int TARGET_CHUNK = FORCE_THREADS * FORCE_R;        // targets per work item
 constexpr int FRONTIER_CAP = 512;                            // traversal frontier per level
+constexpr int SCAN_TILE = 4096;   // counts per tile of the single-pass scans (256 threads x 16)
+constexpr int SITEM_TILE = 256;   // target groups per tile of the streaming work-item kernel
+constexpr int SUM_TILE = 16;      // leaf boxes per side of a summarize tile (pyramid levels 0..4)
 constexpr int STREAM_CHUNK = 128;  // targets per work item of the list-streaming force kernel
 constexpr int LIST_MAX_G = 16384;  // largest G of the list-streaming path (32-bit group indices)
 constexpr int ITEM_BUCKETS = 32;   // log2 cost buckets of the heaviest-first item order
@@ -55,6 +58,8 @@ struct SysDesc {
     long long lfoff, lnoff;      // first far / near list slot of the system's groups
     int lfcap, lncap;            // far / near list slots per group
     long long ooff;              // first entry of the system's box-origin table (G x, then G y)
+    int tps;                     // summarize tiles (SUM_TILE x SUM_TILE leaf boxes) per side
+    long long toff;              // first summarize tile of the system
     int fixed_grid;              // 1: the square box comes from fg_ext, not from the particles
     double fg_ext[4];            // min x, min y, max x, max y of the whole system (bh_set_grid)
 };
@@ -67,6 +72,7 @@ struct SysDyn {
     float minx_f, miny_f;         // the origin rounded to float
     float inv_step_f;             // 1 / step rounded to float
     float key_tol;                // bound on |float quotient - exact quotient| (box edges)
+    unsigned int tiles_done;      // summarize tiles finished this step (the last one resets it)
 };
 
 struct Globals {
@@ -76,6 +82,9 @@ struct Globals {
     unsigned int item_next;   // force work queue head (zeroed before each force launch)
     unsigned int item_next2;  // learned-correction work queue head
     unsigned long long corr_pairs;  // (target, cell) pairs the learned correction evaluated
+    unsigned int scan_ticket[3];    // next tile of each single-pass scan (its last tile resets it)
+    unsigned int scan_gen[3];       // generation of each scan's tile states (its last tile bumps it)
+    unsigned int bbox_done;         // bounding-box blocks finished (the last one finalises)
 };
 
 struct DevPlan {
@@ -88,6 +97,8 @@ struct DevPlan {
     const long long *boff_tab;  // nsys + 1 box offsets
     const long long *coff_tab;  // nsys + 1 cell offsets
     const long long *goff_tab;  // nsys + 1 group offsets
+    const long long *toff_tab;  // nsys + 1 summarize-tile offsets
+    long long T_total;          // summarize tiles over all systems
     const long long *lvl_tab;   // Lmax x (nsys + 1): prefix of level-l cells over systems
     long long lvl_cells[MAX_LEVELS];  // level-l cells over all systems (host copy, sizes grids)
     double *X[2], *Y[2], *VX[2], *VY[2], *M[2];
@@ -98,7 +109,10 @@ struct DevPlan {
                  // packed near-field record (offsets from the box origin; box coordinates),
                  // staged into shared memory by bulk copies
     int *key, *slot, *skey;
-    int *counts, *box_start, *tile_sums;
+    int *counts, *box_start;
+    // single-pass scans (decoupled look-back): per-tile states of the box scan, the walk items'
+    // scan and the streaming items' scan (generation << 34 | flag << 32 | value)
+    unsigned long long *sst_box, *sst_witem, *sst_sitem;
     int *qcounts;  // per box, particles in each quadrant (x half * 2 + y half); a box's particles
                    // are stored quadrant by quadrant
     int *item_cnt, *item_off, *item_group;  // force work items (group, target chunk)

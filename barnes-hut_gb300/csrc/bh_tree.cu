@@ -1,17 +1,17 @@
 // bh_tree.cu -- create_tree and summarize kernels.
 //
-// create_tree = prologue -> bbox -> place -> scan (3 phases) -> scatter.
+// create_tree = prologue -> bbox (its last block squares the box) -> place -> scan (one pass)
+//   -> scatter -> work items (one pass).
 //   Replaces set_particles_bounding_box (python-bh/barneshut/implementations/base.py:211-239),
 //   g_place_particles, g_calculate_box_cumm, g_sort_particles
 //   (python-bh/barneshut/kernels/grid_decomposition/gpu/grid.py:15-76).
-// summarize = leaf moments (segmented warp reduction) -> pyramid levels -> records.
+// summarize = one kernel over tiles of leaf boxes: leaf moments, pyramid, records.
 //   Replaces g_summarize (gpu/grid.py:78-114) and calc_COM (internals/cloud.py:9-17).
 #include "bh_internal.cuh"
 
 namespace bh {
 
 constexpr int TPB = 256;
-constexpr int SCAN_TILE = 4096;  // counts per scan tile (256 threads x 16)
 
 static inline unsigned grid_for(long long n, int tpb, long long cap) {
     long long b = (n + tpb - 1) / tpb;
@@ -21,8 +21,8 @@ static inline unsigned grid_for(long long n, int tpb, long long cap) {
 }
 
 // ----------------------------------------------------------------- prologue
-// Zero the box histogram and the leaf moments, reset the bounding-box
-// accumulators and pair counters, advance the state epoch.
+// Zero the box and quadrant histograms, reset the bounding-box accumulators and
+// pair counters, advance the state epoch.
 __global__ void k_prologue(DevPlan d) {
     long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long stride = (long long)gridDim.x * blockDim.x;
@@ -39,11 +39,40 @@ __global__ void k_prologue(DevPlan d) {
     for (long long b = tid; b < d.B_total; b += stride) {
         d.counts[b] = 0;
         reinterpret_cast<int4 *>(d.qcounts)[b] = make_int4(0, 0, 0, 0);
-        int s = find_seg(d.boff_tab, d.nsys, b);
-        long long c = d.sys[s].coff + (b - d.sys[s].boff);
-        double *q = d.mom + 6 * c;
-#pragma unroll
-        for (int k = 0; k < 6; k++) q[k] = 0.0;
+    }
+}
+
+// One thread per system: the square bounding box (helpers/grid.py:10-26), its
+// box edge step = edge / G (base.py:233) and 1 / step, once per step.
+__device__ void bbox_finalize_sys(const DevPlan &d, int s) {
+    SysDyn &dy = d.dyn[s];
+    double mnx = unord_bits(dy.bbmin[0]), mny = unord_bits(dy.bbmin[1]);
+    double mxx = unord_bits(dy.bbmax[0]), mxy = unord_bits(dy.bbmax[1]);
+    if (d.sys[s].fixed_grid) {  // part of a larger system: the whole system's extents
+        mnx = d.sys[s].fg_ext[0];
+        mny = d.sys[s].fg_ext[1];
+        mxx = d.sys[s].fg_ext[2];
+        mxy = d.sys[s].fg_ext[3];
+    }
+    double step;
+    square_bbox(mnx, mny, mxx, mxy, d.sys[s].G, &step);
+    dy.minx = mnx;
+    dy.miny = mny;
+    dy.step = step;
+    dy.inv_step = step > 0.0 ? 1.0 / step : 0.0;
+    // float key estimate: p and mn rounded to float (relative error 2^-24 each), their
+    // difference and the product with float(1 / step) rounded (2^-24 each); in box edges the
+    // error is at most ((|p| + |mn|) / step + 2 q) 2^-24 <= ((2 |mn| + |edge|) / step + 2 G) 2^-24;
+    // a factor 4 covers the remaining roundings
+    dy.minx_f = __double2float_rn(mnx);
+    dy.miny_f = __double2float_rn(mny);
+    dy.inv_step_f = __double2float_rn(dy.inv_step);
+    if (step > 0.0 && isfinite(step)) {
+        const double am = fmax(fabs(mnx), fabs(mny)), G = (double)d.sys[s].G;
+        const double tol = 4.0 * ((2.0 * am + G * step) / step + 2.0 * G) * 5.9604644775390625e-8;
+        dy.key_tol = tol < 0.25 ? (float)tol : 1.f;
+    } else {
+        dy.key_tol = 1.f;  // the FP64 key for every particle
     }
 }
 
@@ -105,56 +134,29 @@ __global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
         }
         __syncthreads();
     }
-}
-
-// One thread per system: the square bounding box (helpers/grid.py:10-26), its
-// box edge step = edge / G (base.py:233) and 1 / step, once per step.
-__device__ void bbox_finalize_sys(const DevPlan &d, int s) {
-    SysDyn &dy = d.dyn[s];
-    double mnx = unord_bits(dy.bbmin[0]), mny = unord_bits(dy.bbmin[1]);
-    double mxx = unord_bits(dy.bbmax[0]), mxy = unord_bits(dy.bbmax[1]);
-    if (d.sys[s].fixed_grid) {  // part of a larger system: the whole system's extents
-        mnx = d.sys[s].fg_ext[0];
-        mny = d.sys[s].fg_ext[1];
-        mxx = d.sys[s].fg_ext[2];
-        mxy = d.sys[s].fg_ext[3];
-    }
-    double step;
-    square_bbox(mnx, mny, mxx, mxy, d.sys[s].G, &step);
-    dy.minx = mnx;
-    dy.miny = mny;
-    dy.step = step;
-    dy.inv_step = step > 0.0 ? 1.0 / step : 0.0;
-    // float key estimate: p and mn rounded to float (relative error 2^-24 each), their
-    // difference and the product with float(1 / step) rounded (2^-24 each); in box edges the
-    // error is at most ((|p| + |mn|) / step + 2 q) 2^-24 <= ((2 |mn| + |edge|) / step + 2 G) 2^-24;
-    // a factor 4 covers the remaining roundings
-    dy.minx_f = __double2float_rn(mnx);
-    dy.miny_f = __double2float_rn(mny);
-    dy.inv_step_f = __double2float_rn(dy.inv_step);
-    if (step > 0.0 && isfinite(step)) {
-        const double am = fmax(fabs(mnx), fabs(mny)), G = (double)d.sys[s].G;
-        const double tol = 4.0 * ((2.0 * am + G * step) / step + 2.0 * G) * 5.9604644775390625e-8;
-        dy.key_tol = tol < 0.25 ? (float)tol : 1.f;
-    } else {
-        dy.key_tol = 1.f;  // the FP64 key for every particle
-    }
-}
-
-// One CTA per system: thread 0 squares the bounding box and derives the grid; then the CTA
-// tabulates the box origins mn + k step (FP64), which the scatter reads instead of forming
-// them per particle on the slow FP64 pipe.
-__global__ void k_bbox_finalize(DevPlan d) {
-    const int s = blockIdx.x;
-    SysDyn &dy = d.dyn[s];
-    if (d.sys[s].n == 0) return;
-    if (threadIdx.x == 0) bbox_finalize_sys(d, s);
+    // the last block to finish squares every system's box and tabulates the box origins
+    __shared__ unsigned ticket;
+    __threadfence();
     __syncthreads();
-    const int G = d.sys[s].G;
-    double *org = d.org + d.sys[s].ooff;
-    for (int k = threadIdx.x; k < G; k += blockDim.x) {
-        org[k] = box_origin(dy.minx, k, dy.step);
-        org[G + k] = box_origin(dy.miny, k, dy.step);
+    if (threadIdx.x == 0) ticket = atomicAdd(&d.glob->bbox_done, 1u);
+    __syncthreads();
+    if (ticket != gridDim.x - 1) return;
+    __threadfence();
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < d.nsys; s++)
+            if (d.sys[s].n > 0) bbox_finalize_sys(d, s);
+        d.glob->bbox_done = 0u;
+    }
+    __syncthreads();
+    for (int s = 0; s < d.nsys; s++) {
+        if (d.sys[s].n == 0) continue;
+        const SysDyn &dy = d.dyn[s];
+        const int G = d.sys[s].G;
+        double *org = d.org + d.sys[s].ooff;
+        for (int k = threadIdx.x; k < G; k += blockDim.x) {
+            org[k] = box_origin(dy.minx, k, dy.step);
+            org[G + k] = box_origin(dy.miny, k, dy.step);
+        }
     }
 }
 
@@ -206,10 +208,16 @@ __global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
 }
 
 // --------------------------------------------------------------------- scan
-// Exclusive scan of the box histogram (all systems concatenated; systems are
-// laid out in particle order, so the global prefix is the global particle
-// index of each box's first particle).  Phase 1: per-tile sums; phase 2: one
-// block scans the tile sums; phase 3: per-tile scan plus carry.
+// Exclusive scans in one pass (decoupled look-back): tiles are numbered in the order their CTAs
+// start (a ticket), so every tile's predecessors are already running; a tile publishes its sum,
+// then its inclusive prefix once it has read its predecessors' (a predecessor's inclusive prefix
+// ends the look-back).  A tile state is gen << 34 | flag << 32 | value (flag 1 = the tile's sum,
+// 2 = inclusive prefix); a state of another generation is not yet written, and the scan's last
+// tile bumps the generation, so the states need no clearing between scans.  Waits are bounded:
+// on timeout the tile raises BH_DEV_WAIT_TIMEOUT and carries on (the result is then invalid).
+constexpr unsigned long long SST_AGG = 1ull << 32, SST_PRE = 2ull << 32;
+constexpr long long LOOKBACK_SPIN = 1ll << 22;
+
 __device__ __forceinline__ int block_excl_scan(int v, int *sh, int *total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int x = v;
@@ -234,60 +242,102 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh, int *total) {
     return pre;
 }
 
-// Generic over (in, out, n): out[i] = sum(in[0..i)), out[n] = total.
-__global__ void __launch_bounds__(TPB) k_scan_tiles(const int *in, long long n, int *tiles) {
+// Warp 0 of the CTA: publish the tile's sum `agg`, look back, publish the inclusive prefix and
+// return the tile's exclusive prefix (to lane 0; the caller broadcasts through shared memory).
+__device__ int lookback(unsigned long long *state, int tile, unsigned gen, int agg, Globals *glob) {
+    const int lane = threadIdx.x & 31;
+    volatile unsigned long long *vs = state;
+    const unsigned long long tag = (unsigned long long)(gen & 0x3FFFFFFFu) << 34;
+    if (tile == 0) {
+        if (lane == 0) {
+            __threadfence();
+            vs[0] = tag | SST_PRE | (unsigned)agg;
+        }
+        return 0;
+    }
+    if (lane == 0) {
+        __threadfence();
+        vs[tile] = tag | SST_AGG | (unsigned)agg;
+    }
+    int excl = 0;
+    int k = tile - 1;  // the nearest predecessor not yet read
+    bool timed_out = false;
+    while (k >= 0) {
+        const int idx = k - lane;
+        unsigned long long st = idx >= 0 ? 0ull : (tag | SST_PRE);  // before tile 0: prefix 0
+        long long it = 0;
+        for (;;) {
+            if (idx >= 0) st = vs[idx];
+            const bool ready = (st >> 34) == (tag >> 34) && (st & (3ull << 32)) != 0;
+            if (__all_sync(0xffffffffu, ready)) break;
+            if (++it > LOOKBACK_SPIN) {
+                timed_out = true;
+                break;
+            }
+        }
+        if (timed_out) break;
+        const unsigned pre_mask = __ballot_sync(0xffffffffu, (st & SST_PRE) == SST_PRE);
+        const int stop = pre_mask ? __ffs(pre_mask) - 1 : 31;  // nearest inclusive prefix
+        int v = lane <= stop ? (int)(unsigned)(st & 0xFFFFFFFFull) : 0;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        excl += v;
+        if (pre_mask) break;
+        k -= 32;
+    }
+    if (lane == 0) {
+        if (timed_out) raise_err(glob, 8u /*BH_DEV_WAIT_TIMEOUT*/);
+        __threadfence();
+        vs[tile] = tag | SST_PRE | (unsigned)(excl + agg);
+    }
+    return excl;
+}
+
+// out[i] = sum(in[0..i)) for i < n, out[n] = sum(in[0..n)); scan k of the plan's three.
+__global__ void __launch_bounds__(TPB) k_scan_lookback(const int *in, long long n, int *out,
+                                                      unsigned long long *state, Globals *glob, int k) {
     __shared__ int sh[32];
-    long long t0 = (long long)blockIdx.x * SCAN_TILE;
-    int s = 0;
-    for (int k = threadIdx.x; k < SCAN_TILE; k += TPB) {
-        long long b = t0 + k;
-        if (b < n) s += in[b];
+    __shared__ int s_tile, s_excl;
+    __shared__ unsigned s_gen;
+    const long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE > 0 ? (n + SCAN_TILE - 1) / SCAN_TILE : 1;
+    if (threadIdx.x == 0) {
+        s_tile = (int)atomicAdd(&glob->scan_ticket[k], 1u);
+        s_gen = *(volatile unsigned *)&glob->scan_gen[k];
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    const long long b0 = (long long)tile * SCAN_TILE + (long long)threadIdx.x * 16;
+    int v[16], sum = 0;
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        v[q] = b0 + q < n ? in[b0 + q] : 0;
+        sum += v[q];
     }
     int tot;
-    block_excl_scan(s, sh, &tot);
-    if (threadIdx.x == 0) tiles[blockIdx.x] = tot;
-}
-
-__global__ void __launch_bounds__(1024) k_scan_sums(int *tiles, int ntiles, int *out, long long n) {
-    __shared__ int sh[32];
-    int carry = 0;
-    for (int t0 = 0; t0 < ntiles; t0 += 1024) {
-        int t = t0 + threadIdx.x;
-        int v = t < ntiles ? tiles[t] : 0;
-        int tot;
-        int p = block_excl_scan(v, sh, &tot);
-        if (t < ntiles) tiles[t] = carry + p;
-        carry += tot;
+    int pre = block_excl_scan(sum, sh, &tot);
+    if (threadIdx.x < 32) {
+        const int e = lookback(state, tile, s_gen, tot, glob);
+        if (threadIdx.x == 0) s_excl = e;
     }
-    if (threadIdx.x == 0) out[n] = carry;
-}
-
-__global__ void __launch_bounds__(TPB) k_scan_apply(const int *in, long long n, const int *tiles,
-                                                   int *out) {
-    __shared__ int sh[32];
-    long long t0 = (long long)blockIdx.x * SCAN_TILE;
-    // each thread owns 16 consecutive entries
-    long long b0 = t0 + (long long)threadIdx.x * 16;
-    int v[16], s = 0;
+    __syncthreads();
+    pre += s_excl;
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
-        v[k] = (b0 + k < n) ? in[b0 + k] : 0;
-        s += v[k];
+    for (int q = 0; q < 16; q++) {
+        if (b0 + q < n) out[b0 + q] = pre;
+        pre += v[q];
     }
-    int pre = block_excl_scan(s, sh, nullptr) + tiles[blockIdx.x];
-#pragma unroll
-    for (int k = 0; k < 16; k++) {
-        if (b0 + k < n) out[b0 + k] = pre;
-        pre += v[k];
+    if (tile == ntiles - 1 && threadIdx.x == 0) {
+        out[n] = s_excl + tot;
+        glob->scan_ticket[k] = 0u;  // every tile has its ticket: ready for the next scan
+        glob->scan_gen[k] = s_gen + 1u;
     }
 }
 
-static cudaError_t scan_excl(const int *in, int *out, long long n, int *tiles, cudaStream_t st) {
-    int ntiles = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
+static cudaError_t scan_excl(const int *in, int *out, long long n, unsigned long long *state,
+                             Globals *glob, int k, cudaStream_t st) {
+    long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (ntiles < 1) ntiles = 1;
-    k_scan_tiles<<<ntiles, TPB, 0, st>>>(in, n, tiles);
-    k_scan_sums<<<1, 1024, 0, st>>>(tiles, ntiles, out, n);
-    k_scan_apply<<<ntiles, TPB, 0, st>>>(in, n, tiles, out);
+    k_scan_lookback<<<(unsigned)ntiles, TPB, 0, st>>>(in, n, out, state, glob, k);
     return cudaGetLastError();
 }
 
@@ -325,82 +375,94 @@ __global__ void __launch_bounds__(TPB) k_fill_items(DevPlan d) {
 // own (sub = cx * TG + cy), which use per-box refined near lists, and a box holding at least
 // quad_min particles gets items per quadrant instead (sub = TG^2 + 4 (cx * TG + cy) + quadrant),
 // which use per-quadrant refined near lists.  A set of nt targets splits into sitem_count(nt)
-// items: full chunks of STREAM_CHUNK and the remainder's pieces (sitem_range).
-__global__ void __launch_bounds__(TPB) k_sitem_count(DevPlan d) {
-    long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < d.NG_total; g += stride) {
-        int s = find_seg(d.goff_tab, d.nsys, g);
-        const SysDesc &sd = d.sys[s];
-        long long lg = g - sd.goff;
-        int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
-        int gx0 = gi * sd.TG, gy0 = gj * sd.TG;
-        int gx1 = min(sd.G, gx0 + sd.TG), gy1 = min(sd.G, gy0 + sd.TG);
-        int sparse = 0, cnt = 0;
-        for (int c = gx0; c < gx1; c++)
-            for (int r = gy0; r < gy1; r++) {
-                const long long b = sd.boff + (long long)c * sd.G + r;
-                const int nb = d.box_start[b + 1] - d.box_start[b];
-                const int kind = box_item_kind(nb, d.dense_min, d.quad_min);
-                if (kind == 2) {
-                    for (int q = 0; q < 4; q++) cnt += sitem_count(d.qcounts[4 * b + q]);
-                } else if (kind == 1) {
-                    cnt += sitem_count(nb);
-                } else {
-                    sparse += nb;
-                }
+// items: full chunks of STREAM_CHUNK and the remainder's pieces (sitem_range).  One kernel: each
+// thread counts its group's items, the CTA scans its SITEM_TILE groups, a look-back over the
+// preceding tiles gives their offset, and each thread writes its group's items.
+__device__ int group_items(const DevPlan &d, long long g, bool fill, int o) {
+    const int s = find_seg(d.goff_tab, d.nsys, g);
+    const SysDesc &sd = d.sys[s];
+    const long long lg = g - sd.goff;
+    const int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
+    const int gx0 = gi * sd.TG, gy0 = gj * sd.TG;
+    const int gx1 = min(sd.G, gx0 + sd.TG), gy1 = min(sd.G, gy0 + sd.TG);
+    int sparse = 0, cnt = 0;
+    for (int c = gx0; c < gx1; c++)
+        for (int r = gy0; r < gy1; r++) {
+            const long long b = sd.boff + (long long)c * sd.G + r;
+            const int nb = d.box_start[b + 1] - d.box_start[b];
+            const int kind = box_item_kind(nb, d.dense_min, d.quad_min);
+            if (kind == 2) {
+                for (int q = 0; q < 4; q++) cnt += sitem_count(d.qcounts[4 * b + q]);
+            } else if (kind == 1) {
+                cnt += sitem_count(nb);
+            } else {
+                sparse += nb;
             }
-        d.sitem_cnt[g] = cnt + sitem_count(sparse);
-    }
-}
-
-__global__ void __launch_bounds__(TPB) k_sitem_fill(DevPlan d) {
-    long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < d.NG_total; g += stride) {
-        int s = find_seg(d.goff_tab, d.nsys, g);
-        const SysDesc &sd = d.sys[s];
-        long long lg = g - sd.goff;
-        int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
-        int gx0 = gi * sd.TG, gy0 = gj * sd.TG;
-        int gx1 = min(sd.G, gx0 + sd.TG), gy1 = min(sd.G, gy0 + sd.TG);
-        const int nbox = sd.TG * sd.TG;
-        int o = d.sitem_off[g];
-        int sparse = 0;
-        for (int c = gx0; c < gx1; c++)
-            for (int r = gy0; r < gy1; r++) {
-                const long long b = sd.boff + (long long)c * sd.G + r;
-                const int nb = d.box_start[b + 1] - d.box_start[b];
-                if (box_item_kind(nb, d.dense_min, d.quad_min) == 0) sparse += nb;
-            }
-        const int ns = sitem_count(sparse);
-        for (int k = 0; k < ns; k++, o++) {
-            d.sitem_group[o] = (int)g;
-            d.sitem_sub[o] = -1;
-            d.sitem_chunk[o] = make_int2(k, ns);
         }
-        for (int c = gx0; c < gx1; c++)
-            for (int r = gy0; r < gy1; r++) {
-                const long long b = sd.boff + (long long)c * sd.G + r;
-                const int nb = d.box_start[b + 1] - d.box_start[b];
-                const int kind = box_item_kind(nb, d.dense_min, d.quad_min);
-                const int bi = (c - gx0) * sd.TG + (r - gy0);
-                if (kind == 1) {
-                    const int nk = sitem_count(nb);
+    const int ns = sitem_count(sparse);
+    if (!fill) return cnt + ns;
+    for (int k = 0; k < ns; k++, o++) {
+        d.sitem_group[o] = (int)g;
+        d.sitem_sub[o] = -1;
+        d.sitem_chunk[o] = make_int2(k, ns);
+    }
+    const int nbox = sd.TG * sd.TG;
+    for (int c = gx0; c < gx1; c++)
+        for (int r = gy0; r < gy1; r++) {
+            const long long b = sd.boff + (long long)c * sd.G + r;
+            const int nb = d.box_start[b + 1] - d.box_start[b];
+            const int kind = box_item_kind(nb, d.dense_min, d.quad_min);
+            const int bi = (c - gx0) * sd.TG + (r - gy0);
+            if (kind == 1) {
+                const int nk = sitem_count(nb);
+                for (int k = 0; k < nk; k++, o++) {
+                    d.sitem_group[o] = (int)g;
+                    d.sitem_sub[o] = bi;
+                    d.sitem_chunk[o] = make_int2(k, nk);
+                }
+            } else if (kind == 2) {
+                for (int q = 0; q < 4; q++) {
+                    const int nk = sitem_count(d.qcounts[4 * b + q]);
                     for (int k = 0; k < nk; k++, o++) {
                         d.sitem_group[o] = (int)g;
-                        d.sitem_sub[o] = bi;
+                        d.sitem_sub[o] = nbox + 4 * bi + q;
                         d.sitem_chunk[o] = make_int2(k, nk);
-                    }
-                } else if (kind == 2) {
-                    for (int q = 0; q < 4; q++) {
-                        const int nk = sitem_count(d.qcounts[4 * b + q]);
-                        for (int k = 0; k < nk; k++, o++) {
-                            d.sitem_group[o] = (int)g;
-                            d.sitem_sub[o] = nbox + 4 * bi + q;
-                            d.sitem_chunk[o] = make_int2(k, nk);
-                        }
                     }
                 }
             }
+        }
+    return cnt + ns;
+}
+
+__global__ void __launch_bounds__(SITEM_TILE) k_sitems(DevPlan d) {
+    __shared__ int sh[32];
+    __shared__ int s_tile, s_excl;
+    __shared__ unsigned s_gen;
+    const long long ntiles = (d.NG_total + SITEM_TILE - 1) / SITEM_TILE;
+    if (threadIdx.x == 0) {
+        s_tile = (int)atomicAdd(&d.glob->scan_ticket[2], 1u);
+        s_gen = *(volatile unsigned *)&d.glob->scan_gen[2];
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    const long long g = (long long)tile * SITEM_TILE + threadIdx.x;
+    const int cnt = g < d.NG_total ? group_items(d, g, false, 0) : 0;
+    int tot;
+    const int pre = block_excl_scan(cnt, sh, &tot);
+    if (threadIdx.x < 32) {
+        const int e = lookback(d.sst_sitem, tile, s_gen, tot, d.glob);
+        if (threadIdx.x == 0) s_excl = e;
+    }
+    __syncthreads();
+    const int off = s_excl + pre;
+    if (g < d.NG_total) {
+        d.sitem_off[g] = off;
+        group_items(d, g, true, off);
+    }
+    if (tile == ntiles - 1 && threadIdx.x == 0) {
+        d.sitem_off[d.NG_total] = s_excl + tot;
+        d.glob->scan_ticket[2] = 0u;
+        d.glob->scan_gen[2] = s_gen + 1u;
     }
 }
 
@@ -464,7 +526,7 @@ __global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
             d.VY[nxt][t] = vy[u];
             d.M[nxt][t] = m[u];
             d.PID[nxt][t] = pid[u];
-            const double *org = d.org + sd.ooff;  // box origins (k_bbox_finalize)
+            const double *org = d.org + sd.ooff;  // box origins (tabulated by k_bbox's last block)
             const float ox = f64_to_f32_rn(__dsub_rn(x[u], org[kx]));
             const float oy = f64_to_f32_rn(__dsub_rn(y[u], org[sd.G + ky]));
             const float mf = f64_to_f32_rn(m[u]);
@@ -476,96 +538,211 @@ __global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
     }
 }
 
-// ------------------------------------------------------------- leaf moments
-// Segmented warp reduction over the box-sorted particles: lanes holding the
-// same box key are contiguous; an inclusive segmented scan of the float
-// contributions (offsets are box-relative, so 32 terms in FP32 are exact to
-// ~1e-7 of a box) ends in the segment's last lane, which adds the partial
-// into the box's FP64 moments with FP64 atomics.
-__global__ void __launch_bounds__(TPB) k_leaf_moments(DevPlan d) {
-    const int lane = threadIdx.x & 31;
-    long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < d.n_total; base += stride) {
-        long long i = base + threadIdx.x;
-        int key = -1;
-        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if (i < d.n_total) {
-            key = d.skey[i];
-            float4 p = d.P[i];
-            v[0] = p.z;
-            v[1] = p.z * p.x;
-            v[2] = p.z * p.y;
-            v[3] = v[1] * p.x;
-            v[4] = v[1] * p.y;
-            v[5] = v[2] * p.y;
-        }
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int k2 = __shfl_up_sync(0xffffffffu, key, o);
-#pragma unroll
-            for (int c = 0; c < 6; c++) {
-                float y = __shfl_up_sync(0xffffffffu, v[c], o);
-                if (lane >= o && k2 == key) v[c] += y;
-            }
-        }
-        int knext = __shfl_down_sync(0xffffffffu, key, 1);
-        bool tail = (lane == 31) || (knext != key);
-        if (tail && key >= 0) {
-            int s = find_seg(d.boff_tab, d.nsys, key);
-            long long c = d.sys[s].coff + (key - d.sys[s].boff);
-            double *q = d.mom + 6 * c;
-#pragma unroll
-            for (int k = 0; k < 6; k++) atomicAdd(q + k, (double)v[k]);
-        }
+// ---------------------------------------------------------------- summarize
+// One CTA per tile of SUM_TILE x SUM_TILE leaf boxes: the boxes' moments (M, Sx, Sy, Sxx, Sxy,
+// Syy about the box origin) from their box-sorted particles, then pyramid levels 1..4 inside the
+// tile, then the cell records of all of them; the CTA that finishes a system's last tile builds
+// the levels above (cells of 2^5 boxes and larger) from the tiles' level-4 cells.  Every sum runs
+// in a fixed order -- a box's particles in chunks of 32 in sorted order, each chunk reduced in FP32
+// by a butterfly (offsets are box-relative, so 32 terms keep ~1e-7 of a box edge) and the chunk
+// sums added in FP64 in chunk order -- so the moments do not depend on scheduling.
+constexpr int SUM_THREADS = 256;
+constexpr int SUM_WARPS = SUM_THREADS / 32;
+constexpr int SUM_BIG = 2048;  // boxes with more particles are summed by the whole CTA
+constexpr int SUM_CELLS = 256 + 64 + 16 + 4 + 1;  // a tile's cells at levels 0..4
+
+// FP32 butterfly sum of v over the warp (every lane ends with the same bits), then lane k < 6
+// adds component k to its FP64 accumulator.
+__device__ __forceinline__ void chunk_moments(const float4 *P, long long i, long long i1, int lane,
+                                              double &acc) {
+    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (i < i1) {
+        const float4 p = P[i];
+        v[0] = p.z;
+        v[1] = p.z * p.x;
+        v[2] = p.z * p.y;
+        v[3] = v[1] * p.x;
+        v[4] = v[1] * p.y;
+        v[5] = v[2] * p.y;
     }
+#pragma unroll
+    for (int o = 16; o; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < 6; c++) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
+    float mine = v[0];
+#pragma unroll
+    for (int c = 1; c < 6; c++)
+        if (lane == c) mine = v[c];
+    if (lane < 6) acc += (double)mine;
 }
 
-// ------------------------------------------------------------------ pyramid
-// Level-l cell = sum of its (up to) four level-(l-1) children, moments shifted
-// from the child origin to the parent origin (FP64).
-__device__ __forceinline__ void pyramid_cell(const DevPlan &d, int l, long long t) {
-    const long long *tab = d.lvl_tab + (long long)l * (d.nsys + 1);
-    int s = find_seg(tab, d.nsys, t);
-    const SysDesc &sd = d.sys[s];
-    double step = d.dyn[s].step;
-    long long loc = t - tab[s];
-    int gl = sd.lvg[l], gc = sd.lvg[l - 1];
-    int i = (int)(loc / gl), j = (int)(loc - (long long)i * gl);
-    double p[6] = {0, 0, 0, 0, 0, 0};
+// Cell (I, J) of level l of system s from its up to four level-(l-1) children (c: their moments,
+// child (a, b) at c + 6 * (2 * a + b), flag has_child[2 * a + b]), shifted to the parent origin.
+__device__ __forceinline__ void shift_children(const double *c, const bool *has, int l, double step,
+                                               double *p) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) p[k] = 0.0;
     for (int a = 0; a < 2; a++)
         for (int b = 0; b < 2; b++) {
-            int ci = 2 * i + a, cj = 2 * j + b;
-            if (ci >= gc || cj >= gc) continue;
-            const double *c = d.mom + 6 * (sd.coff + sd.lvoff[l - 1] + (long long)ci * gc + cj);
+            if (!has[2 * a + b]) continue;
+            const double *q = c + 6 * (2 * a + b);
             double dx = (double)(a << (l - 1)) * step, dy = (double)(b << (l - 1)) * step;
-            double M = c[0], Sx = c[1], Sy = c[2];
+            double M = q[0], Sx = q[1], Sy = q[2];
             p[0] += M;
             p[1] += Sx + M * dx;
             p[2] += Sy + M * dy;
-            p[3] += c[3] + 2.0 * dx * Sx + M * dx * dx;
-            p[4] += c[4] + dx * Sy + dy * Sx + M * dx * dy;
-            p[5] += c[5] + 2.0 * dy * Sy + M * dy * dy;
+            p[3] += q[3] + 2.0 * dx * Sx + M * dx * dx;
+            p[4] += q[4] + dx * Sy + dy * Sx + M * dx * dy;
+            p[5] += q[5] + 2.0 * dy * Sy + M * dy * dy;
         }
-    double *q = d.mom + 6 * (sd.coff + sd.lvoff[l] + loc);
-#pragma unroll
-    for (int k = 0; k < 6; k++) q[k] = p[k];
 }
 
-__global__ void __launch_bounds__(TPB) k_pyramid_level(DevPlan d, int l) {
-    const long long total = d.lvl_tab[(long long)l * (d.nsys + 1) + d.nsys];
-    long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride)
-        pyramid_cell(d, l, t);
+// Float records of cell c (level l) of system s: centre of mass relative to the cell origin and
+// mass; with `second`, the second moments about the centre of mass normalised by M s^2.
+__device__ __forceinline__ void cell_record(const DevPlan &d, long long c, int l, double step,
+                                            const double *q, int second) {
+    const double M = q[0];
+    if (M > 0.0) {
+        const double cx = q[1] / M, cy = q[2] / M;
+        d.rec[c] = make_float4(f64_to_f32_rn(cx), f64_to_f32_rn(cy), f64_to_f32_rn(M), 0.f);
+        if (second) {
+            const double sz = (double)(1 << l) * step;
+            const double nrm = 1.0 / (M * sz * sz);
+            const double ixx = q[3] - q[1] * cx, ixy = q[4] - q[1] * cy, iyy = q[5] - q[2] * cy;
+            d.rec2[c] = make_float4(f64_to_f32_rn(ixx * nrm), f64_to_f32_rn(ixy * nrm),
+                                    f64_to_f32_rn(iyy * nrm), 0.f);
+        }
+    } else {
+        d.rec[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (second) d.rec2[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
 }
 
-// Levels l0 .. Lmax - 1 in one CTA (their cells are few): level by level, a barrier between.
-constexpr int TAIL_THREADS = 1024;
-constexpr long long TAIL_MAX_CELLS = 256;  // the first level given to the single CTA (FP64 work on one SM)
-__global__ void __launch_bounds__(TAIL_THREADS) k_pyramid_tail(DevPlan d, int l0) {
-    for (int l = l0; l < d.Lmax; l++) {
-        const long long total = d.lvl_tab[(long long)l * (d.nsys + 1) + d.nsys];
-        for (long long t = threadIdx.x; t < total; t += blockDim.x) pyramid_cell(d, l, t);
-        __syncthreads();  // level l is complete before level l + 1 reads it
+// leaves_given: the leaf moments are already in d.mom (bh_set_leaf_moments); build the rest.
+__global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int second, int leaves_given) {
+    __shared__ double cm[SUM_CELLS * 6];  // the tile's cells, level by level
+    __shared__ int big[SUM_TILE * SUM_TILE], nbig;
+    __shared__ double wpart[SUM_WARPS][6];
+    __shared__ unsigned ticket;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int loff[5] = {0, 256, 320, 336, 340};
+    for (long long t = blockIdx.x; t < d.T_total; t += gridDim.x) {
+        const int s = find_seg(d.toff_tab, d.nsys, t);
+        const SysDesc &sd = d.sys[s];
+        const double step = d.dyn[s].step;
+        const int G = sd.G, lt = (int)(t - sd.toff), ti = lt / sd.tps, tj = lt - ti * sd.tps;
+        const int bx0 = ti * SUM_TILE, by0 = tj * SUM_TILE;
+        const int lmax = min(4, sd.L - 1);  // the tile's top level
+        if (tid == 0) nbig = 0;
+        __syncthreads();
+        // ---- level 0: the tile's boxes (zeros outside the grid)
+        for (int k = warp; k < SUM_TILE * SUM_TILE; k += SUM_WARPS) {
+            const int cx = k / SUM_TILE, cy = k - cx * SUM_TILE;
+            double acc = 0.0;
+            if (bx0 + cx < G && by0 + cy < G) {
+                const long long lb = (long long)(bx0 + cx) * G + (by0 + cy);
+                if (leaves_given) {
+                    if (lane < 6) acc = d.mom[6 * (sd.coff + lb) + lane];
+                } else {
+                    const long long i0 = d.box_start[sd.boff + lb], i1 = d.box_start[sd.boff + lb + 1];
+                    if (i1 - i0 > SUM_BIG) {
+                        if (lane == 0) big[atomicAdd(&nbig, 1)] = k;
+                        continue;
+                    }
+                    for (long long c = i0; c < i1; c += 32) chunk_moments(d.P, c + lane, i1, lane, acc);
+                    if (lane < 6) d.mom[6 * (sd.coff + lb) + lane] = acc;
+                }
+            }
+            if (lane < 6) cm[6 * k + lane] = acc;
+        }
+        __syncthreads();
+        // boxes of more than SUM_BIG particles: chunks dealt to the warps round-robin, the warps'
+        // sums added in warp order
+        for (int q = 0; q < nbig; q++) {
+            const int k = big[q];
+            const int cx = k / SUM_TILE, cy = k - cx * SUM_TILE;
+            const long long lb = (long long)(bx0 + cx) * G + (by0 + cy);
+            const long long i0 = d.box_start[sd.boff + lb], i1 = d.box_start[sd.boff + lb + 1];
+            double acc = 0.0;
+            for (long long c = i0 + 32LL * warp; c < i1; c += 32LL * SUM_WARPS)
+                chunk_moments(d.P, c + lane, i1, lane, acc);
+            if (lane < 6) wpart[warp][lane] = acc;
+            __syncthreads();
+            if (tid < 6) {
+                double a = 0.0;
+                for (int w = 0; w < SUM_WARPS; w++) a += wpart[w][tid];
+                cm[6 * k + tid] = a;
+                d.mom[6 * (sd.coff + lb) + tid] = a;
+            }
+            __syncthreads();
+        }
+        // ---- levels 1..lmax inside the tile
+        for (int l = 1; l <= lmax; l++) {
+            const int nl = SUM_TILE >> l, nc = nl << 1;  // cells per side at l and l - 1
+            const int gl = sd.lvg[l], gc = sd.lvg[l - 1];
+            const int I0 = bx0 >> l, J0 = by0 >> l;
+            if (tid < nl * nl) {
+                const int ci = tid / nl, cj = tid - ci * nl;
+                double ch[24], p[6];
+                bool has[4];
+                for (int a = 0; a < 2; a++)
+                    for (int b = 0; b < 2; b++) {
+                        const int li = 2 * ci + a, lj = 2 * cj + b;
+                        has[2 * a + b] = 2 * (I0 + ci) + a < gc && 2 * (J0 + cj) + b < gc;
+                        for (int k = 0; k < 6; k++) ch[6 * (2 * a + b) + k] = cm[6 * (loff[l - 1] + li * nc + lj) + k];
+                    }
+                shift_children(ch, has, l, step, p);
+                const bool inside = I0 + ci < gl && J0 + cj < gl;
+                for (int k = 0; k < 6; k++) cm[6 * (loff[l] + tid) + k] = inside ? p[k] : 0.0;
+                if (inside) {
+                    double *q = d.mom + 6 * (sd.coff + sd.lvoff[l] + (long long)(I0 + ci) * gl + (J0 + cj));
+                    for (int k = 0; k < 6; k++) q[k] = p[k];
+                }
+            }
+            __syncthreads();
+        }
+        // ---- records of the tile's cells
+        for (int l = 0; l <= lmax; l++) {
+            const int nl = SUM_TILE >> l, gl = sd.lvg[l];
+            const int I0 = bx0 >> l, J0 = by0 >> l;
+            for (int k = tid; k < nl * nl; k += SUM_THREADS) {
+                const int ci = k / nl, cj = k - ci * nl;
+                if (I0 + ci >= gl || J0 + cj >= gl) continue;
+                const long long c = sd.coff + sd.lvoff[l] + (long long)(I0 + ci) * gl + (J0 + cj);
+                cell_record(d, c, l, step, cm + 6 * (loff[l] + k), second);
+            }
+        }
+        // ---- the system's last tile builds the levels above the tiles
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) ticket = atomicAdd(&d.dyn[s].tiles_done, 1u);
+        __syncthreads();
+        if (ticket == (unsigned)(sd.tps * sd.tps) - 1u) {
+            __threadfence();
+            for (int l = lmax + 1; l < sd.L; l++) {
+                const int gl = sd.lvg[l], gc = sd.lvg[l - 1];
+                for (int k = tid; k < gl * gl; k += SUM_THREADS) {
+                    const int I = k / gl, J = k - I * gl;
+                    double ch[24], p[6];
+                    bool has[4];
+                    for (int a = 0; a < 2; a++)
+                        for (int b = 0; b < 2; b++) {
+                            const int ci = 2 * I + a, cj = 2 * J + b;
+                            has[2 * a + b] = ci < gc && cj < gc;
+                            const double *q = d.mom + 6 * (sd.coff + sd.lvoff[l - 1] + (long long)ci * gc + cj);
+                            for (int c = 0; c < 6; c++) ch[6 * (2 * a + b) + c] = has[2 * a + b] ? __ldcg(q + c) : 0.0;
+                        }
+                    shift_children(ch, has, l, step, p);
+                    const long long c = sd.coff + sd.lvoff[l] + k;
+                    for (int q = 0; q < 6; q++) d.mom[6 * c + q] = p[q];
+                    cell_record(d, c, l, step, p, second);
+                }
+                __threadfence();
+                __syncthreads();
+            }
+            if (tid == 0) d.dyn[s].tiles_done = 0u;
+        }
+        __syncthreads();
     }
 }
 
@@ -610,18 +787,17 @@ cudaError_t launch_bbox(const DevPlan &d, cudaStream_t st) {
 }
 cudaError_t launch_place(const DevPlan &d, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_bbox_finalize<<<d.nsys, 128, 0, st>>>(d);
     k_place<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
 cudaError_t launch_scan(const DevPlan &d, cudaStream_t st) {
-    return scan_excl(d.counts, d.box_start, d.B_total, d.tile_sums, st);
+    return scan_excl(d.counts, d.box_start, d.B_total, d.sst_box, d.glob, 0, st);
 }
 // Work items of the walk kernel and of the learned correction (group, target chunk).
 cudaError_t launch_walk_items(const DevPlan &d, cudaStream_t st) {
     unsigned g = grid_for(d.NG_total, TPB, d.nsm * 8LL);
     k_group_items<<<g, TPB, 0, st>>>(d);
-    cudaError_t e = scan_excl(d.item_cnt, d.item_off, d.NG_total, d.tile_sums, st);
+    cudaError_t e = scan_excl(d.item_cnt, d.item_off, d.NG_total, d.sst_witem, d.glob, 1, st);
     if (e != cudaSuccess) return e;
     k_fill_items<<<g, TPB, 0, st>>>(d);
     return cudaGetLastError();
@@ -635,12 +811,8 @@ cudaError_t launch_items(const DevPlan &d, cudaStream_t st) {
         e = launch_walk_items(d, st);
         if (e != cudaSuccess) return e;
     }
-    if (d.stream) {
-        unsigned g = grid_for(d.NG_total, TPB, d.nsm * 8LL);
-        k_sitem_count<<<g, TPB, 0, st>>>(d);
-        e = scan_excl(d.sitem_cnt, d.sitem_off, d.NG_total, d.tile_sums, st);
-        if (e != cudaSuccess) return e;
-        k_sitem_fill<<<g, TPB, 0, st>>>(d);
+    if (d.stream && d.NG_total > 0) {
+        k_sitems<<<(unsigned)((d.NG_total + SITEM_TILE - 1) / SITEM_TILE), SITEM_TILE, 0, st>>>(d);
     }
     return cudaGetLastError();
 }
@@ -650,21 +822,13 @@ cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
     return cudaGetLastError();
 }
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st) {
-    if (d.n_total > 0) k_leaf_moments<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
-    return launch_pyramid(d, st);
+    // the normalised second moments feed only the learned correction
+    k_summarize<<<grid_for(d.T_total, 1, d.nsm * 8LL), SUM_THREADS, 0, st>>>(d, d.learned != 0, 0);
+    return cudaGetLastError();
 }
 cudaError_t launch_pyramid(const DevPlan &d, cudaStream_t st) {
-    for (int l = 1; l < d.Lmax; l++) {
-        // the level's cell count over all systems is known on the host: one thread per cell
-        // while the level is large, then one CTA for all the remaining (small) levels
-        if (d.lvl_cells[l] <= TAIL_MAX_CELLS) {
-            k_pyramid_tail<<<1, TAIL_THREADS, 0, st>>>(d, l);
-            break;
-        }
-        k_pyramid_level<<<grid_for(d.lvl_cells[l], TPB, d.nsm * 4LL), TPB, 0, st>>>(d, l);
-    }
-    // the normalised second moments feed only the learned correction
-    return launch_records(d, d.learned != 0, st);
+    k_summarize<<<grid_for(d.T_total, 1, d.nsm * 8LL), SUM_THREADS, 0, st>>>(d, d.learned != 0, 1);
+    return cudaGetLastError();
 }
 cudaError_t launch_records(const DevPlan &d, bool second, cudaStream_t st) {
     k_records<<<grid_for(d.C_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d, second ? 1 : 0);

@@ -101,8 +101,8 @@ def test_missing_library_fails_loudly(monkeypatch):
 
 def test_launch_count_host_logic(lib):
     """bh_kernels_per_step is host-only: a list-streaming plan builds no walk work items unless
-    it carries the learned correction; a walking plan builds them (5 kernels: count, 3 scan
-    phases, fill).  No step graph exists before the first capture."""
+    it carries the learned correction; a walking plan builds them (3 kernels: count, scan,
+    fill).  No step graph exists before the first capture."""
     from barneshut.gb300 import native
 
     def count(**kw):
@@ -116,8 +116,8 @@ def test_launch_count_host_logic(lib):
         return c.value
 
     stream = count()
-    assert count(flags=native.BH_FLAG_WALK) == stream + 5 - 8  # walk items in, stream items and lists out
-    assert count(flags=native.BH_FLAG_LEARNED) == stream + 5
+    assert count(flags=native.BH_FLAG_WALK) == stream + 3 - 4  # walk items in, stream items and lists out
+    assert count(flags=native.BH_FLAG_LEARNED) == stream + 3
 
 
 def _workspace(lib, n, G, **kw):
