@@ -7,6 +7,7 @@
 // captured into a CUDA graph replays correctly.
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -45,6 +46,7 @@ struct bh_plan {
     bool acc_stale = true;  // next bh_evaluate overwrites instead of accumulating
     // graph cache
     cudaGraphExec_t gexec = nullptr;
+    size_t sst_bytes = 0;  // the single-pass scans' tile states
     cudaEvent_t tev[2] = {nullptr, nullptr};  // bh_set_kernel_timing: around the force kernel
     bool timing = false;
     bool tev_recorded = false;
@@ -265,7 +267,8 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_counts = take(4 * B);
     p->o_qcnt = take(16 * B);
     p->o_bstart = take(4 * (B + 1));
-    p->o_sst = take(8 * (B / SCAN_TILE + 2 + (size_t)p->NG_total / SCAN_TILE + 2 + (size_t)p->NG_total / SITEM_TILE + 2));
+    p->sst_bytes = 8 * (B / SCAN_TILE + 2 + (size_t)p->NG_total / SCAN_TILE + 2 + (size_t)p->NG_total / SITEM_TILE + 2);
+    p->o_sst = take(p->sst_bytes);
     p->o_icnt = take(4 * (size_t)p->NG_total);
     p->o_ioff = take(4 * ((size_t)p->NG_total + 1));
     p->o_igrp = take(4 * ((size_t)p->NG_total + N / p->chunk + 1));
@@ -414,6 +417,12 @@ extern "C" int bh_bind(bh_plan *p, void *workspace, size_t bytes, void *stream) 
     CK(p, cudaMemcpyAsync(w + p->o_lvl, p->lvl.data(), 8 * p->lvl.size(), cudaMemcpyHostToDevice, st), "upload lvl");
     CK(p, cudaMemsetAsync(w + p->o_dyn, 0, sizeof(SysDyn) * p->nsys, st), "zero dyn");
     CK(p, cudaMemsetAsync(w + p->o_glob, 0, sizeof(Globals), st), "zero globals");
+    {  // scan generations start at 1 over zeroed tile states
+        const unsigned one[3] = {1u, 1u, 1u};
+        CK(p, cudaMemcpyAsync(w + p->o_glob + offsetof(Globals, scan_gen), one, sizeof(one),
+                              cudaMemcpyHostToDevice, st), "scan generations");
+        CK(p, cudaMemsetAsync(w + p->o_sst, 0, p->sst_bytes, st), "zero scan states");
+    }
     CK(p, cudaStreamSynchronize(st), "bind sync");
     p->has_tree = false;
     p->acc_stale = true;

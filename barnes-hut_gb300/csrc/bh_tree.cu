@@ -242,6 +242,10 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh, int *total) {
     return pre;
 }
 
+// Generations run 1 .. 2^30 - 1 (30 bits in a state); 0 never tags a state, so the zeroed
+// states of a freshly bound plan read as not yet written.
+__device__ __forceinline__ unsigned next_gen(unsigned g) { return g >= 0x3FFFFFFFu ? 1u : g + 1u; }
+
 // Warp 0 of the CTA: publish the tile's sum `agg`, look back, publish the inclusive prefix and
 // return the tile's exclusive prefix (to lane 0; the caller broadcasts through shared memory).
 __device__ int lookback(unsigned long long *state, int tile, unsigned gen, int agg, Globals *glob) {
@@ -329,7 +333,7 @@ __global__ void __launch_bounds__(TPB) k_scan_lookback(const int *in, long long 
     if (tile == ntiles - 1 && threadIdx.x == 0) {
         out[n] = s_excl + tot;
         glob->scan_ticket[k] = 0u;  // every tile has its ticket: ready for the next scan
-        glob->scan_gen[k] = s_gen + 1u;
+        glob->scan_gen[k] = next_gen(s_gen);
     }
 }
 
@@ -462,7 +466,7 @@ __global__ void __launch_bounds__(SITEM_TILE) k_sitems(DevPlan d) {
     if (tile == ntiles - 1 && threadIdx.x == 0) {
         d.sitem_off[d.NG_total] = s_excl + tot;
         d.glob->scan_ticket[2] = 0u;
-        d.glob->scan_gen[2] = s_gen + 1u;
+        d.glob->scan_gen[2] = next_gen(s_gen);
     }
 }
 
@@ -542,39 +546,15 @@ __global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
 // One CTA per tile of SUM_TILE x SUM_TILE leaf boxes: the boxes' moments (M, Sx, Sy, Sxx, Sxy,
 // Syy about the box origin) from their box-sorted particles, then pyramid levels 1..4 inside the
 // tile, then the cell records of all of them; the CTA that finishes a system's last tile builds
-// the levels above (cells of 2^5 boxes and larger) from the tiles' level-4 cells.  Every sum runs
-// in a fixed order -- a box's particles in chunks of 32 in sorted order, each chunk reduced in FP32
-// by a butterfly (offsets are box-relative, so 32 terms keep ~1e-7 of a box edge) and the chunk
-// sums added in FP64 in chunk order -- so the moments do not depend on scheduling.
+// the levels above (cells of 2^5 boxes and larger) from the tiles' level-4 cells.  A tile row (a
+// column of SUM_TILE boxes of one x) is contiguous in particle order; one warp streams it in
+// chunks of 32 particles, a segmented FP32 scan by box sums each box's part of a chunk (offsets
+// are box-relative, so 32 terms keep ~1e-7 of a box edge), and the segment's last lane adds it
+// to the box's FP64 sum in shared memory.  Every sum runs in a fixed order, so the moments do
+// not depend on scheduling.
 constexpr int SUM_THREADS = 256;
 constexpr int SUM_WARPS = SUM_THREADS / 32;
-constexpr int SUM_BIG = 2048;  // boxes with more particles are summed by the whole CTA
 constexpr int SUM_CELLS = 256 + 64 + 16 + 4 + 1;  // a tile's cells at levels 0..4
-
-// FP32 butterfly sum of v over the warp (every lane ends with the same bits), then lane k < 6
-// adds component k to its FP64 accumulator.
-__device__ __forceinline__ void chunk_moments(const float4 *P, long long i, long long i1, int lane,
-                                              double &acc) {
-    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (i < i1) {
-        const float4 p = P[i];
-        v[0] = p.z;
-        v[1] = p.z * p.x;
-        v[2] = p.z * p.y;
-        v[3] = v[1] * p.x;
-        v[4] = v[1] * p.y;
-        v[5] = v[2] * p.y;
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1)
-#pragma unroll
-        for (int c = 0; c < 6; c++) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
-    float mine = v[0];
-#pragma unroll
-    for (int c = 1; c < 6; c++)
-        if (lane == c) mine = v[c];
-    if (lane < 6) acc += (double)mine;
-}
 
 // Cell (I, J) of level l of system s from its up to four level-(l-1) children (c: their moments,
 // child (a, b) at c + 6 * (2 * a + b), flag has_child[2 * a + b]), shifted to the parent origin.
@@ -621,8 +601,6 @@ __device__ __forceinline__ void cell_record(const DevPlan &d, long long c, int l
 // leaves_given: the leaf moments are already in d.mom (bh_set_leaf_moments); build the rest.
 __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int second, int leaves_given) {
     __shared__ double cm[SUM_CELLS * 6];  // the tile's cells, level by level
-    __shared__ int big[SUM_TILE * SUM_TILE], nbig;
-    __shared__ double wpart[SUM_WARPS][6];
     __shared__ unsigned ticket;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int loff[5] = {0, 256, 320, 336, 340};
@@ -632,49 +610,59 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
         const double step = d.dyn[s].step;
         const int G = sd.G, lt = (int)(t - sd.toff), ti = lt / sd.tps, tj = lt - ti * sd.tps;
         const int bx0 = ti * SUM_TILE, by0 = tj * SUM_TILE;
+        const int nbx = min(SUM_TILE, G - bx0), nby = min(SUM_TILE, G - by0);
         const int lmax = min(4, sd.L - 1);  // the tile's top level
-        if (tid == 0) nbig = 0;
-        __syncthreads();
         // ---- level 0: the tile's boxes (zeros outside the grid)
-        for (int k = warp; k < SUM_TILE * SUM_TILE; k += SUM_WARPS) {
-            const int cx = k / SUM_TILE, cy = k - cx * SUM_TILE;
-            double acc = 0.0;
-            if (bx0 + cx < G && by0 + cy < G) {
-                const long long lb = (long long)(bx0 + cx) * G + (by0 + cy);
-                if (leaves_given) {
-                    if (lane < 6) acc = d.mom[6 * (sd.coff + lb) + lane];
-                } else {
-                    const long long i0 = d.box_start[sd.boff + lb], i1 = d.box_start[sd.boff + lb + 1];
-                    if (i1 - i0 > SUM_BIG) {
-                        if (lane == 0) big[atomicAdd(&nbig, 1)] = k;
-                        continue;
-                    }
-                    for (long long c = i0; c < i1; c += 32) chunk_moments(d.P, c + lane, i1, lane, acc);
-                    if (lane < 6) d.mom[6 * (sd.coff + lb) + lane] = acc;
-                }
-            }
-            if (lane < 6) cm[6 * k + lane] = acc;
+        for (int k = tid; k < 6 * SUM_TILE * SUM_TILE; k += SUM_THREADS) {
+            const int box = k / 6, cx = box / SUM_TILE, cy = box - cx * SUM_TILE;
+            double v = 0.0;
+            if (leaves_given && cx < nbx && cy < nby)
+                v = d.mom[6 * (sd.coff + (long long)(bx0 + cx) * G + (by0 + cy)) + (k - 6 * box)];
+            cm[k] = v;
         }
         __syncthreads();
-        // boxes of more than SUM_BIG particles: chunks dealt to the warps round-robin, the warps'
-        // sums added in warp order
-        for (int q = 0; q < nbig; q++) {
-            const int k = big[q];
-            const int cx = k / SUM_TILE, cy = k - cx * SUM_TILE;
-            const long long lb = (long long)(bx0 + cx) * G + (by0 + cy);
-            const long long i0 = d.box_start[sd.boff + lb], i1 = d.box_start[sd.boff + lb + 1];
-            double acc = 0.0;
-            for (long long c = i0 + 32LL * warp; c < i1; c += 32LL * SUM_WARPS)
-                chunk_moments(d.P, c + lane, i1, lane, acc);
-            if (lane < 6) wpart[warp][lane] = acc;
-            __syncthreads();
-            if (tid < 6) {
-                double a = 0.0;
-                for (int w = 0; w < SUM_WARPS; w++) a += wpart[w][tid];
-                cm[6 * k + tid] = a;
-                d.mom[6 * (sd.coff + lb) + tid] = a;
+        if (!leaves_given) {
+            for (int cx = warp; cx < nbx; cx += SUM_WARPS) {
+                const long long b0 = sd.boff + (long long)(bx0 + cx) * G + by0;  // the row's first box
+                const int i0 = d.box_start[b0], i1 = d.box_start[b0 + nby];
+                double *row = cm + 6 * cx * SUM_TILE;
+                for (int c = i0; c < i1; c += 32) {
+                    const int i = c + lane;
+                    int key = -1;
+                    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                    if (i < i1) {
+                        key = d.skey[i] - (int)b0;  // box within the row
+                        const float4 p = d.P[i];
+                        v[0] = p.z;
+                        v[1] = p.z * p.x;
+                        v[2] = p.z * p.y;
+                        v[3] = v[1] * p.x;
+                        v[4] = v[1] * p.y;
+                        v[5] = v[2] * p.y;
+                    }
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int k2 = __shfl_up_sync(0xffffffffu, key, o);
+#pragma unroll
+                        for (int q = 0; q < 6; q++) {
+                            const float y = __shfl_up_sync(0xffffffffu, v[q], o);
+                            if (lane >= o && k2 == key) v[q] += y;
+                        }
+                    }
+                    const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+                    if (key >= 0 && (lane == 31 || knext != key)) {
+#pragma unroll
+                        for (int q = 0; q < 6; q++) row[6 * key + q] += (double)v[q];
+                    }
+                    __syncwarp();
+                }
             }
             __syncthreads();
+            for (int k = tid; k < 6 * SUM_TILE * SUM_TILE; k += SUM_THREADS) {
+                const int box = k / 6, cx = box / SUM_TILE, cy = box - cx * SUM_TILE;
+                if (cx < nbx && cy < nby)
+                    d.mom[6 * (sd.coff + (long long)(bx0 + cx) * G + (by0 + cy)) + (k - 6 * box)] = cm[k];
+            }
         }
         // ---- levels 1..lmax inside the tile
         for (int l = 1; l <= lmax; l++) {

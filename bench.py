@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--ref-sample-boxes", type=int, default=1024)
     ap.add_argument("--quick", action="store_true",
                     help="skip the autotuner and the batched / learned side measurements")
+    ap.add_argument("--profile-learned", action="store_true",
+                    help="for an ncu capture: train a small correction network, then run two "
+                         "learned evaluates at N=1,048,576 (256 x 256 boxes, theta 0.8) and exit")
     ap.add_argument("--tile", default=None,
                     help="group_dim,dense_min,tune[,quad_min]: use this tile instead of the autotuner's")
     return ap.parse_args()
@@ -605,11 +608,47 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def profile_learned():
+    """Two learned evaluates at N = 1,048,576 (cluster mixture seed 1, 256 x 256 boxes, theta 0.8,
+    correction theta 0.5) with a network trained on 2^19 pairs of a 2^18-particle system: a small
+    case for capturing k_learned_correct under ncu (the second launch)."""
+    import torch
+
+    from barneshut.gb300 import learned, native, workloads
+
+    mlp, _ = learned.train_correction([workloads.cluster_mixture(1 << 18, seed=11)], 128, 0.8, 0.5,
+                                      n_pairs=1 << 19, epochs=1)
+    x, y, m, vx, vy = workloads.cluster_mixture(1 << 20, seed=1)
+    prm = native.make_params(1.0, DT, SOFTENING, 0.0, 0.8, 0, native.BH_PREC_FP32_KAHAN,
+                             native.BH_FLAG_LEARNED, 0, 0.5)
+    plan = native.Plan([len(x)], [256], prm)
+    plan.set_correction(mlp)
+    ms = []
+    for _ in range(2):
+        plan.load(x, y, m, vx, vy)
+        plan.create_tree()
+        plan.summarize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        plan.evaluate()
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    near, far = plan.pair_counts()
+    print(json.dumps({"profile": "learned", "n": len(x), "grid": 256, "theta": 0.8,
+                      "evaluate_ms": ms, "pairs_corrected": plan.corrected_pairs(),
+                      "pairs_near": near, "pairs_far": far,
+                      "device_error_flags": plan.error_flags(raise_on_error=False)}), flush=True)
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.profile_learned:
+        profile_learned()
         return
     import numpy as np
     import torch
