@@ -222,6 +222,23 @@ __device__ __forceinline__ int box_key1_fast(double p, double mn, double step, d
     return (int)k;
 }
 
+// float -> double on the integer pipes: exact for normal floats and zeros (rebias the exponent,
+// widen the mantissa); subnormal, infinite and NaN inputs take the hardware conversion, which
+// GB300 runs on its slow FP64 pipe.
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    if (e == 0u) {
+        if ((u & 0x7FFFFFu) == 0u) return __longlong_as_double((long long)(u & 0x80000000u) << 32);
+        return (double)f;
+    }
+    if (e == 0xFFu) return (double)f;
+    const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                    ((unsigned long long)(e + 896u) << 52) |
+                                    ((unsigned long long)(u & 0x7FFFFFu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
 // The same key with a float estimate first: q_f = (float(p) - float(mn)) * float(1 / step) is
 // within tol of the FP64 quotient (tol from the system's extent, set in k_bbox_finalize), so
 // floor(q_f) is the exact key unless q_f lies within tol of an integer; only then (and for an

@@ -626,6 +626,12 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
                 const long long b0 = sd.boff + (long long)(bx0 + cx) * G + by0;  // the row's first box
                 const int i0 = d.box_start[b0], i1 = d.box_start[b0 + nby];
                 double *row = cm + 6 * cx * SUM_TILE;
+                // the box still open at the end of the previous chunk: its Kahan-compensated FP32
+                // sums (s, c), the same in every lane
+                int ckey = -1;
+                float cs[6], cc[6];
+#pragma unroll
+                for (int q = 0; q < 6; q++) cs[q] = cc[q] = 0.f;
                 for (int c = i0; c < i1; c += 32) {
                     const int i = c + lane;
                     int key = -1;
@@ -650,11 +656,60 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
                         }
                     }
                     const int knext = __shfl_down_sync(0xffffffffu, key, 1);
-                    if (key >= 0 && (lane == 31 || knext != key)) {
+                    const int kfirst = __shfl_sync(0xffffffffu, key, 0);
+                    const int klast = __shfl_sync(0xffffffffu, key, 31);
+                    if (ckey >= 0 && ckey != kfirst && lane < 6) {  // the open box ended with the last chunk
+                        float r = cs[0];
 #pragma unroll
-                        for (int q = 0; q < 6; q++) row[6 * key + q] += (double)v[q];
+                        for (int q = 1; q < 6; q++)
+                            if (lane == q) r = cs[q];
+                        float e = cc[0];
+#pragma unroll
+                        for (int q = 1; q < 6; q++)
+                            if (lane == q) e = cc[q];
+                        row[6 * ckey + lane] = f32_to_f64(__fsub_rn(r, e));
                     }
+                    // boxes that end inside this chunk: a segment's last lane, not lane 31
+                    if (key >= 0 && lane < 31 && knext != key) {
+                        const bool cont = key == ckey;  // the first segment continues the open box
+#pragma unroll
+                        for (int q = 0; q < 6; q++) {
+                            float tot = v[q];
+                            if (cont) {  // (s, c) + v, compensated, then s - c
+                                const float y = __fsub_rn(v[q], cc[q]);
+                                const float t = __fadd_rn(cs[q], y);
+                                const float cn = __fsub_rn(__fsub_rn(t, cs[q]), y);
+                                tot = __fsub_rn(t, cn);
+                            }
+                            row[6 * key + q] = f32_to_f64(tot);
+                        }
+                    }
+                    // the box open at lane 31 carries into the next chunk
+#pragma unroll
+                    for (int q = 0; q < 6; q++) {
+                        const float v31 = __shfl_sync(0xffffffffu, v[q], 31);
+                        if (klast >= 0 && klast == ckey && kfirst == ckey) {
+                            const float y = __fsub_rn(v31, cc[q]);
+                            const float t = __fadd_rn(cs[q], y);
+                            cc[q] = __fsub_rn(__fsub_rn(t, cs[q]), y);
+                            cs[q] = t;
+                        } else {
+                            cs[q] = v31;
+                            cc[q] = 0.f;
+                        }
+                    }
+                    ckey = klast;
                     __syncwarp();
+                }
+                if (ckey >= 0 && lane < 6) {  // the row's last box
+                    float r = cs[0], e = cc[0];
+#pragma unroll
+                    for (int q = 1; q < 6; q++)
+                        if (lane == q) {
+                            r = cs[q];
+                            e = cc[q];
+                        }
+                    row[6 * ckey + lane] = f32_to_f64(__fsub_rn(r, e));
                 }
             }
             __syncthreads();
