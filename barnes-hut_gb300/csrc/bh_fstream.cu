@@ -32,48 +32,56 @@ namespace bh {
 constexpr int NR = FORCE_R;
 constexpr int FW = 4;       // warps per CTA
 constexpr int WFAR = 128;   // far entries per staging pass (per warp)
-constexpr int WSRC = 88;    // near sources per bulk-copy pass (per warp, per buffer)
 constexpr int WDESC = 64;   // near descriptors per batch (per warp)
-
-// per-warp shared-memory carve-up (bytes).  The far phase of an item ends before its near phase
-// starts, and the slice reduction follows both, so the far staging and the reduction buffer
-// share the two near-source buffers.
-constexpr int W_SRC = 0;                             // 2 x WSRC x 32 bytes
-constexpr int W_FARXY = 0;                           // WFAR x float4 (x, x, y, y), aliases W_SRC
-constexpr int W_FARM = W_FARXY + WFAR * 16;          // WFAR x float2 (M, M), aliases W_SRC
-constexpr int W_NBOX = W_SRC + 2 * WSRC * 32;        // (WDESC + 1) x int
-constexpr int W_NPRE = W_NBOX + (WDESC + 1) * 4;     // (WDESC + 1) x int
 constexpr int NRUN = MAX_TG * MAX_TG;                // target runs (boxes) of a work item
-constexpr int W_RUN = W_NPRE + (WDESC + 1) * 4;      // 2 x (NRUN + 1) x int
-constexpr int W_MBAR = (W_RUN + 2 * (NRUN + 1) * 4 + 7) / 8 * 8;  // 2 x uint64
-constexpr int W_CNT = W_MBAR + 16;                   // 2 x uint64: the warp's near, far pair counts
-constexpr int W_BYTES = (W_CNT + 16 + 127) / 128 * 128;
-constexpr size_t FS_SMEM = (size_t)FW * W_BYTES;
-static_assert(W_FARM + WFAR * 8 <= W_NBOX, "far staging must fit in the near-source buffers");
-static_assert(2 * 32 * NR * sizeof(float) <= (size_t)W_NBOX, "slice partials alias the source buffers");
+
+// Per-warp shared-memory carve-up (bytes) of the build with MINB CTAs per SM.  The far phase of an
+// item ends before its near phase starts, and the slice reduction follows both, so the far staging
+// and the reduction buffer share the two near-source buffers.  WSRC near sources per bulk-copy
+// pass: the largest pass that keeps MINB CTAs of FW warps within the SM's shared memory (the
+// 8-CTA build, which spills, also leaves L1 room for its spills): 88 at 8 CTAs, 120 at 6.
+template <int MINB>
+struct FsLayout {
+    static constexpr int WSRC = MINB >= 8 ? 88 : 120;
+    static constexpr int W_SRC = 0;                             // 2 x WSRC x 32 bytes
+    static constexpr int W_FARXY = 0;                           // WFAR x float4 (x, x, y, y)
+    static constexpr int W_FARM = W_FARXY + WFAR * 16;          // WFAR x float2 (M, M)
+    static constexpr int W_NBOX = W_SRC + 2 * WSRC * 32;        // (WDESC + 1) x int
+    static constexpr int W_NPRE = W_NBOX + (WDESC + 1) * 4;     // (WDESC + 1) x int
+    static constexpr int W_RUN = W_NPRE + (WDESC + 1) * 4;      // 2 x (NRUN + 1) x int
+    static constexpr int W_MBAR = (W_RUN + 2 * (NRUN + 1) * 4 + 7) / 8 * 8;  // 2 x uint64
+    static constexpr int W_CNT = W_MBAR + 16;   // 2 x uint64: the warp's near, far pair counts
+    static constexpr int W_BYTES = (W_CNT + 16 + 127) / 128 * 128;
+    static constexpr size_t SMEM = (size_t)FW * W_BYTES;
+    static_assert(W_FARM + WFAR * 8 <= W_NBOX, "far staging must fit in the near-source buffers");
+    static_assert(2 * 32 * NR * sizeof(float) <= (size_t)W_NBOX, "slice partials alias the source buffers");
+    static_assert((WSRC * 32) % 16 == 0 && W_BYTES % 128 == 0, "bulk-copy destinations must be 16-byte aligned");
+    static_assert(MINB * (SMEM + 1024) <= 228 * 1024, "MINB CTAs must fit in the SM's shared memory");
+};
 static_assert(32 * NR >= STREAM_CHUNK, "a warp must cover every target of a work item");
 static_assert(WFAR % 32 == 0, "far staging passes are whole lane rounds");
-static_assert((WSRC * 32) % 16 == 0 && W_BYTES % 128 == 0, "bulk-copy destinations must be 16-byte aligned");
 
 template <bool KAHAN, int MINB>
 __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, int accumulate) {
     extern __shared__ __align__(128) unsigned char smem[];
+    using Ly = FsLayout<MINB>;
+    constexpr int WSRC = Ly::WSRC;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned char *ws = smem + warp * W_BYTES;
-    float4 *farxy = reinterpret_cast<float4 *>(ws + W_FARXY);
-    float2 *farm = reinterpret_cast<float2 *>(ws + W_FARM);
-    unsigned char *srcb = ws + W_SRC;
-    int *nbox = reinterpret_cast<int *>(ws + W_NBOX);
-    int *npre = reinterpret_cast<int *>(ws + W_NPRE);
-    int *rstart = reinterpret_cast<int *>(ws + W_RUN);  // first particle of target run r
+    unsigned char *ws = smem + warp * Ly::W_BYTES;
+    float4 *farxy = reinterpret_cast<float4 *>(ws + Ly::W_FARXY);
+    float2 *farm = reinterpret_cast<float2 *>(ws + Ly::W_FARM);
+    unsigned char *srcb = ws + Ly::W_SRC;
+    int *nbox = reinterpret_cast<int *>(ws + Ly::W_NBOX);
+    int *npre = reinterpret_cast<int *>(ws + Ly::W_NPRE);
+    int *rstart = reinterpret_cast<int *>(ws + Ly::W_RUN);  // first particle of target run r
     int *rpre = rstart + NRUN + 1;                       // exclusive prefix of the run lengths
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(ws + W_MBAR);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(ws + Ly::W_MBAR);
     float *red = reinterpret_cast<float *>(ws);  // aliases the source buffers
 
     const int nxt = (d.glob->epoch + 1) & 1;
     const double *Xs = d.X[nxt], *Ys = d.Y[nxt];
     const long long nitems = d.sitem_off[d.NG_total];
-    unsigned long long *wcnt = reinterpret_cast<unsigned long long *>(ws + W_CNT);  // lane 0 counts
+    unsigned long long *wcnt = reinterpret_cast<unsigned long long *>(ws + Ly::W_CNT);  // lane 0 counts
     uint32_t phases = 0u;  // bit b: parity of buffer b's current mbarrier phase
     bool tma_ok = true;  // warp-uniform; cleared (and flagged) when a copy wait times out
     if (lane == 0) {
@@ -205,7 +213,7 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                 f2_t px2[NR / 2], py2[NR / 2];
 #pragma unroll
                 for (int kk = 0; kk < NR / 2; kk++) px2[kk] = py2[kk] = f2_pack(0.f, 0.f);
-#pragma unroll 2
+#pragma unroll 4
                 for (int k = slice; k < nf; k += nslice) {
                     const ulonglong2 rxy = fp[k];  // (rx, rx), (ry, ry)
                     const f2_t mm = fm[k];         // (M, M)
@@ -389,7 +397,7 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                 }
                 __syncwarp();
                 if (active) {
-#pragma unroll 2
+#pragma unroll 4
                     for (int j = slice; j < ns; j += nslice) {
                         const ulonglong2 sxy = *reinterpret_cast<const ulonglong2 *>(s4 + 2 * j);
                         const f2_t mm = *reinterpret_cast<const f2_t *>(s4 + 2 * j + 1);
@@ -475,7 +483,7 @@ static cudaError_t launch_fstream_t(const DevPlan &d, bool tick, bool accumulate
     cudaError_t e = cudaMemsetAsync(&d.glob->item_next, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     if (ev && (e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
-    k_fstream<KAHAN, MINB><<<(unsigned)grid, FW * 32, FS_SMEM, st>>>(d, tick ? 1 : 0, accumulate ? 1 : 0);
+    k_fstream<KAHAN, MINB><<<(unsigned)grid, FW * 32, FsLayout<MINB>::SMEM, st>>>(d, tick ? 1 : 0, accumulate ? 1 : 0);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     return ev ? cudaEventRecord(ev[1], st) : cudaSuccess;
 }
@@ -483,7 +491,7 @@ static cudaError_t launch_fstream_t(const DevPlan &d, bool tick, bool accumulate
 template <bool KAHAN, int MINB>
 static cudaError_t init_fstream_t() {
     return cudaFuncSetAttribute(k_fstream<KAHAN, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)FS_SMEM);
+                                (int)FsLayout<MINB>::SMEM);
 }
 
 cudaError_t fstream_init() {

@@ -556,25 +556,29 @@ constexpr int SUM_THREADS = 256;
 constexpr int SUM_WARPS = SUM_THREADS / 32;
 constexpr int SUM_CELLS = 256 + 64 + 16 + 4 + 1;  // a tile's cells at levels 0..4
 
-// Cell (I, J) of level l of system s from its up to four level-(l-1) children (c: their moments,
-// child (a, b) at c + 6 * (2 * a + b), flag has_child[2 * a + b]), shifted to the parent origin.
-__device__ __forceinline__ void shift_children(const double *c, const bool *has, int l, double step,
-                                               double *p) {
+// The moments of child (a, b) of a level-l cell (q, FP64 about the child's origin) shifted to the
+// cell origin, into o[6]; zeros when the child lies outside the grid.  sum_children adds a cell's
+// four shifted children in (0, 0), (0, 1), (1, 0), (1, 1) order.
+__device__ __forceinline__ void child_terms(const double *q, bool has, int a, int b, int l, double step,
+                                            double *o) {
+    if (!has) {
 #pragma unroll
-    for (int k = 0; k < 6; k++) p[k] = 0.0;
-    for (int a = 0; a < 2; a++)
-        for (int b = 0; b < 2; b++) {
-            if (!has[2 * a + b]) continue;
-            const double *q = c + 6 * (2 * a + b);
-            double dx = (double)(a << (l - 1)) * step, dy = (double)(b << (l - 1)) * step;
-            double M = q[0], Sx = q[1], Sy = q[2];
-            p[0] += M;
-            p[1] += Sx + M * dx;
-            p[2] += Sy + M * dy;
-            p[3] += q[3] + 2.0 * dx * Sx + M * dx * dx;
-            p[4] += q[4] + dx * Sy + dy * Sx + M * dx * dy;
-            p[5] += q[5] + 2.0 * dy * Sy + M * dy * dy;
-        }
+        for (int k = 0; k < 6; k++) o[k] = 0.0;
+        return;
+    }
+    const double dx = (double)(a << (l - 1)) * step, dy = (double)(b << (l - 1)) * step;
+    const double M = q[0], Sx = q[1], Sy = q[2];
+    o[0] = M;
+    o[1] = Sx + M * dx;
+    o[2] = Sy + M * dy;
+    o[3] = q[3] + 2.0 * dx * Sx + M * dx * dx;
+    o[4] = q[4] + dx * Sy + dy * Sx + M * dx * dy;
+    o[5] = q[5] + 2.0 * dy * Sy + M * dy * dy;
+}
+
+__device__ __forceinline__ void sum_children(const double *t, double *p) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) p[k] = ((t[k] + t[6 + k]) + t[12 + k]) + t[18 + k];
 }
 
 // Float records of cell c (level l) of system s: centre of mass relative to the cell origin and
@@ -601,6 +605,7 @@ __device__ __forceinline__ void cell_record(const DevPlan &d, long long c, int l
 // leaves_given: the leaf moments are already in d.mom (bh_set_leaf_moments); build the rest.
 __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int second, int leaves_given) {
     __shared__ double cm[SUM_CELLS * 6];  // the tile's cells, level by level
+    __shared__ double chm[4 * 64 * 6];    // shifted child moments: 64 cells x 4 children
     __shared__ unsigned ticket;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int loff[5] = {0, 256, 320, 336, 340};
@@ -632,13 +637,25 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
                 float cs[6], cc[6];
 #pragma unroll
                 for (int q = 0; q < 6; q++) cs[q] = cc[q] = 0.f;
+                // the next chunk's key and record are loaded while this one is summed
+                int nkey = -1;
+                float4 np = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (i0 + lane < i1) {
+                    nkey = d.skey[i0 + lane];
+                    np = d.P[i0 + lane];
+                }
                 for (int c = i0; c < i1; c += 32) {
                     const int i = c + lane;
                     int key = -1;
                     float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                    const int ckey_in = nkey;
+                    const float4 p = np;
+                    if (i + 32 < i1) {
+                        nkey = d.skey[i + 32];
+                        np = d.P[i + 32];
+                    }
                     if (i < i1) {
-                        key = d.skey[i] - (int)b0;  // box within the row
-                        const float4 p = d.P[i];
+                        key = ckey_in - (int)b0;  // box within the row
                         v[0] = p.z;
                         v[1] = p.z * p.x;
                         v[2] = p.z * p.y;
@@ -719,43 +736,43 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
                     d.mom[6 * (sd.coff + (long long)(bx0 + cx) * G + (by0 + cy)) + (k - 6 * box)] = cm[k];
             }
         }
-        // ---- levels 1..lmax inside the tile
+        // ---- levels 1..lmax inside the tile: a thread per (cell, child) shifts the child's
+        // moments to the cell origin, then a thread per cell adds its four children in order
         for (int l = 1; l <= lmax; l++) {
             const int nl = SUM_TILE >> l, nc = nl << 1;  // cells per side at l and l - 1
             const int gl = sd.lvg[l], gc = sd.lvg[l - 1];
             const int I0 = bx0 >> l, J0 = by0 >> l;
-            if (tid < nl * nl) {
-                const int ci = tid / nl, cj = tid - ci * nl;
-                double ch[24], p[6];
-                bool has[4];
-                for (int a = 0; a < 2; a++)
-                    for (int b = 0; b < 2; b++) {
-                        const int li = 2 * ci + a, lj = 2 * cj + b;
-                        has[2 * a + b] = 2 * (I0 + ci) + a < gc && 2 * (J0 + cj) + b < gc;
-                        for (int k = 0; k < 6; k++) ch[6 * (2 * a + b) + k] = cm[6 * (loff[l - 1] + li * nc + lj) + k];
-                    }
-                shift_children(ch, has, l, step, p);
+            for (int t = tid; t < 4 * nl * nl; t += SUM_THREADS) {
+                const int cell = t >> 2, a = (t >> 1) & 1, b = t & 1;
+                const int ci = cell / nl, cj = cell - ci * nl;
+                const bool has = 2 * (I0 + ci) + a < gc && 2 * (J0 + cj) + b < gc;
+                child_terms(cm + 6 * (loff[l - 1] + (2 * ci + a) * nc + (2 * cj + b)), has, a, b, l,
+                            step, chm + 6 * t);
+            }
+            __syncthreads();
+            for (int c = tid; c < nl * nl; c += SUM_THREADS) {
+                const int ci = c / nl, cj = c - ci * nl;
                 const bool inside = I0 + ci < gl && J0 + cj < gl;
-                for (int k = 0; k < 6; k++) cm[6 * (loff[l] + tid) + k] = inside ? p[k] : 0.0;
+                double p[6];
+                sum_children(chm + 24 * c, p);
+#pragma unroll
+                for (int k = 0; k < 6; k++) cm[6 * (loff[l] + c) + k] = inside ? p[k] : 0.0;
                 if (inside) {
-                    double *q = d.mom + 6 * (sd.coff + sd.lvoff[l] + (long long)(I0 + ci) * gl + (J0 + cj));
-                    for (int k = 0; k < 6; k++) q[k] = p[k];
+                    const long long cc = sd.coff + sd.lvoff[l] + (long long)(I0 + ci) * gl + (J0 + cj);
+#pragma unroll
+                    for (int k = 0; k < 6; k++) d.mom[6 * cc + k] = p[k];
+                    cell_record(d, cc, l, step, p, second);
                 }
             }
             __syncthreads();
         }
-        // ---- records of the tile's cells
-        for (int l = 0; l <= lmax; l++) {
-            const int nl = SUM_TILE >> l, gl = sd.lvg[l];
-            const int I0 = bx0 >> l, J0 = by0 >> l;
-            for (int k = tid; k < nl * nl; k += SUM_THREADS) {
-                const int ci = k / nl, cj = k - ci * nl;
-                if (I0 + ci >= gl || J0 + cj >= gl) continue;
-                const long long c = sd.coff + sd.lvoff[l] + (long long)(I0 + ci) * gl + (J0 + cj);
-                cell_record(d, c, l, step, cm + 6 * (loff[l] + k), second);
-            }
+        // ---- records of the tile's boxes
+        for (int k = tid; k < SUM_TILE * SUM_TILE; k += SUM_THREADS) {
+            const int cx = k / SUM_TILE, cy = k - cx * SUM_TILE;
+            if (cx >= nbx || cy >= nby) continue;
+            cell_record(d, sd.coff + (long long)(bx0 + cx) * G + (by0 + cy), 0, step, cm + 6 * k, second);
         }
-        // ---- the system's last tile builds the levels above the tiles
+        // ---- the system's last tile builds the levels above the tiles, 64 cells at a time
         __threadfence();
         __syncthreads();
         if (tid == 0) ticket = atomicAdd(&d.dyn[s].tiles_done, 1u);
@@ -764,21 +781,30 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
             __threadfence();
             for (int l = lmax + 1; l < sd.L; l++) {
                 const int gl = sd.lvg[l], gc = sd.lvg[l - 1];
-                for (int k = tid; k < gl * gl; k += SUM_THREADS) {
-                    const int I = k / gl, J = k - I * gl;
-                    double ch[24], p[6];
-                    bool has[4];
-                    for (int a = 0; a < 2; a++)
-                        for (int b = 0; b < 2; b++) {
-                            const int ci = 2 * I + a, cj = 2 * J + b;
-                            has[2 * a + b] = ci < gc && cj < gc;
-                            const double *q = d.mom + 6 * (sd.coff + sd.lvoff[l - 1] + (long long)ci * gc + cj);
-                            for (int c = 0; c < 6; c++) ch[6 * (2 * a + b) + c] = has[2 * a + b] ? __ldcg(q + c) : 0.0;
+                for (int c0 = 0; c0 < gl * gl; c0 += 64) {
+                    const int t = tid, cell = c0 + (t >> 2), a = (t >> 1) & 1, b = t & 1;
+                    if (cell < gl * gl) {
+                        const int I = cell / gl, J = cell - I * gl;
+                        const int ci = 2 * I + a, cj = 2 * J + b;
+                        const bool has = ci < gc && cj < gc;
+                        double q[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+                        if (has) {
+                            const double *src = d.mom + 6 * (sd.coff + sd.lvoff[l - 1] + (long long)ci * gc + cj);
+#pragma unroll
+                            for (int k = 0; k < 6; k++) q[k] = __ldcg(src + k);
                         }
-                    shift_children(ch, has, l, step, p);
-                    const long long c = sd.coff + sd.lvoff[l] + k;
-                    for (int q = 0; q < 6; q++) d.mom[6 * c + q] = p[q];
-                    cell_record(d, c, l, step, p, second);
+                        child_terms(q, has, a, b, l, step, chm + 6 * t);
+                    }
+                    __syncthreads();
+                    if (tid < 64 && c0 + tid < gl * gl) {
+                        double p[6];
+                        sum_children(chm + 24 * tid, p);
+                        const long long cc = sd.coff + sd.lvoff[l] + c0 + tid;
+#pragma unroll
+                        for (int k = 0; k < 6; k++) d.mom[6 * cc + k] = p[k];
+                        cell_record(d, cc, l, step, p, second);
+                    }
+                    __syncthreads();
                 }
                 __threadfence();
                 __syncthreads();
