@@ -32,7 +32,7 @@ struct bh_plan {
     size_t ws_bytes = 0;
     size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_toff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
-    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_sst, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
+    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_sst, o_leafpart, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
         o_rec2, o_org, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk, o_qcnt;
     bool stream = false;  // theta-mode interaction lists built once per group and streamed
     int chunk = TARGET_CHUNK;
@@ -288,6 +288,7 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_sichk = take(8 * sitems);
     p->o_ibkt = take(p->stream ? 4 * 2 * ITEM_BUCKETS : 0);
     p->o_mom = take(48 * C);
+    p->o_leafpart = take(48 * (N / 32 + 1));
     p->o_rec = take(16 * C);
     p->o_rec2 = take(16 * C);
     p->o_org = take(8 * (size_t)p->org_total);
@@ -361,6 +362,7 @@ static void fill_dev(bh_plan *p) {
     d.item_off = (int *)(w + p->o_ioff);
     d.item_group = (int *)(w + p->o_igrp);
     d.mom = (double *)(w + p->o_mom);
+    d.leafpart = (float *)(w + p->o_leafpart);
     d.rec = (float4 *)(w + p->o_rec);
     d.rec2 = (float4 *)(w + p->o_rec2);
     d.org = (double *)(w + p->o_org);
@@ -625,12 +627,12 @@ extern "C" int bh_force_kernel_ms(bh_plan *p, float *ms) {
 
 extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     if (!p || !count) return BH_ERR_INVALID;
-    // prologue, box scan, summarize; with particles also bbox (which finalises the box), place,
-    // scatter, force (and before it, when streaming, the list build and the two kernels of the
-    // heaviest-first item order); work items: count, scan, fill for the walk or the learned
-    // correction, one kernel for list streaming
+    // prologue, box scan, summarize tiles; with particles also bbox (which finalises the box),
+    // place, scatter, leaf sums, force (and before it, when streaming, the list build and the two
+    // kernels of the heaviest-first item order); work items: count, scan, fill for the walk or
+    // the learned correction, one kernel for list streaming
     const bool walk_items = !p->stream || (p->params.flags & BH_FLAG_LEARNED);
-    *count = 1 + 1 + (walk_items ? 3 : 0) + 1 + (p->n_total > 0 ? 4 : 0) + (p->stream ? 1 : 0) +
+    *count = 1 + 1 + (walk_items ? 3 : 0) + 1 + (p->n_total > 0 ? 5 : 0) + (p->stream ? 1 : 0) +
              (p->stream && p->n_total > 0 ? 3 : 0);
     return BH_OK;
 }

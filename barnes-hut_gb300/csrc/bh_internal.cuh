@@ -118,6 +118,7 @@ struct DevPlan {
     int *item_cnt, *item_off, *item_group;  // force work items (group, target chunk)
     double *org;  // per system: box origins mn + k step along x (k < G), then along y, FP64
     double *mom;
+    float *leafpart;  // per chunk of 32 box-sorted particles: head and tail partial moments (k_leaf)
     float4 *rec, *rec2;
     // interaction lists of every target group (list-streaming path), in fixed per-group slots
     // (SysDesc lfcap far entries, lncap + 1 near descriptors), counts in lcnt (x far, y near):

@@ -602,6 +602,78 @@ __device__ __forceinline__ void cell_record(const DevPlan &d, long long c, int l
     }
 }
 
+// Leaf moments, balanced over the particles: a warp per chunk of 32 box-sorted particles sums
+// each box's part of the chunk with a segmented FP32 scan (offsets are box-relative, so 32 terms
+// keep ~1e-7 of a box edge).  A box that lies inside the chunk gets its FP64 moments written
+// here; a box that starts before the chunk leaves its part in the chunk's head partial, a box
+// that runs past it in the tail partial (a chunk of one box that runs both ways: both), and
+// k_summarize adds a multi-chunk box's partials in chunk order.  No atomics: fixed summation
+// order.
+__global__ void __launch_bounds__(TPB) k_leaf(DevPlan d) {
+    const int lane = threadIdx.x & 31;
+    const long long nch = (d.n_total + 31) >> 5;
+    for (long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nch;
+         c += ((long long)gridDim.x * blockDim.x) >> 5) {
+        const long long i = (c << 5) + lane;
+        int key = -1;
+        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (i < d.n_total) {
+            key = d.skey[i];
+            const float4 p = d.P[i];
+            v[0] = p.z;
+            v[1] = p.z * p.x;
+            v[2] = p.z * p.y;
+            v[3] = v[1] * p.x;
+            v[4] = v[1] * p.y;
+            v[5] = v[2] * p.y;
+        }
+        // the keys just before and after the chunk tell whether its first and last boxes go on
+        int kprev = -1, knext_chunk = -1;
+        if (lane == 0 && c > 0) kprev = d.skey[(c << 5) - 1];
+        if (lane == 0 && (c << 5) + 32 < d.n_total) knext_chunk = d.skey[(c << 5) + 32];
+        kprev = __shfl_sync(0xffffffffu, kprev, 0);
+        knext_chunk = __shfl_sync(0xffffffffu, knext_chunk, 0);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int k2 = __shfl_up_sync(0xffffffffu, key, o);
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                const float y = __shfl_up_sync(0xffffffffu, v[q], o);
+                if (lane >= o && k2 == key) v[q] += y;
+            }
+        }
+        const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+        const int kfirst = __shfl_sync(0xffffffffu, key, 0);
+        const bool last = key >= 0 && (lane == 31 || knext != key);  // the segment's last lane
+        if (last) {
+            const bool head = key == kfirst && key == kprev;        // began in an earlier chunk
+            const bool tail = lane == 31 && key == knext_chunk;     // goes on in a later chunk
+            if (head || tail) {
+                float *pt = d.leafpart + 12 * c;
+                if (head)
+#pragma unroll
+                    for (int q = 0; q < 6; q++) pt[q] = v[q];
+                if (tail)
+#pragma unroll
+                    for (int q = 0; q < 6; q++) pt[6 + q] = v[q];
+            } else {
+                const int s = find_seg(d.boff_tab, d.nsys, key);
+                double *m = d.mom + 6 * (d.sys[s].coff + (key - d.sys[s].boff));
+#pragma unroll
+                for (int q = 0; q < 6; q++) m[q] = f32_to_f64(v[q]);
+            }
+        }
+    }
+}
+
+// (s, c) += x, Kahan-compensated in FP32
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+}
+
 // leaves_given: the leaf moments are already in d.mom (bh_set_leaf_moments); build the rest.
 __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int second, int leaves_given) {
     __shared__ double cm[SUM_CELLS * 6];  // the tile's cells, level by level
@@ -627,107 +699,32 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
         }
         __syncthreads();
         if (!leaves_given) {
-            for (int cx = warp; cx < nbx; cx += SUM_WARPS) {
-                const long long b0 = sd.boff + (long long)(bx0 + cx) * G + by0;  // the row's first box
-                const int i0 = d.box_start[b0], i1 = d.box_start[b0 + nby];
-                double *row = cm + 6 * cx * SUM_TILE;
-                // the box still open at the end of the previous chunk: its Kahan-compensated FP32
-                // sums (s, c), the same in every lane
-                int ckey = -1;
-                float cs[6], cc[6];
+            // a box inside one chunk has its moments from k_leaf; a box over several chunks adds
+            // its partials in chunk order: the first chunk's tail, whole middle chunks, the last
+            // chunk's head
+            for (int k = tid; k < SUM_TILE * SUM_TILE; k += SUM_THREADS) {
+                const int cx = k / SUM_TILE, cy = k - cx * SUM_TILE;
+                if (cx >= nbx || cy >= nby) continue;
+                const long long lb = (long long)(bx0 + cx) * G + (by0 + cy);
+                const int i0 = d.box_start[sd.boff + lb], i1 = d.box_start[sd.boff + lb + 1];
+                if (i1 == i0) continue;  // empty: zeros
+                const long long c0 = i0 >> 5, c1 = (long long)(i1 - 1) >> 5;
+                if (c0 == c1) {
 #pragma unroll
-                for (int q = 0; q < 6; q++) cs[q] = cc[q] = 0.f;
-                // the next chunk's key and record are loaded while this one is summed
-                int nkey = -1;
-                float4 np = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (i0 + lane < i1) {
-                    nkey = d.skey[i0 + lane];
-                    np = d.P[i0 + lane];
+                    for (int q = 0; q < 6; q++) cm[6 * k + q] = d.mom[6 * (sd.coff + lb) + q];
+                    continue;
                 }
-                for (int c = i0; c < i1; c += 32) {
-                    const int i = c + lane;
-                    int key = -1;
-                    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                    const int ckey_in = nkey;
-                    const float4 p = np;
-                    if (i + 32 < i1) {
-                        nkey = d.skey[i + 32];
-                        np = d.P[i + 32];
-                    }
-                    if (i < i1) {
-                        key = ckey_in - (int)b0;  // box within the row
-                        v[0] = p.z;
-                        v[1] = p.z * p.x;
-                        v[2] = p.z * p.y;
-                        v[3] = v[1] * p.x;
-                        v[4] = v[1] * p.y;
-                        v[5] = v[2] * p.y;
-                    }
+                float sm_[6], cc_[6];
 #pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int k2 = __shfl_up_sync(0xffffffffu, key, o);
-#pragma unroll
-                        for (int q = 0; q < 6; q++) {
-                            const float y = __shfl_up_sync(0xffffffffu, v[q], o);
-                            if (lane >= o && k2 == key) v[q] += y;
-                        }
-                    }
-                    const int knext = __shfl_down_sync(0xffffffffu, key, 1);
-                    const int kfirst = __shfl_sync(0xffffffffu, key, 0);
-                    const int klast = __shfl_sync(0xffffffffu, key, 31);
-                    if (ckey >= 0 && ckey != kfirst && lane < 6) {  // the open box ended with the last chunk
-                        float r = cs[0];
-#pragma unroll
-                        for (int q = 1; q < 6; q++)
-                            if (lane == q) r = cs[q];
-                        float e = cc[0];
-#pragma unroll
-                        for (int q = 1; q < 6; q++)
-                            if (lane == q) e = cc[q];
-                        row[6 * ckey + lane] = f32_to_f64(__fsub_rn(r, e));
-                    }
-                    // boxes that end inside this chunk: a segment's last lane, not lane 31
-                    if (key >= 0 && lane < 31 && knext != key) {
-                        const bool cont = key == ckey;  // the first segment continues the open box
-#pragma unroll
-                        for (int q = 0; q < 6; q++) {
-                            float tot = v[q];
-                            if (cont) {  // (s, c) + v, compensated, then s - c
-                                const float y = __fsub_rn(v[q], cc[q]);
-                                const float t = __fadd_rn(cs[q], y);
-                                const float cn = __fsub_rn(__fsub_rn(t, cs[q]), y);
-                                tot = __fsub_rn(t, cn);
-                            }
-                            row[6 * key + q] = f32_to_f64(tot);
-                        }
-                    }
-                    // the box open at lane 31 carries into the next chunk
-#pragma unroll
-                    for (int q = 0; q < 6; q++) {
-                        const float v31 = __shfl_sync(0xffffffffu, v[q], 31);
-                        if (klast >= 0 && klast == ckey && kfirst == ckey) {
-                            const float y = __fsub_rn(v31, cc[q]);
-                            const float t = __fadd_rn(cs[q], y);
-                            cc[q] = __fsub_rn(__fsub_rn(t, cs[q]), y);
-                            cs[q] = t;
-                        } else {
-                            cs[q] = v31;
-                            cc[q] = 0.f;
-                        }
-                    }
-                    ckey = klast;
-                    __syncwarp();
+                for (int q = 0; q < 6; q++) {
+                    sm_[q] = d.leafpart[12 * c0 + 6 + q];
+                    cc_[q] = 0.f;
                 }
-                if (ckey >= 0 && lane < 6) {  // the row's last box
-                    float r = cs[0], e = cc[0];
+                for (long long c = c0 + 1; c <= c1; c++)
 #pragma unroll
-                    for (int q = 1; q < 6; q++)
-                        if (lane == q) {
-                            r = cs[q];
-                            e = cc[q];
-                        }
-                    row[6 * ckey + lane] = f32_to_f64(__fsub_rn(r, e));
-                }
+                    for (int q = 0; q < 6; q++) kahan_add(sm_[q], cc_[q], d.leafpart[12 * c + q]);
+#pragma unroll
+                for (int q = 0; q < 6; q++) cm[6 * k + q] = f32_to_f64(__fsub_rn(sm_[q], cc_[q]));
             }
             __syncthreads();
             for (int k = tid; k < 6 * SUM_TILE * SUM_TILE; k += SUM_THREADS) {
@@ -891,6 +888,7 @@ cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
     return cudaGetLastError();
 }
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st) {
+    if (d.n_total > 0) k_leaf<<<grid_for((d.n_total + 31) / 32, TPB / 32, d.nsm * 8LL), TPB, 0, st>>>(d);
     // the normalised second moments feed only the learned correction
     k_summarize<<<grid_for(d.T_total, 1, d.nsm * 8LL), SUM_THREADS, 0, st>>>(d, d.learned != 0, 0);
     return cudaGetLastError();
