@@ -32,7 +32,7 @@ struct bh_plan {
     size_t ws_bytes = 0;
     size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_toff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
-    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_sst, o_leafpart, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
+    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_sst, o_leafpart, o_perm, o_bigseg, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
         o_rec2, o_org, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk, o_qcnt;
     bool stream = false;  // theta-mode interaction lists built once per group and streamed
     int chunk = TARGET_CHUNK;
@@ -264,6 +264,8 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_key = take(4 * N);
     p->o_slot = take(4 * N);
     p->o_skey = take(4 * N);
+    p->o_perm = take(4 * N);
+    p->o_bigseg = take(8 * (N / 17 + 1));  // quadrants of more than 16 particles: at most N / 17
     p->o_counts = take(4 * B);
     p->o_qcnt = take(16 * B);
     p->o_bstart = take(4 * (B + 1));
@@ -352,6 +354,8 @@ static void fill_dev(bh_plan *p) {
     d.key = (int *)(w + p->o_key);
     d.slot = (int *)(w + p->o_slot);
     d.skey = (int *)(w + p->o_skey);
+    d.perm = (int *)(w + p->o_perm);
+    d.bigseg = (int2 *)(w + p->o_bigseg);
     d.counts = (int *)(w + p->o_counts);
     d.qcounts = (int *)(w + p->o_qcnt);
     d.box_start = (int *)(w + p->o_bstart);
@@ -628,11 +632,12 @@ extern "C" int bh_force_kernel_ms(bh_plan *p, float *ms) {
 extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     if (!p || !count) return BH_ERR_INVALID;
     // prologue, box scan, summarize tiles; with particles also bbox (which finalises the box),
-    // place, scatter, leaf sums, force (and before it, when streaming, the list build and the two
-    // kernels of the heaviest-first item order); work items: count, scan, fill for the walk or
-    // the learned correction, one kernel for list streaming
+    // place, the scatter's four kernels (permutation, quadrant sort, long quadrants, gather), leaf
+    // sums, force (and before it, when streaming, the list build and the two kernels of the
+    // heaviest-first item order); work items: count, scan, fill for the walk or the learned
+    // correction, one kernel for list streaming
     const bool walk_items = !p->stream || (p->params.flags & BH_FLAG_LEARNED);
-    *count = 1 + 1 + (walk_items ? 3 : 0) + 1 + (p->n_total > 0 ? 5 : 0) + (p->stream ? 1 : 0) +
+    *count = 1 + 1 + (walk_items ? 3 : 0) + 1 + (p->n_total > 0 ? 8 : 0) + (p->stream ? 1 : 0) +
              (p->stream && p->n_total > 0 ? 3 : 0);
     return BH_OK;
 }

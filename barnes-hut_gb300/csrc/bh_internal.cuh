@@ -85,6 +85,7 @@ struct Globals {
     unsigned int scan_ticket[3];    // next tile of each single-pass scan (its last tile resets it)
     unsigned int scan_gen[3];       // generation of each scan's tile states (its last tile bumps it)
     unsigned int bbox_done;         // bounding-box blocks finished (the last one finalises)
+    unsigned int nbig;              // entries of the long-quadrant list (k_segsort)
 };
 
 struct DevPlan {
@@ -109,6 +110,8 @@ struct DevPlan {
                  // packed near-field record (offsets from the box origin; box coordinates),
                  // staged into shared memory by bulk copies
     int *key, *slot, *skey;
+    int *perm;     // box-sorted position -> input index (k_perm, k_segsort)
+    int2 *bigseg;  // quadrant stretches too long for a thread's registers: (first, count)
     int *counts, *box_start;
     // single-pass scans (decoupled look-back): per-tile states of the box scan, the walk items'
     // scan and the streaming items' scan (generation << 34 | flag << 32 | value)

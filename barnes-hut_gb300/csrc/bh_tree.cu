@@ -1,7 +1,7 @@
 // bh_tree.cu -- create_tree and summarize kernels.
 //
 // create_tree = prologue -> bbox (its last block squares the box) -> place -> scan (one pass)
-//   -> scatter -> work items (one pass).
+//   -> scatter (permutation, per-quadrant sort, gather) -> work items (one pass).
 //   Replaces set_particles_bounding_box (python-bh/barneshut/implementations/base.py:211-239),
 //   g_place_particles, g_calculate_box_cumm, g_sort_particles
 //   (python-bh/barneshut/kernels/grid_decomposition/gpu/grid.py:15-76).
@@ -471,42 +471,172 @@ __global__ void __launch_bounds__(SITEM_TILE) k_sitems(DevPlan d) {
 }
 
 // ------------------------------------------------------------------ scatter
-// Counting-sort scatter into box order, each box's particles quadrant by quadrant:
-// destination = box_start[box] + (particles of the box's earlier quadrants) + slot.
-// Writes the FP64 state of the next buffer, the packed float4 record (offsets
-// from the box origin computed in FP64, rounded once to float) and the
-// per-sorted-particle key.
-__global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
+// Counting sort into box order, each box's particles quadrant by quadrant, and within a quadrant
+// in input order (the order the previous step left, or the caller's), so the step does not depend
+// on the order in which k_place's atomics handed out slots:
+//   k_perm     perm[box_start + earlier quadrants + slot] = input index (slots: k_place);
+//   k_segsort  each quadrant's stretch of perm sorted ascending -- up to SEG_REG entries in a
+//              thread's registers, longer ones listed for k_segsort_big (a CTA each: a bitonic
+//              network in shared memory up to SEG_SMEM entries, beyond that four stable 8-bit
+//              radix passes through the dead slot array);
+//   k_gather   output particle t takes input perm[t]: the FP64 state of the next buffer, the
+//              packed float4 record (offsets from the box origin computed in FP64, rounded once
+//              to float), the 32-byte near-source record and the sorted key.
+constexpr int SEG_REG = 16;
+constexpr int SEG_SMEM = 4096;
+
+__device__ __forceinline__ int quad_first(const DevPlan &d, int key4) {
+    const int box = key4 >> 2, quad = key4 & 3;
+    const int4 qc = reinterpret_cast<const int4 *>(d.qcounts)[box];
+    return d.box_start[box] + (quad > 0 ? qc.x : 0) + (quad > 1 ? qc.y : 0) + (quad > 2 ? qc.z : 0);
+}
+
+__global__ void __launch_bounds__(TPB) k_perm(DevPlan d) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < d.n_total; i += stride)
+        d.perm[quad_first(d, d.key[i]) + d.slot[i]] = (int)i;
+}
+
+__global__ void __launch_bounds__(TPB) k_segsort(DevPlan d) {
+    const long long nq = 4 * d.B_total, stride = (long long)gridDim.x * blockDim.x;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
+        const int n = d.qcounts[q];
+        if (n < 2) continue;
+        const int s0 = quad_first(d, (int)q);
+        if (n > SEG_REG) {
+            const unsigned k = atomicAdd(&d.glob->nbig, 1u);
+            d.bigseg[k] = make_int2(s0, n);
+            continue;
+        }
+        int v[SEG_REG];
+#pragma unroll
+        for (int k = 0; k < SEG_REG; k++) v[k] = k < n ? d.perm[s0 + k] : 0x7FFFFFFF;
+        // odd-even transposition network: SEG_REG rounds sort SEG_REG entries
+#pragma unroll
+        for (int r = 0; r < SEG_REG; r++)
+#pragma unroll
+            for (int k = r & 1; k + 1 < SEG_REG; k += 2) {
+                const int lo = min(v[k], v[k + 1]), hi = max(v[k], v[k + 1]);
+                v[k] = lo;
+                v[k + 1] = hi;
+            }
+#pragma unroll
+        for (int k = 0; k < SEG_REG; k++)
+            if (k < n) d.perm[s0 + k] = v[k];
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_segsort_big(DevPlan d) {
+    __shared__ int sv[SEG_SMEM];
+    __shared__ int hist[256], base[256], run[256], wcnt[TPB / 32][256];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned nbig = d.glob->nbig;
+    for (unsigned b = blockIdx.x; b < nbig; b += gridDim.x) {
+        const int2 sg = d.bigseg[b];
+        const int s0 = sg.x, n = sg.y;
+        if (n <= SEG_SMEM) {  // bitonic network over the next power of two, padded with INT_MAX
+            int m = 1;
+            while (m < n) m <<= 1;
+            for (int k = tid; k < m; k += TPB) sv[k] = k < n ? d.perm[s0 + k] : 0x7FFFFFFF;
+            __syncthreads();
+            for (int size = 2; size <= m; size <<= 1)
+                for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                    for (int k = tid; k < m; k += TPB) {
+                        const int j = k ^ stride;
+                        if (j > k) {
+                            const bool up = (k & size) == 0;
+                            const int x = sv[k], y = sv[j];
+                            if ((x > y) == up) {
+                                sv[k] = y;
+                                sv[j] = x;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            for (int k = tid; k < n; k += TPB) d.perm[s0 + k] = sv[k];
+            __syncthreads();
+            continue;
+        }
+        // four stable 8-bit radix passes: perm -> slot -> perm -> slot -> perm
+        int *src = d.perm + s0, *dst = d.slot + s0;
+        for (int pass = 0; pass < 4; pass++) {
+            const int sh = 8 * pass;
+            for (int k = tid; k < 256; k += TPB) {
+                hist[k] = 0;
+                run[k] = 0;
+            }
+            __syncthreads();
+            for (int k = tid; k < n; k += TPB) atomicAdd(&hist[(src[k] >> sh) & 255], 1);
+            __syncthreads();
+            if (tid == 0) {
+                int acc = 0;
+                for (int k = 0; k < 256; k++) {
+                    base[k] = acc;
+                    acc += hist[k];
+                }
+            }
+            __syncthreads();
+            for (int c0 = 0; c0 < n; c0 += TPB) {
+                const int k = c0 + tid;
+                const bool ok = k < n;
+                const int v = ok ? src[k] : 0;
+                const int dg = ok ? (v >> sh) & 255 : 256 + lane;  // invalid lanes match nobody
+                for (int q = tid; q < (TPB / 32) * 256; q += TPB) (&wcnt[0][0])[q] = 0;
+                __syncthreads();
+                const unsigned peers = __match_any_sync(0xffffffffu, dg);
+                const int rank = __popc(peers & ((1u << lane) - 1u));
+                if (ok && rank == 0) wcnt[warp][dg] = __popc(peers);
+                __syncthreads();
+                if (ok) {
+                    int pos = base[dg] + run[dg] + rank;
+                    for (int w = 0; w < warp; w++) pos += wcnt[w][dg];
+                    dst[pos] = v;
+                }
+                __syncthreads();
+                for (int q = tid; q < 256; q += TPB) {
+                    int t = 0;
+                    for (int w = 0; w < TPB / 32; w++) t += wcnt[w][q];
+                    run[q] += t;
+                }
+                __syncthreads();
+            }
+            int *t = src;
+            src = dst;
+            dst = t;
+            __threadfence_block();
+            __syncthreads();
+        }
+    }
+    // the list is read by this launch only; the next step's k_segsort starts it again
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
     const int cur = d.glob->epoch & 1, nxt = cur ^ 1;
     // SU particles per thread per round, each stage's loads issued for all of them before the
-    // next stage uses them (the chain key -> box start and quadrant counts -> destination, and
-    // the state loads, would otherwise run one particle at a time)
+    // next stage uses them
     constexpr int SU = 4;
     const long long n = d.n_total, stride = (long long)gridDim.x * blockDim.x;
-    for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += SU * stride) {
-        int key4[SU], dst[SU];
+    for (long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; t0 < n; t0 += SU * stride) {
+        int src[SU], key4[SU];
 #pragma unroll
         for (int u = 0; u < SU; u++) {
-            const long long i = i0 + u * stride;
-            key4[u] = i < n ? d.key[i] : 0;
+            const long long t = t0 + u * stride;
+            src[u] = t < n ? d.perm[t] : 0;
         }
 #pragma unroll
         for (int u = 0; u < SU; u++) {
-            const long long i = i0 + u * stride;
-            dst[u] = 0;
-            if (i < n) {
-                const int key = key4[u] >> 2, quad = key4[u] & 3;
-                const int4 qc = reinterpret_cast<const int4 *>(d.qcounts)[key];
-                const int qpre = (quad > 0 ? qc.x : 0) + (quad > 1 ? qc.y : 0) + (quad > 2 ? qc.z : 0);
-                dst[u] = d.box_start[key] + qpre + d.slot[i];
-            }
+            const long long t = t0 + u * stride;
+            key4[u] = t < n ? d.key[src[u]] : 0;
         }
         double x[SU], y[SU], m[SU], vx[SU], vy[SU];
         int pid[SU];
 #pragma unroll
         for (int u = 0; u < SU; u++) {
-            const long long i = i0 + u * stride;
-            if (i < n) {
+            const long long t = t0 + u * stride;
+            if (t < n) {
+                const int i = src[u];
                 x[u] = d.X[cur][i];
                 y[u] = d.Y[cur][i];
                 m[u] = d.M[cur][i];
@@ -517,9 +647,9 @@ __global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
         }
 #pragma unroll
         for (int u = 0; u < SU; u++) {
-            const long long i = i0 + u * stride;
-            if (i >= n) continue;
-            const int key = key4[u] >> 2, t = dst[u];
+            const long long t = t0 + u * stride;
+            if (t >= n) continue;
+            const int key = key4[u] >> 2;
             const int s = find_seg(d.boff_tab, d.nsys, key);
             const SysDesc &sd = d.sys[s];
             const int lb = (int)(key - sd.boff);
@@ -534,9 +664,9 @@ __global__ void __launch_bounds__(TPB) k_scatter(DevPlan d) {
             const float ox = f64_to_f32_rn(__dsub_rn(x[u], org[kx]));
             const float oy = f64_to_f32_rn(__dsub_rn(y[u], org[sd.G + ky]));
             const float mf = f64_to_f32_rn(m[u]);
-            d.P[t] = make_float4(ox, oy, mf, __int_as_float(t));
-            d.PD[2 * (long long)t] = make_float4(ox, ox, oy, oy);
-            d.PD[2 * (long long)t + 1] = make_float4(mf, mf, __int_as_float(t), __int_as_float((kx << 16) | ky));
+            d.P[t] = make_float4(ox, oy, mf, __int_as_float((int)t));
+            d.PD[2 * t] = make_float4(ox, ox, oy, oy);
+            d.PD[2 * t + 1] = make_float4(mf, mf, __int_as_float((int)t), __int_as_float((kx << 16) | ky));
             d.skey[t] = key;
         }
     }
@@ -884,7 +1014,12 @@ cudaError_t launch_items(const DevPlan &d, cudaStream_t st) {
 }
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_scatter<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
+    cudaError_t e = cudaMemsetAsync(&d.glob->nbig, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    k_perm<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
+    k_segsort<<<grid_for(4 * d.B_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
+    k_segsort_big<<<(unsigned)(d.nsm * 2), TPB, 0, st>>>(d);
+    k_gather<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
 cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st) {

@@ -11,9 +11,11 @@ Tolerances:
     lists: relative RMS <= 1e-5 (FP32), 1e-8 (FP64 pairs: the cell centres of
     mass come from FP32 per-warp partial sums accumulated in FP64); pair
     counts exact;
-  * two runs of the same step (eager vs graph, fused vs unfused, batched vs
-    separate): within-box order follows atomic arrival (as in the reference
-    GPU path), so FP32 sums may differ in the last bits: accelerations and
+  * two runs of the same step (eager vs graph, fused vs unfused, a second plan on
+    the same input): bit-identical -- particles are ordered within a quadrant by
+    input order, not by atomic arrival, and every reduction runs in a fixed order;
+  * batched vs separate systems: the leaf sums start their 32-particle chunks at
+    other offsets, so FP32 sums may differ in the last bits: accelerations and
     velocities within relative RMS 1e-6, positions within 1e-9 absolute.
 """
 import numpy as np
@@ -44,9 +46,13 @@ def make_plan(n, G, **kw):
     return N.Plan([n] if np.isscalar(n) else n, [G] if np.isscalar(G) else G, prm)
 
 
-def assert_same_run(oa, ob, sl=slice(None)):
+def assert_same_run(oa, ob, sl=slice(None), exact=False):
     from oracle import oracle
 
+    if exact:
+        for k in ("x", "y", "vx", "vy", "ax", "ay"):
+            np.testing.assert_array_equal(oa[k][sl].cpu().numpy(), ob[k].cpu().numpy(), err_msg=k)
+        return
     for k in ("x", "y"):
         d = np.max(np.abs(oa[k][sl].cpu().numpy() - ob[k].cpu().numpy()))
         assert d <= 1e-9, (k, d)
@@ -157,7 +163,7 @@ def test_unfused_phases_equal_fused():
     b.create_tree()
     b.summarize()
     b.evaluate()
-    assert_same_run(a.store(), b.store())
+    assert_same_run(a.store(), b.store(), exact=True)
 
 
 # ---------------------------------------------------------------- theta mode
@@ -338,6 +344,64 @@ def test_batched_equals_separate():
         off += n
 
 
+@pytest.mark.parametrize("theta", [0.5, 0.0])
+def test_step_bit_reproducible_n1m(theta):
+    """Two plans on the same N = 1,048,576 cluster mixture (256 x 256 boxes), from the caller's
+    particle order, three steps each (graph replays): positions, velocities and accelerations
+    bit-identical.  theta 0.5: list streaming with quadrant items; theta 0: the reference's flat
+    far field (the walk).  Quadrants hold up to about seventy particles here, so both the
+    in-register and the shared-memory paths of the quadrant sort run."""
+    from barneshut.gb300 import workloads
+
+    x, y, m, vx, vy = workloads.cluster_mixture(1 << 20, seed=1)
+    if theta > 0:
+        kw = dict(grav_constant=1.0, tick_seconds=1e-5, softening=1e-4, cutoff_r2=0.0, theta=0.5,
+                  group_dim=4, dense_min=16, quad_min=128)
+    else:
+        kw = dict(REF_KW, tick_seconds=1e-5)
+    outs = []
+    for _ in range(2):
+        plan = make_plan(1 << 20, 256, **kw)
+        plan.load(x, y, m, vx, vy)
+        plan.step_graph(3)
+        outs.append(plan.store())
+        assert plan.error_flags() == 0
+        plan.close()
+    assert_same_run(outs[0], outs[1], exact=True)
+
+
+def test_long_quadrants_sorted():
+    """Ten thousand particles in one box (a 1 x 1 grid) and a few hundred in others: the quadrant
+    sort's CTA paths (bitonic up to 4,096 entries, radix beyond) give the same step as a second
+    plan, and the step matches the oracle's flat evaluation."""
+    from barneshut.gb300 import workloads
+    from oracle import oracle
+
+    rng = np.random.default_rng(77)
+    n = 40000
+    x = np.concatenate([rng.normal(0.3, 0.01, n // 2), rng.random(n // 2)])
+    y = np.concatenate([rng.normal(0.3, 0.01, n // 2), rng.random(n // 2)])
+    m = rng.uniform(1, 2, n)
+    z = np.zeros(n)
+    outs = []
+    for _ in range(2):
+        plan = make_plan(n, 8, **REF_KW)
+        plan.load(x, y, m, z, z)
+        plan.create_tree()
+        plan.summarize()
+        plan.evaluate()
+        outs.append(plan.store())
+        rec = plan.store_records().cpu().numpy()
+        kx, ky = oracle.keys(x, y, 8)
+        np.testing.assert_array_equal(rec[:, 7].astype(np.int32), kx)
+        np.testing.assert_array_equal(rec[:, 8].astype(np.int32), ky)
+        plan.close()
+    assert_same_run(outs[0], outs[1], exact=True)
+    ref = oracle.reference_evaluate(x, y, m, G=8, gconst=1.0)
+    assert oracle.rel_rms(outs[0]["ax"].cpu().numpy(), outs[0]["ay"].cpu().numpy(),
+                          ref["ax"], ref["ay"]) <= 1e-5
+
+
 def test_graph_replay_equals_eager():
     from barneshut.gb300 import workloads
 
@@ -350,7 +414,7 @@ def test_graph_replay_equals_eager():
     a.step(4)
     b.step_graph(2)
     b.step_graph(2)
-    assert_same_run(a.store(), b.store())
+    assert_same_run(a.store(), b.store(), exact=True)
 
 
 @pytest.mark.parametrize("case", ["stream", "stream_quad", "walk", "flat", "batched"])
