@@ -637,8 +637,9 @@ extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     // heaviest-first item order); work items: count, scan, fill for the walk or the learned
     // correction, one kernel for list streaming
     const bool walk_items = !p->stream || (p->params.flags & BH_FLAG_LEARNED);
+    // (a walking plan's tick is a kernel of its own: the walk reads the state the tick writes)
     *count = 1 + 1 + (walk_items ? 3 : 0) + 1 + (p->n_total > 0 ? 8 : 0) + (p->stream ? 1 : 0) +
-             (p->stream && p->n_total > 0 ? 3 : 0);
+             (p->stream && p->n_total > 0 ? 3 : 0) + (!p->stream && p->n_total > 0 ? 1 : 0);
     return BH_OK;
 }
 

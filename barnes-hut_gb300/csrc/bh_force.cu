@@ -669,6 +669,10 @@ cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStrea
         if (e != cudaSuccess) return e;
         return launch_fstream(d, tick, accumulate, st, ev);
     }
+    // The walk reads source positions from the FP64 state that the fused tick would update in
+    // place while other CTAs still read them, so here the tick runs as its own kernel.
+    const bool fused_tick = tick;
+    tick = false;
     cudaError_t e = cudaSuccess;
     if (ev && (e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
     const bool test = d.cutoff > 0.0 || d.eps2 == 0.0;
@@ -688,7 +692,8 @@ cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStrea
         else e = launch_force_t<float, FORCE_R, false, false, false>(d, tick, accumulate, st);
     }
     if (e != cudaSuccess) return e;
-    return ev ? cudaEventRecord(ev[1], st) : cudaSuccess;
+    if (ev && (e = cudaEventRecord(ev[1], st)) != cudaSuccess) return e;
+    return fused_tick ? launch_tick(d, st) : cudaSuccess;
 }
 
 }  // namespace bh

@@ -116,7 +116,8 @@ def test_launch_count_host_logic(lib):
         return c.value
 
     stream = count()
-    assert count(flags=native.BH_FLAG_WALK) == stream + 3 - 4  # walk items in, stream items and lists out
+    # walk items and the walk's own tick in, stream items and lists out
+    assert count(flags=native.BH_FLAG_WALK) == stream + 3 + 1 - 4
     assert count(flags=native.BH_FLAG_LEARNED) == stream + 3
 
 
