@@ -693,7 +693,7 @@ cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStrea
     }
     if (e != cudaSuccess) return e;
     if (ev && (e = cudaEventRecord(ev[1], st)) != cudaSuccess) return e;
-    return fused_tick ? launch_tick(d, st) : cudaSuccess;
+    return fused_tick ? launch_tick(d, st, true) : cudaSuccess;
 }
 
 }  // namespace bh

@@ -372,7 +372,7 @@ cudaError_t launch_fstream(const DevPlan &d, bool tick, bool accumulate, cudaStr
                            const cudaEvent_t *ev = nullptr);
 cudaError_t fstream_init();
 cudaError_t force_init();
-cudaError_t launch_tick(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_tick(const DevPlan &d, cudaStream_t st, bool keep_acc = false);
 cudaError_t launch_load(const DevPlan &d, const double *x, const double *y, const double *m,
                         const double *vx, const double *vy, long long rec_stride,
                         cudaStream_t st);

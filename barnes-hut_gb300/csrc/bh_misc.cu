@@ -27,8 +27,10 @@ __global__ void k_load(DevPlan d, const double *x, const double *y, const double
         d.VX[b][i] = vx[k];
         d.VY[b][i] = vy[k];
         d.PID[b][i] = (int)i;
-        d.AX[i] = 0.f;
-        d.AY[i] = 0.f;
+        if (!keep_acc) {
+            d.AX[i] = 0.f;
+            d.AY[i] = 0.f;
+        }
     }
 }
 
@@ -66,7 +68,9 @@ __global__ void k_store(DevPlan d, double *rec, double *x, double *y, double *vx
 }
 
 // v += a dt; a = 0; x += v dt  (gpu/grid.py:159-174)
-__global__ void k_tick(DevPlan d) {
+// keep_acc: leave the accelerations in place (the fused step's tick, which keeps the last
+// evaluation's accelerations; the reference's tick, gpu/grid.py:159-174, zeroes them)
+__global__ void k_tick(DevPlan d, int keep_acc) {
     const int b = (d.glob->epoch + 1) & 1;
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < d.n_total; i += stride) {
@@ -201,9 +205,9 @@ cudaError_t launch_store(const DevPlan &d, int has_tree, double *rec, double *x,
     return cudaGetLastError();
 }
 
-cudaError_t launch_tick(const DevPlan &d, cudaStream_t st) {
+cudaError_t launch_tick(const DevPlan &d, cudaStream_t st, bool keep_acc) {
     if (d.n_total == 0) return cudaSuccess;
-    k_tick<<<grid_of(d.n_total, MT, d.nsm), MT, 0, st>>>(d);
+    k_tick<<<grid_of(d.n_total, MT, d.nsm), MT, 0, st>>>(d, keep_acc ? 1 : 0);
     return cudaGetLastError();
 }
 
