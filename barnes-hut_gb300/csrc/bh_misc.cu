@@ -27,10 +27,8 @@ __global__ void k_load(DevPlan d, const double *x, const double *y, const double
         d.VX[b][i] = vx[k];
         d.VY[b][i] = vy[k];
         d.PID[b][i] = (int)i;
-        if (!keep_acc) {
-            d.AX[i] = 0.f;
-            d.AY[i] = 0.f;
-        }
+        d.AX[i] = 0.f;
+        d.AY[i] = 0.f;
     }
 }
 
@@ -78,8 +76,10 @@ __global__ void k_tick(DevPlan d, int keep_acc) {
         double vx = d.VX[b][i] + ax * d.dt, vy = d.VY[b][i] + ay * d.dt;
         d.VX[b][i] = vx;
         d.VY[b][i] = vy;
-        d.AX[i] = 0.f;
-        d.AY[i] = 0.f;
+        if (!keep_acc) {
+            d.AX[i] = 0.f;
+            d.AY[i] = 0.f;
+        }
         d.X[b][i] = d.X[b][i] + vx * d.dt;
         d.Y[b][i] = d.Y[b][i] + vy * d.dt;
     }
