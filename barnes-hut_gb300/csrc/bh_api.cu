@@ -356,6 +356,7 @@ static void fill_dev(bh_plan *p) {
     d.skey = (int *)(w + p->o_skey);
     d.perm = (int *)(w + p->o_perm);
     d.bigseg = (int2 *)(w + p->o_bigseg);
+    d.bigseg_cap = p->n_total / 17 + 1;
     d.counts = (int *)(w + p->o_counts);
     d.qcounts = (int *)(w + p->o_qcnt);
     d.box_start = (int *)(w + p->o_bstart);

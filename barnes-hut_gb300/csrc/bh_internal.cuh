@@ -86,6 +86,7 @@ struct Globals {
     unsigned int scan_gen[3];       // generation of each scan's tile states (its last tile bumps it)
     unsigned int bbox_done;         // bounding-box blocks finished (the last one finalises)
     unsigned int nbig;              // entries of the long-quadrant list (k_segsort)
+    unsigned int nhuge;             // entries of the very-long-quadrant list, from its far end
 };
 
 struct DevPlan {
@@ -112,6 +113,7 @@ struct DevPlan {
     int *key, *slot, *skey;
     int *perm;     // box-sorted position -> input index (k_perm, k_segsort)
     int2 *bigseg;  // quadrant stretches too long for a thread's registers: (first, count)
+    long long bigseg_cap;
     int *counts, *box_start;
     // single-pass scans (decoupled look-back): per-tile states of the box scan, the walk items'
     // scan and the streaming items' scan (generation << 34 | flag << 32 | value)

@@ -476,14 +476,14 @@ __global__ void __launch_bounds__(SITEM_TILE) k_sitems(DevPlan d) {
 // on the order in which k_place's atomics handed out slots:
 //   k_perm     perm[box_start + earlier quadrants + slot] = input index (slots: k_place);
 //   k_segsort  each quadrant's stretch of perm sorted ascending -- up to SEG_REG entries in a
-//              thread's registers, longer ones listed for k_segsort_big (a CTA each: a bitonic
-//              network in shared memory up to SEG_SMEM entries, beyond that four stable 8-bit
-//              radix passes through the dead slot array);
+//              thread's registers, longer ones listed for k_segsort_big (up to SEG_WARP entries
+//              a warp each, a bitonic network in its slice of shared memory; longer ones a CTA
+//              each, four stable 8-bit radix passes through the dead slot array);
 //   k_gather   output particle t takes input perm[t]: the FP64 state of the next buffer, the
 //              packed float4 record (offsets from the box origin computed in FP64, rounded once
 //              to float), the 32-byte near-source record and the sorted key.
 constexpr int SEG_REG = 16;
-constexpr int SEG_SMEM = 4096;
+constexpr int SEG_WARP = 1024;
 
 __device__ __forceinline__ int quad_first(const DevPlan &d, int key4) {
     const int box = key4 >> 2, quad = key4 & 3;
@@ -503,6 +503,11 @@ __global__ void __launch_bounds__(TPB) k_segsort(DevPlan d) {
         const int n = d.qcounts[q];
         if (n < 2) continue;
         const int s0 = quad_first(d, (int)q);
+        if (n > SEG_WARP) {  // listed from the far end of the same array
+            const unsigned k = atomicAdd(&d.glob->nhuge, 1u);
+            d.bigseg[d.bigseg_cap - 1 - k] = make_int2(s0, n);
+            continue;
+        }
         if (n > SEG_REG) {
             const unsigned k = atomicAdd(&d.glob->nbig, 1u);
             d.bigseg[k] = make_int2(s0, n);
@@ -527,38 +532,44 @@ __global__ void __launch_bounds__(TPB) k_segsort(DevPlan d) {
 }
 
 __global__ void __launch_bounds__(TPB) k_segsort_big(DevPlan d) {
-    __shared__ int sv[SEG_SMEM];
+    __shared__ int sv[TPB / 32][SEG_WARP];
     __shared__ int hist[256], base[256], run[256], wcnt[TPB / 32][256];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // stretches of SEG_REG + 1 .. SEG_WARP entries: a warp each, a bitonic network over the next
+    // power of two (padded with INT_MAX) in the warp's slice of shared memory
     const unsigned nbig = d.glob->nbig;
-    for (unsigned b = blockIdx.x; b < nbig; b += gridDim.x) {
-        const int2 sg = d.bigseg[b];
+    int *w = sv[warp];
+    for (unsigned e = (unsigned)(blockIdx.x * (TPB / 32) + warp); e < nbig; e += gridDim.x * (TPB / 32)) {
+        const int2 sg = d.bigseg[e];
         const int s0 = sg.x, n = sg.y;
-        if (n <= SEG_SMEM) {  // bitonic network over the next power of two, padded with INT_MAX
-            int m = 1;
-            while (m < n) m <<= 1;
-            for (int k = tid; k < m; k += TPB) sv[k] = k < n ? d.perm[s0 + k] : 0x7FFFFFFF;
-            __syncthreads();
-            for (int size = 2; size <= m; size <<= 1)
-                for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                    for (int k = tid; k < m; k += TPB) {
-                        const int j = k ^ stride;
-                        if (j > k) {
-                            const bool up = (k & size) == 0;
-                            const int x = sv[k], y = sv[j];
-                            if ((x > y) == up) {
-                                sv[k] = y;
-                                sv[j] = x;
-                            }
+        int m = 32;
+        while (m < n) m <<= 1;
+        for (int k = lane; k < m; k += 32) w[k] = k < n ? d.perm[s0 + k] : 0x7FFFFFFF;
+        __syncwarp();
+        for (int size = 2; size <= m; size <<= 1)
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int k = lane; k < m; k += 32) {
+                    const int j = k ^ stride;
+                    if (j > k) {
+                        const bool up = (k & size) == 0;
+                        const int x = w[k], y = w[j];
+                        if ((x > y) == up) {
+                            w[k] = y;
+                            w[j] = x;
                         }
                     }
-                    __syncthreads();
                 }
-            for (int k = tid; k < n; k += TPB) d.perm[s0 + k] = sv[k];
-            __syncthreads();
-            continue;
-        }
-        // four stable 8-bit radix passes: perm -> slot -> perm -> slot -> perm
+                __syncwarp();
+            }
+        for (int k = lane; k < n; k += 32) d.perm[s0 + k] = w[k];
+        __syncwarp();
+    }
+    // longer stretches: a CTA each, four stable 8-bit radix passes perm -> slot -> perm -> slot
+    // -> perm (the slot array is dead once k_perm has run)
+    const unsigned nhuge = d.glob->nhuge;
+    for (unsigned b = blockIdx.x; b < nhuge; b += gridDim.x) {
+        const int2 sg = d.bigseg[d.bigseg_cap - 1 - b];
+        const int s0 = sg.x, n = sg.y;
         int *src = d.perm + s0, *dst = d.slot + s0;
         for (int pass = 0; pass < 4; pass++) {
             const int sh = 8 * pass;
@@ -590,13 +601,13 @@ __global__ void __launch_bounds__(TPB) k_segsort_big(DevPlan d) {
                 __syncthreads();
                 if (ok) {
                     int pos = base[dg] + run[dg] + rank;
-                    for (int w = 0; w < warp; w++) pos += wcnt[w][dg];
+                    for (int q = 0; q < warp; q++) pos += wcnt[q][dg];
                     dst[pos] = v;
                 }
                 __syncthreads();
                 for (int q = tid; q < 256; q += TPB) {
                     int t = 0;
-                    for (int w = 0; w < TPB / 32; w++) t += wcnt[w][q];
+                    for (int ww = 0; ww < TPB / 32; ww++) t += wcnt[ww][q];
                     run[q] += t;
                 }
                 __syncthreads();
@@ -608,8 +619,6 @@ __global__ void __launch_bounds__(TPB) k_segsort_big(DevPlan d) {
             __syncthreads();
         }
     }
-    // the list is read by this launch only; the next step's k_segsort starts it again
-    __syncthreads();
 }
 
 __global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
@@ -1014,7 +1023,7 @@ cudaError_t launch_items(const DevPlan &d, cudaStream_t st) {
 }
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(&d.glob->nbig, 0, sizeof(unsigned), st);
+    cudaError_t e = cudaMemsetAsync(&d.glob->nbig, 0, 2 * sizeof(unsigned), st);  // nbig, nhuge
     if (e != cudaSuccess) return e;
     k_perm<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     k_segsort<<<grid_for(4 * d.B_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
