@@ -516,6 +516,10 @@ __global__ void __launch_bounds__(TPB) k_segsort(DevPlan d) {
         int v[SEG_REG];
 #pragma unroll
         for (int k = 0; k < SEG_REG; k++) v[k] = k < n ? d.perm[s0 + k] : 0x7FFFFFFF;
+        bool sorted = true;  // (padding sorts after every index)
+#pragma unroll
+        for (int k = 0; k + 1 < SEG_REG; k++) sorted &= v[k] <= v[k + 1];
+        if (sorted) continue;
         // odd-even transposition network: SEG_REG rounds sort SEG_REG entries
 #pragma unroll
         for (int r = 0; r < SEG_REG; r++)
@@ -544,8 +548,19 @@ __global__ void __launch_bounds__(TPB) k_segsort_big(DevPlan d) {
         const int s0 = sg.x, n = sg.y;
         int m = 32;
         while (m < n) m <<= 1;
-        for (int k = lane; k < m; k += 32) w[k] = k < n ? d.perm[s0 + k] : 0x7FFFFFFF;
+        // a stretch whose slots the atomics happened to hand out in input order is done already
+        // (the common case when the input is the previous step's order)
+        bool sorted = true;
+        for (int k = lane; k < m; k += 32) {
+            const int v = k < n ? d.perm[s0 + k] : 0x7FFFFFFF;
+            w[k] = v;
+        }
         __syncwarp();
+        for (int k = lane; k + 1 < n; k += 32) sorted &= w[k] < w[k + 1];
+        if (__all_sync(0xffffffffu, sorted)) {
+            __syncwarp();
+            continue;
+        }
         for (int size = 2; size <= m; size <<= 1)
             for (int stride = size >> 1; stride > 0; stride >>= 1) {
                 for (int k = lane; k < m; k += 32) {
@@ -1027,7 +1042,7 @@ cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     k_perm<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     k_segsort<<<grid_for(4 * d.B_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
-    k_segsort_big<<<(unsigned)(d.nsm * 2), TPB, 0, st>>>(d);
+    k_segsort_big<<<(unsigned)(d.nsm * 4), TPB, 0, st>>>(d);
     k_gather<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
