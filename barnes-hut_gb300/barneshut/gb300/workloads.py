@@ -81,9 +81,9 @@ def gen_input(n, distribution="normal", seed=None, domain=500.0):
 
 
 def box_order(x, y, G):
-    """Permutation that sorts particles by box key (gx * G + gy) of the square
-    bounding-box grid, stable within a box (the order of the state between
-    steps of a running simulation)."""
+    """Permutation into the order of the state between steps of a running simulation: by box
+    key (gx * G + gy) of the square bounding-box grid, within a box quadrant by quadrant (x
+    half * 2 + y half, from the key at twice the box resolution), stable within a quadrant."""
     mnx, mny, mxx, mxy = float(x.min()), float(y.min()), float(x.max()), float(y.max())
     xe, ye = mxx - mnx, mxy - mny
     if xe > ye:
@@ -95,7 +95,9 @@ def box_order(x, y, G):
         return np.arange(len(x))
     kx = np.clip(np.floor((x - mnx) / step), 0, G - 1).astype(np.int64)
     ky = np.clip(np.floor((y - mny) / step), 0, G - 1).astype(np.int64)
-    return np.argsort(kx * G + ky, kind="stable")
+    hx = np.clip(np.floor(((x - mnx) / step) * 2.0), 0, 2 * G - 1).astype(np.int64) & 1
+    hy = np.clip(np.floor(((y - mny) / step) * 2.0), 0, 2 * G - 1).astype(np.int64) & 1
+    return np.argsort(4 * (kx * G + ky) + 2 * hx + hy, kind="stable")
 
 
 def precision_subsample(n, k=16384, seed=2):

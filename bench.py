@@ -14,7 +14,8 @@ CUDA-graph replay).  The reload is inside the timed region.  It keeps every
 timed step on the same distribution: with G = 1 and these masses the clusters
 collapse within a few steps of dt = 1e-5, and a free-running simulation would
 time a different (much denser) state at every step count.  The batch is
-stored in box order, as the state is between steps of a running simulation.
+stored in the order the state has between steps of a running simulation (by
+box, within a box by quadrant).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 N > 1 runs under torchrun: every rank steps its own replica (weak scaling);
@@ -662,7 +663,7 @@ def main():
     from barneshut.gb300 import native, workloads
 
     x, y, m, vx, vy = workloads.cluster_mixture(args.n, seed=replica_seed(rank))
-    # batch in box order (the state's order between steps of a running simulation)
+    # batch in the state's order between steps of a running simulation (box, then quadrant)
     order = workloads.box_order(x, y, args.grid)
     x, y, m, vx, vy = (a[order].copy() for a in (x, y, m, vx, vy))
     tile = {"group_dim": 0, "tune": 0, "dense_min": 0}
