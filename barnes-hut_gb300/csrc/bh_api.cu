@@ -32,7 +32,7 @@ struct bh_plan {
     size_t ws_bytes = 0;
     size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_toff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
-    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_counts, o_bstart, o_sst, o_leafpart, o_perm, o_bigseg, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
+    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_bstart, o_sst, o_leafpart, o_perm, o_bigseg, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
         o_rec2, o_org, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk, o_qcnt;
     bool stream = false;  // theta-mode interaction lists built once per group and streamed
     int chunk = TARGET_CHUNK;
@@ -266,7 +266,6 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_skey = take(4 * N);
     p->o_perm = take(4 * N);
     p->o_bigseg = take(8 * (N / 17 + 1));  // quadrants of more than 16 particles: at most N / 17
-    p->o_counts = take(4 * B);
     p->o_qcnt = take(16 * B);
     p->o_bstart = take(4 * (B + 1));
     p->sst_bytes = 8 * (B / SCAN_TILE + 2 + (size_t)p->NG_total / SCAN_TILE + 2 + (size_t)p->NG_total / SITEM_TILE + 2);
@@ -357,7 +356,6 @@ static void fill_dev(bh_plan *p) {
     d.perm = (int *)(w + p->o_perm);
     d.bigseg = (int2 *)(w + p->o_bigseg);
     d.bigseg_cap = p->n_total / 17 + 1;
-    d.counts = (int *)(w + p->o_counts);
     d.qcounts = (int *)(w + p->o_qcnt);
     d.box_start = (int *)(w + p->o_bstart);
     d.sst_box = (unsigned long long *)(w + p->o_sst);

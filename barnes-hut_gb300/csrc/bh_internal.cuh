@@ -114,7 +114,7 @@ struct DevPlan {
     int *perm;     // box-sorted position -> input index (k_perm, k_segsort)
     int2 *bigseg;  // quadrant stretches too long for a thread's registers: (first, count)
     long long bigseg_cap;
-    int *counts, *box_start;
+    int *box_start;
     // single-pass scans (decoupled look-back): per-tile states of the box scan, the walk items'
     // scan and the streaming items' scan (generation << 34 | flag << 32 | value)
     unsigned long long *sst_box, *sst_witem, *sst_sitem;

@@ -37,7 +37,6 @@ __global__ void k_prologue(DevPlan d) {
         d.dyn[tid].bbmax[0] = d.dyn[tid].bbmax[1] = 0ull;
     }
     for (long long b = tid; b < d.B_total; b += stride) {
-        d.counts[b] = 0;
         reinterpret_cast<int4 *>(d.qcounts)[b] = make_int4(0, 0, 0, 0);
     }
 }
@@ -163,7 +162,8 @@ __global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
 // -------------------------------------------------------------------- place
 // Box keys bit-exact with the reference's FP64 keys (computed at twice the box resolution, so
 // each particle also gets its quadrant within the box), and a warp-aggregated histogram of
-// boxes and of (box, quadrant) pairs; a particle's slot is its rank within its quadrant.
+// (box, quadrant) pairs (a box's count is the sum of its four); a particle's slot is its rank
+// within its quadrant.
 __global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
     const int cur = d.glob->epoch & 1;
     const double *X = d.X[cur], *Y = d.Y[cur];
@@ -195,10 +195,7 @@ __global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
         int leader = __ffs(peers) - 1;
         int rank = __popc(peers & ((1u << lane) - 1u));
         int old = 0;
-        if (lane == leader && key >= 0) {
-            atomicAdd(&d.counts[key >> 2], __popc(peers));
-            old = atomicAdd(&d.qcounts[key], __popc(peers));
-        }
+        if (lane == leader && key >= 0) old = atomicAdd(&d.qcounts[key], __popc(peers));
         old = __shfl_sync(0xffffffffu, old, leader);
         if (i < d.n_total) {
             d.key[i] = key;  // 4 * box + quadrant
@@ -297,7 +294,9 @@ __device__ int lookback(unsigned long long *state, int tile, unsigned gen, int a
     return excl;
 }
 
-// out[i] = sum(in[0..i)) for i < n, out[n] = sum(in[0..n)); scan k of the plan's three.
+// out[i] = sum(in[0..i)) for i < n, out[n] = sum(in[0..n)); scan k of the plan's three.  QSUM:
+// element i is the sum of the four quadrant counts in[4 i .. 4 i + 3] (a box's particles).
+template <bool QSUM>
 __global__ void __launch_bounds__(TPB) k_scan_lookback(const int *in, long long n, int *out,
                                                       unsigned long long *state, Globals *glob, int k) {
     __shared__ int sh[32];
@@ -314,7 +313,15 @@ __global__ void __launch_bounds__(TPB) k_scan_lookback(const int *in, long long 
     int v[16], sum = 0;
 #pragma unroll
     for (int q = 0; q < 16; q++) {
-        v[q] = b0 + q < n ? in[b0 + q] : 0;
+        v[q] = 0;
+        if (b0 + q < n) {
+            if (QSUM) {
+                const int4 c = reinterpret_cast<const int4 *>(in)[b0 + q];
+                v[q] = c.x + c.y + c.z + c.w;
+            } else {
+                v[q] = in[b0 + q];
+            }
+        }
         sum += v[q];
     }
     int tot;
@@ -338,10 +345,13 @@ __global__ void __launch_bounds__(TPB) k_scan_lookback(const int *in, long long 
 }
 
 static cudaError_t scan_excl(const int *in, int *out, long long n, unsigned long long *state,
-                             Globals *glob, int k, cudaStream_t st) {
+                             Globals *glob, int k, cudaStream_t st, bool qsum = false) {
     long long ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (ntiles < 1) ntiles = 1;
-    k_scan_lookback<<<(unsigned)ntiles, TPB, 0, st>>>(in, n, out, state, glob, k);
+    if (qsum)
+        k_scan_lookback<true><<<(unsigned)ntiles, TPB, 0, st>>>(in, n, out, state, glob, k);
+    else
+        k_scan_lookback<false><<<(unsigned)ntiles, TPB, 0, st>>>(in, n, out, state, glob, k);
     return cudaGetLastError();
 }
 
@@ -1011,7 +1021,7 @@ cudaError_t launch_place(const DevPlan &d, cudaStream_t st) {
     return cudaGetLastError();
 }
 cudaError_t launch_scan(const DevPlan &d, cudaStream_t st) {
-    return scan_excl(d.counts, d.box_start, d.B_total, d.sst_box, d.glob, 0, st);
+    return scan_excl(d.qcounts, d.box_start, d.B_total, d.sst_box, d.glob, 0, st, true);
 }
 // Work items of the walk kernel and of the learned correction (group, target chunk).
 cudaError_t launch_walk_items(const DevPlan &d, cudaStream_t st) {
