@@ -161,13 +161,14 @@ __global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
 
 // -------------------------------------------------------------------- place
 // Box keys bit-exact with the reference's FP64 keys (computed at twice the box resolution, so
-// each particle also gets its quadrant within the box), and a warp-aggregated histogram of
-// (box, quadrant) pairs (a box's count is the sum of its four); a particle's slot is its rank
-// within its quadrant.
+// each particle also gets its quadrant within the box), and a histogram of (box, quadrant)
+// pairs aggregated over runs of equal keys in the block (a box's count is the sum of its
+// four); a particle's slot is its rank within its quadrant.
 __global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
+    __shared__ int skeys[TPB], runold[TPB], wmax[TPB / 32];
     const int cur = d.glob->epoch & 1;
     const double *X = d.X[cur], *Y = d.Y[cur];
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     long long stride = (long long)gridDim.x * blockDim.x;
     long long base = (long long)blockIdx.x * blockDim.x;
     for (; base < d.n_total; base += stride) {
@@ -188,19 +189,29 @@ __global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
             const int box = (int)(sd.boff + (long long)(k2x >> 1) * sd.G + (k2y >> 1));
             key = 4 * box + (k2x & 1) * 2 + (k2y & 1);
         }
-        // lanes with the same (box, quadrant) elect one leader that adds the group's size to the
-        // box count (the scan's input) and to the quadrant count, whose old value is the group's
-        // first slot in the quadrant
-        unsigned peers = __match_any_sync(0xffffffffu, key);
-        int leader = __ffs(peers) - 1;
-        int rank = __popc(peers & ((1u << lane) - 1u));
-        int old = 0;
-        if (lane == leader && key >= 0) old = atomicAdd(&d.qcounts[key], __popc(peers));
-        old = __shfl_sync(0xffffffffu, old, leader);
+        // runs of consecutive particles of the block with the same (box, quadrant): the run's
+        // last particle adds the run's length to the quadrant count, whose old value is the run's
+        // first slot, so a quadrant whose particles lie in one block gets its slots in input
+        // order (the common case when the input is the previous step's order); k_segsort puts
+        // the runs of different blocks in order
+        skeys[threadIdx.x] = key;
+        __syncthreads();
+        const int kprev = threadIdx.x > 0 ? skeys[threadIdx.x - 1] : INT_MIN;
+        const int knext = threadIdx.x + 1 < TPB ? skeys[threadIdx.x + 1] : INT_MIN;
+        int h = key != kprev ? (int)threadIdx.x : 0;  // this run's first thread: a max-scan
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) h = max(h, __shfl_up_sync(0xffffffffu, h, o) * (lane >= o));
+        if (lane == 31) wmax[warp] = h;
+        __syncthreads();
+        for (int w = 0; w < warp; w++) h = max(h, wmax[w]);
+        const int rank = (int)threadIdx.x - h;
+        if (key >= 0 && key != knext) runold[h] = atomicAdd(&d.qcounts[key], rank + 1);
+        __syncthreads();
         if (i < d.n_total) {
             d.key[i] = key;  // 4 * box + quadrant
-            d.slot[i] = old + rank;
+            d.slot[i] = runold[h] + rank;
         }
+        __syncthreads();  // the block's shared arrays are reused in the next round
     }
 }
 
