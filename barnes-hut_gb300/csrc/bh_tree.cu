@@ -92,6 +92,7 @@ __global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
         bool one_sys = d.poff_tab[s_first + 1] >= t1;
         unsigned long long mn0 = ~0ull, mn1 = ~0ull, mx0 = 0, mx1 = 0;
         int cs = s_first;
+#pragma unroll 4
         for (long long i = t0 + threadIdx.x; i < t1; i += TPB) {
             if (!one_sys) {
                 int s = find_seg(d.poff_tab, d.nsys, i);
@@ -505,6 +506,7 @@ __global__ void __launch_bounds__(SITEM_TILE) k_sitems(DevPlan d) {
 //              to float), the 32-byte near-source record and the sorted key.
 constexpr int SEG_REG = 16;
 constexpr int SEG_WARP = 1024;
+constexpr int SEG_CHECK = 128;  // stretches up to this long are checked for order by their thread
 
 __device__ __forceinline__ int quad_first(const DevPlan &d, int key4) {
     const int box = key4 >> 2, quad = key4 & 3;
@@ -524,6 +526,21 @@ __global__ void __launch_bounds__(TPB) k_segsort(DevPlan d) {
         const int n = d.qcounts[q];
         if (n < 2) continue;
         const int s0 = quad_first(d, (int)q);
+        if (n > SEG_REG && n <= SEG_CHECK) {  // listed only when out of order
+            bool sorted = true;
+            int prev = d.perm[s0];
+            for (int k0 = 1; k0 < n && sorted; k0 += 8) {
+                int v[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) v[k] = k0 + k < n ? d.perm[s0 + k0 + k] : 0x7FFFFFFF;
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    sorted &= prev < v[k] || k0 + k >= n;
+                    prev = v[k];
+                }
+            }
+            if (sorted) continue;
+        }
         if (n > SEG_WARP) {  // listed from the far end of the same array
             const unsigned k = atomicAdd(&d.glob->nhuge, 1u);
             d.bigseg[d.bigseg_cap - 1 - k] = make_int2(s0, n);
@@ -787,14 +804,28 @@ __device__ __forceinline__ void cell_record(const DevPlan &d, long long c, int l
 __global__ void __launch_bounds__(TPB) k_leaf(DevPlan d) {
     const int lane = threadIdx.x & 31;
     const long long nch = (d.n_total + 31) >> 5;
-    for (long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nch;
-         c += ((long long)gridDim.x * blockDim.x) >> 5) {
+    const long long cstride = ((long long)gridDim.x * blockDim.x) >> 5;
+    long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    // the next chunk's key and record are loaded while this one is summed
+    int nkey = -1;
+    float4 np = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (c < nch && (c << 5) + lane < d.n_total) {
+        nkey = d.skey[(c << 5) + lane];
+        np = d.P[(c << 5) + lane];
+    }
+    for (; c < nch; c += cstride) {
         const long long i = (c << 5) + lane;
+        const int ckey = nkey;
+        const float4 p = np;
+        const long long inx = ((c + cstride) << 5) + lane;
+        if (c + cstride < nch && inx < d.n_total) {
+            nkey = d.skey[inx];
+            np = d.P[inx];
+        }
         int key = -1;
         float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (i < d.n_total) {
-            key = d.skey[i];
-            const float4 p = d.P[i];
+            key = ckey;
             v[0] = p.z;
             v[1] = p.z * p.x;
             v[2] = p.z * p.y;
