@@ -44,6 +44,7 @@ struct bh_plan {
     DevPlan dev;
     bool has_tree = false;
     bool acc_stale = true;  // next bh_evaluate overwrites instead of accumulating
+    bool leaves_stale = false;  // leaf moments overwritten since the last create_tree
     // graph cache
     cudaGraphExec_t gexec = nullptr;
     size_t sst_bytes = 0;  // the single-pass scans' tile states
@@ -488,7 +489,8 @@ static int enqueue_tree(bh_plan *p, cudaStream_t st) {
     CK(p, launch_bbox(p->dev, st), "bbox");
     CK(p, launch_place(p->dev, st), "place");
     CK(p, launch_scan(p->dev, st), "scan");
-    CK(p, launch_scatter(p->dev, st), "scatter");
+    CK(p, launch_scatter(p->dev, st), "scatter");  // (and the leaf sums)
+    p->leaves_stale = false;
     CK(p, launch_items(p->dev, st), "work items");
     return BH_OK;
 }
@@ -507,7 +509,8 @@ extern "C" int bh_summarize(bh_plan *p, void *stream) {
     int r = need_bound(p);
     if (r) return r;
     if (!p->has_tree) return fail(p, BH_ERR_INVALID, "summarize before create_tree");
-    CK(p, launch_summarize(p->dev, (cudaStream_t)stream), "summarize");
+    CK(p, launch_summarize(p->dev, p->leaves_stale, (cudaStream_t)stream), "summarize");
+    p->leaves_stale = false;
     return BH_OK;
 }
 
@@ -538,7 +541,7 @@ static int enqueue_steps(bh_plan *p, int nsteps, cudaStream_t st) {
     for (int k = 0; k < nsteps; k++) {
         int r = enqueue_tree(p, st);
         if (r) return r;
-        CK(p, launch_summarize(p->dev, st), "summarize");
+        CK(p, launch_summarize(p->dev, false, st), "summarize");
         if (p->dev.learned) {
             if (!p->mlp_img) return fail(p, BH_ERR_INVALID, "BH_FLAG_LEARNED without bh_set_correction");
             CK(p, launch_force(p->dev, false, false, st), "force");
@@ -631,13 +634,13 @@ extern "C" int bh_force_kernel_ms(bh_plan *p, float *ms) {
 extern "C" int bh_kernels_per_step(const bh_plan *p, int *count) {
     if (!p || !count) return BH_ERR_INVALID;
     // prologue, box scan, summarize tiles; with particles also bbox (which finalises the box),
-    // place, the scatter's four kernels (permutation, quadrant sort, long quadrants, gather), leaf
-    // sums, force (and before it, when streaming, the list build and the two kernels of the
-    // heaviest-first item order); work items: count, scan, fill for the walk or the learned
+    // place, the scatter's four kernels (permutation, quadrant sort, long quadrants, gather with
+    // the leaf sums), force (and before it, when streaming, the list build and the two kernels of
+    // the heaviest-first item order); work items: count, scan, fill for the walk or the learned
     // correction, one kernel for list streaming
     const bool walk_items = !p->stream || (p->params.flags & BH_FLAG_LEARNED);
     // (a walking plan's tick is a kernel of its own: the walk reads the state the tick writes)
-    *count = 1 + 1 + (walk_items ? 3 : 0) + 1 + (p->n_total > 0 ? 8 : 0) + (p->stream ? 1 : 0) +
+    *count = 1 + 1 + (walk_items ? 3 : 0) + 1 + (p->n_total > 0 ? 7 : 0) + (p->stream ? 1 : 0) +
              (p->stream && p->n_total > 0 ? 3 : 0) + (!p->stream && p->n_total > 0 ? 1 : 0);
     return BH_OK;
 }
@@ -736,6 +739,7 @@ extern "C" int bh_set_leaf_moments(bh_plan *p, int sys, const double *in, void *
     cudaStream_t st = (cudaStream_t)stream;
     CK(p, cudaMemcpyAsync((char *)p->ws + p->o_mom + 48 * d.coff, in, 48 * (size_t)d.G * d.G,
                           cudaMemcpyDeviceToDevice, st), "copy leaf moments");
+    p->leaves_stale = true;  // a later bh_summarize sums the leaves from the particles again
     CK(p, launch_pyramid(p->dev, st), "pyramid");
     return BH_OK;
 }

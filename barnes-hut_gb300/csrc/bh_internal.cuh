@@ -363,7 +363,7 @@ cudaError_t launch_items(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_walk_items(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_records(const DevPlan &d, bool second, cudaStream_t st);
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st);
-cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st);
+cudaError_t launch_summarize(const DevPlan &d, bool leaves, cudaStream_t st);
 // the pyramid levels above the leaves and the cell records, from the leaf moments
 cudaError_t launch_pyramid(const DevPlan &d, cudaStream_t st);
 // ev (optional): two events recorded on st right before and after the force kernel proper

@@ -78,13 +78,78 @@ __device__ void bbox_finalize_sys(const DevPlan &d, int s) {
 // --------------------------------------------------------------------- bbox
 // Min / max of x and y per system on the ordered-integer image of the doubles
 // (integer min/max, no FP64 pipe work).  Each block reduces a contiguous tile.
+__device__ __forceinline__ void minmax_ord(unsigned long long u, unsigned long long &mn, unsigned long long &mx) {
+    mn = u < mn ? u : mn;
+    mx = u > mx ? u : mx;
+}
+
+__device__ __forceinline__ void bbox_block_commit(const DevPlan &d, int s, unsigned long long mn0,
+                                                  unsigned long long mn1, unsigned long long mx0,
+                                                  unsigned long long mx1, unsigned long long (*red)[TPB / 32]) {
+    for (int o = 16; o; o >>= 1) {
+        unsigned long long a = __shfl_xor_sync(0xffffffffu, mn0, o); mn0 = a < mn0 ? a : mn0;
+        a = __shfl_xor_sync(0xffffffffu, mn1, o); mn1 = a < mn1 ? a : mn1;
+        a = __shfl_xor_sync(0xffffffffu, mx0, o); mx0 = a > mx0 ? a : mx0;
+        a = __shfl_xor_sync(0xffffffffu, mx1, o); mx1 = a > mx1 ? a : mx1;
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { red[0][w] = mn0; red[1][w] = mn1; red[2][w] = mx0; red[3][w] = mx1; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < TPB / 32; k++) {
+            mn0 = red[0][k] < mn0 ? red[0][k] : mn0; mn1 = red[1][k] < mn1 ? red[1][k] : mn1;
+            mx0 = red[2][k] > mx0 ? red[2][k] : mx0; mx1 = red[3][k] > mx1 ? red[3][k] : mx1;
+        }
+        if (mx0 | mx1) {
+            atomicMin(&d.dyn[s].bbmin[0], mn0); atomicMin(&d.dyn[s].bbmin[1], mn1);
+            atomicMax(&d.dyn[s].bbmax[0], mx0); atomicMax(&d.dyn[s].bbmax[1], mx1);
+        }
+    }
+    __syncthreads();
+}
+
 __global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
     const int cur = d.glob->epoch & 1;
     const double *X = d.X[cur], *Y = d.Y[cur];
     __shared__ unsigned long long red[4][TPB / 32];
     __shared__ int sys0;
+    if (d.nsys == 1) {
+        // one system: a grid-stride sweep over 16-byte pairs, four pairs of each array in flight
+        // per thread (the state arrays are 256-byte aligned)
+        const long long n2 = d.n_total >> 1, stride = (long long)gridDim.x * TPB;
+        const double2 *X2 = reinterpret_cast<const double2 *>(X), *Y2 = reinterpret_cast<const double2 *>(Y);
+        unsigned long long mn0 = ~0ull, mn1 = ~0ull, mx0 = 0, mx1 = 0;
+        long long i = (long long)blockIdx.x * TPB + threadIdx.x;
+        for (; i + 3 * stride < n2; i += 4 * stride) {
+            double2 a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                a[u] = X2[i + u * stride];
+                b[u] = Y2[i + u * stride];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                minmax_ord(ord_bits(a[u].x), mn0, mx0);
+                minmax_ord(ord_bits(a[u].y), mn0, mx0);
+                minmax_ord(ord_bits(b[u].x), mn1, mx1);
+                minmax_ord(ord_bits(b[u].y), mn1, mx1);
+            }
+        }
+        for (; i < n2; i += stride) {
+            const double2 a = X2[i], b = Y2[i];
+            minmax_ord(ord_bits(a.x), mn0, mx0);
+            minmax_ord(ord_bits(a.y), mn0, mx0);
+            minmax_ord(ord_bits(b.x), mn1, mx1);
+            minmax_ord(ord_bits(b.y), mn1, mx1);
+        }
+        if ((d.n_total & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+            minmax_ord(ord_bits(X[d.n_total - 1]), mn0, mx0);
+            minmax_ord(ord_bits(Y[d.n_total - 1]), mn1, mx1);
+        }
+        bbox_block_commit(d, 0, mn0, mn1, mx0, mx1, red);
+    }
     const long long tile = (long long)TPB * 16;
-    for (long long t0 = (long long)blockIdx.x * tile; t0 < d.n_total; t0 += (long long)gridDim.x * tile) {
+    for (long long t0 = (long long)blockIdx.x * tile; d.nsys > 1 && t0 < d.n_total; t0 += (long long)gridDim.x * tile) {
         long long t1 = t0 + tile < d.n_total ? t0 + tile : d.n_total;
         if (threadIdx.x == 0) sys0 = find_seg(d.poff_tab, d.nsys, t0);
         __syncthreads();
@@ -92,7 +157,6 @@ __global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
         bool one_sys = d.poff_tab[s_first + 1] >= t1;
         unsigned long long mn0 = ~0ull, mn1 = ~0ull, mx0 = 0, mx1 = 0;
         int cs = s_first;
-#pragma unroll 4
         for (long long i = t0 + threadIdx.x; i < t1; i += TPB) {
             if (!one_sys) {
                 int s = find_seg(d.poff_tab, d.nsys, i);
@@ -114,23 +178,7 @@ __global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
                 atomicMax(&d.dyn[cs].bbmax[0], mx0); atomicMax(&d.dyn[cs].bbmax[1], mx1);
             }
         } else {
-            for (int o = 16; o; o >>= 1) {
-                unsigned long long a = __shfl_xor_sync(0xffffffffu, mn0, o); mn0 = a < mn0 ? a : mn0;
-                a = __shfl_xor_sync(0xffffffffu, mn1, o); mn1 = a < mn1 ? a : mn1;
-                a = __shfl_xor_sync(0xffffffffu, mx0, o); mx0 = a > mx0 ? a : mx0;
-                a = __shfl_xor_sync(0xffffffffu, mx1, o); mx1 = a > mx1 ? a : mx1;
-            }
-            int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-            if (l == 0) { red[0][w] = mn0; red[1][w] = mn1; red[2][w] = mx0; red[3][w] = mx1; }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                for (int k = 1; k < TPB / 32; k++) {
-                    mn0 = red[0][k] < mn0 ? red[0][k] : mn0; mn1 = red[1][k] < mn1 ? red[1][k] : mn1;
-                    mx0 = red[2][k] > mx0 ? red[2][k] : mx0; mx1 = red[3][k] > mx1 ? red[3][k] : mx1;
-                }
-                atomicMin(&d.dyn[s_first].bbmin[0], mn0); atomicMin(&d.dyn[s_first].bbmin[1], mn1);
-                atomicMax(&d.dyn[s_first].bbmax[0], mx0); atomicMax(&d.dyn[s_first].bbmax[1], mx1);
-            }
+            bbox_block_commit(d, s_first, mn0, mn1, mx0, mx1, red);
         }
         __syncthreads();
     }
@@ -165,52 +213,101 @@ __global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
 // each particle also gets its quadrant within the box), and a histogram of (box, quadrant)
 // pairs aggregated over runs of equal keys in the block (a box's count is the sum of its
 // four); a particle's slot is its rank within its quadrant.
+constexpr int PLACE_PP = 4;  // consecutive particles per thread
+
 __global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
-    __shared__ int skeys[TPB], runold[TPB], wmax[TPB / 32];
+    constexpr int PT = TPB * PLACE_PP;  // particles per block round
+    __shared__ int skeys[PT + 1], runold[PT], wmax[TPB / 32];
     const int cur = d.glob->epoch & 1;
     const double *X = d.X[cur], *Y = d.Y[cur];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    long long stride = (long long)gridDim.x * blockDim.x;
-    long long base = (long long)blockIdx.x * blockDim.x;
-    for (; base < d.n_total; base += stride) {
-        long long i = base + threadIdx.x;
-        int key = -1;
-        if (i < d.n_total) {
-            int s = find_seg(d.poff_tab, d.nsys, i);
-            const SysDesc &sd = d.sys[s];
-            const SysDyn &dy = d.dyn[s];
-            double x = X[i], y = Y[i];
-            // finite test on the exponent bits (no FP64 operation)
-            const unsigned hx = (unsigned)(__double_as_longlong(x) >> 52) & 0x7FFu;
-            const unsigned hy = (unsigned)(__double_as_longlong(y) >> 52) & 0x7FFu;
-            if (hx == 0x7FFu || hy == 0x7FFu) raise_err(d.glob, 1u /*BH_DEV_NAN_POSITION*/);
-            // keys at twice the box resolution: box key and quadrant within the box
-            const int k2x = half_key1_f32(x, dy.minx, dy.step, dy.inv_step, dy.minx_f, dy.inv_step_f, dy.key_tol, sd.G);
-            const int k2y = half_key1_f32(y, dy.miny, dy.step, dy.inv_step, dy.miny_f, dy.inv_step_f, dy.key_tol, sd.G);
-            const int box = (int)(sd.boff + (long long)(k2x >> 1) * sd.G + (k2y >> 1));
-            key = 4 * box + (k2x & 1) * 2 + (k2y & 1);
+    const int e0 = (int)threadIdx.x * PLACE_PP;  // the thread's first particle in the round
+    for (long long base = (long long)blockIdx.x * PT; base < d.n_total; base += (long long)gridDim.x * PT) {
+        const long long i0 = base + e0;
+        double x[PLACE_PP], y[PLACE_PP];
+        if (i0 + PLACE_PP <= d.n_total && (i0 & 1) == 0) {  // (always, but for a ragged end)
+            const double2 *X2 = reinterpret_cast<const double2 *>(X + i0);
+            const double2 *Y2 = reinterpret_cast<const double2 *>(Y + i0);
+#pragma unroll
+            for (int j = 0; j < PLACE_PP / 2; j++) {
+                const double2 a = X2[j], b = Y2[j];
+                x[2 * j] = a.x; x[2 * j + 1] = a.y;
+                y[2 * j] = b.x; y[2 * j + 1] = b.y;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < PLACE_PP; j++) {
+                x[j] = i0 + j < d.n_total ? X[i0 + j] : 0.0;
+                y[j] = i0 + j < d.n_total ? Y[i0 + j] : 0.0;
+            }
         }
-        // runs of consecutive particles of the block with the same (box, quadrant): the run's
+        int key[PLACE_PP];
+#pragma unroll
+        for (int j = 0; j < PLACE_PP; j++) {
+            const long long i = i0 + j;
+            key[j] = -1;
+            if (i < d.n_total) {
+                const int s = find_seg(d.poff_tab, d.nsys, i);
+                const SysDesc &sd = d.sys[s];
+                const SysDyn &dy = d.dyn[s];
+                // finite test on the exponent bits (no FP64 operation)
+                const unsigned hx = (unsigned)(__double_as_longlong(x[j]) >> 52) & 0x7FFu;
+                const unsigned hy = (unsigned)(__double_as_longlong(y[j]) >> 52) & 0x7FFu;
+                if (hx == 0x7FFu || hy == 0x7FFu) raise_err(d.glob, 1u /*BH_DEV_NAN_POSITION*/);
+                // keys at twice the box resolution: box key and quadrant within the box
+                const int k2x = half_key1_f32(x[j], dy.minx, dy.step, dy.inv_step, dy.minx_f, dy.inv_step_f, dy.key_tol, sd.G);
+                const int k2y = half_key1_f32(y[j], dy.miny, dy.step, dy.inv_step, dy.miny_f, dy.inv_step_f, dy.key_tol, sd.G);
+                const int box = (int)(sd.boff + (long long)(k2x >> 1) * sd.G + (k2y >> 1));
+                key[j] = 4 * box + (k2x & 1) * 2 + (k2y & 1);
+            }
+            skeys[e0 + j] = key[j];
+        }
+        if (threadIdx.x == 0) skeys[PT] = INT_MIN;
+        // runs of consecutive particles of the round with the same (box, quadrant): the run's
         // last particle adds the run's length to the quadrant count, whose old value is the run's
-        // first slot, so a quadrant whose particles lie in one block gets its slots in input
+        // first slot, so a quadrant whose particles lie in one round gets its slots in input
         // order (the common case when the input is the previous step's order); k_segsort puts
         // the runs of different blocks in order
-        skeys[threadIdx.x] = key;
         __syncthreads();
-        const int kprev = threadIdx.x > 0 ? skeys[threadIdx.x - 1] : INT_MIN;
-        const int knext = threadIdx.x + 1 < TPB ? skeys[threadIdx.x + 1] : INT_MIN;
-        int h = key != kprev ? (int)threadIdx.x : 0;  // this run's first thread: a max-scan
+        int h[PLACE_PP];  // the first particle of each particle's run: a max-scan of run heads
+        int hm = 0;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) h = max(h, __shfl_up_sync(0xffffffffu, h, o) * (lane >= o));
-        if (lane == 31) wmax[warp] = h;
+        for (int j = 0; j < PLACE_PP; j++) {
+            const int e = e0 + j;
+            const int kp = e > 0 ? skeys[e - 1] : INT_MIN;
+            if (key[j] != kp) hm = e;
+            h[j] = hm;
+        }
+        int hx = hm;  // inclusive max over the threads before and including this one
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) hx = max(hx, __shfl_up_sync(0xffffffffu, hx, o) * (lane >= o));
+        if (lane == 31) wmax[warp] = hx;
+        int hb = __shfl_up_sync(0xffffffffu, hx, 1) * (lane >= 1);  // exclusive, within the warp
         __syncthreads();
-        for (int w = 0; w < warp; w++) h = max(h, wmax[w]);
-        const int rank = (int)threadIdx.x - h;
-        if (key >= 0 && key != knext) runold[h] = atomicAdd(&d.qcounts[key], rank + 1);
+        for (int w = 0; w < warp; w++) hb = max(hb, wmax[w]);
+#pragma unroll
+        for (int j = 0; j < PLACE_PP; j++) {
+            h[j] = max(h[j], hb);
+            const int e = e0 + j;
+            if (key[j] >= 0 && key[j] != skeys[e + 1]) runold[h[j]] = atomicAdd(&d.qcounts[key[j]], e - h[j] + 1);
+        }
         __syncthreads();
-        if (i < d.n_total) {
-            d.key[i] = key;  // 4 * box + quadrant
-            d.slot[i] = runold[h] + rank;
+        int kv[PLACE_PP], sv[PLACE_PP];
+#pragma unroll
+        for (int j = 0; j < PLACE_PP; j++) {
+            kv[j] = key[j];  // 4 * box + quadrant
+            sv[j] = key[j] >= 0 ? runold[h[j]] + (e0 + j - h[j]) : 0;
+        }
+        if (i0 + PLACE_PP <= d.n_total && (i0 & 3) == 0) {
+            *reinterpret_cast<int4 *>(d.key + i0) = make_int4(kv[0], kv[1], kv[2], kv[3]);
+            *reinterpret_cast<int4 *>(d.slot + i0) = make_int4(sv[0], sv[1], sv[2], sv[3]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < PLACE_PP; j++)
+                if (i0 + j < d.n_total) {
+                    d.key[i0 + j] = kv[j];
+                    d.slot[i0 + j] = sv[j];
+                }
         }
         __syncthreads();  // the block's shared arrays are reused in the next round
     }
@@ -674,13 +771,68 @@ __global__ void __launch_bounds__(TPB) k_segsort_big(DevPlan d) {
     }
 }
 
+// The leaf-moment terms of one particle (offsets from its box origin, mass), the segmented scan
+// of a warp's chunk of 32 box-sorted particles and the write of its sums: the box inside the
+// chunk gets its FP64 moments in mom, a box that starts before the chunk leaves its part in the
+// chunk's head partial, one that runs past it in the tail partial (k_summarize adds a multi-chunk
+// box's partials in chunk order).  The products are rounded one by one (no contraction), so the
+// fused pass in k_gather and the stand-alone k_leaf give the same sums.
+__device__ __forceinline__ void leaf_terms(float ox, float oy, float mf, float v[6]) {
+    v[0] = mf;
+    v[1] = __fmul_rn(mf, ox);
+    v[2] = __fmul_rn(mf, oy);
+    v[3] = __fmul_rn(v[1], ox);
+    v[4] = __fmul_rn(v[1], oy);
+    v[5] = __fmul_rn(v[2], oy);
+}
+
+// key: the lane's box (-1 past the end); c: the chunk (its first particle is 32 c)
+__device__ __forceinline__ void leaf_chunk(const DevPlan &d, long long c, int key, float v[6]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int k2 = __shfl_up_sync(0xffffffffu, key, o);
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            const float y = __shfl_up_sync(0xffffffffu, v[q], o);
+            if (lane >= o && k2 == key) v[q] = __fadd_rn(v[q], y);
+        }
+    }
+    const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+    const int kfirst = __shfl_sync(0xffffffffu, key, 0);
+    const bool last = key >= 0 && (lane == 31 || knext != key);  // the segment's last lane
+    if (!last) return;
+    const long long i0 = c << 5;
+    const bool head = key == kfirst && d.box_start[key] < i0;              // began in an earlier chunk
+    const bool tail = lane == 31 && d.box_start[key + 1] > i0 + 32;        // goes on in a later chunk
+    if (head || tail) {
+        float *pt = d.leafpart + 12 * c;
+        if (head)
+#pragma unroll
+            for (int q = 0; q < 6; q++) pt[q] = v[q];
+        if (tail)
+#pragma unroll
+            for (int q = 0; q < 6; q++) pt[6 + q] = v[q];
+    } else {
+        const int s = find_seg(d.boff_tab, d.nsys, key);
+        double *m = d.mom + 6 * (d.sys[s].coff + (key - d.sys[s].boff));
+#pragma unroll
+        for (int q = 0; q < 6; q++) m[q] = f32_to_f64(v[q]);
+    }
+}
+
+// Output particle t takes input perm[t]; each warp's 32 consecutive outputs form a leaf chunk,
+// whose moments are summed on the spot (the stand-alone k_leaf repeats this from the packed
+// records when the leaf moments were overwritten since).
 __global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
     const int cur = d.glob->epoch & 1, nxt = cur ^ 1;
+    const int lane = threadIdx.x & 31;
     // SU particles per thread per round, each stage's loads issued for all of them before the
-    // next stage uses them
+    // next stage uses them; the loop runs per warp (its first lane's index), for the scans
     constexpr int SU = 4;
     const long long n = d.n_total, stride = (long long)gridDim.x * blockDim.x;
-    for (long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; t0 < n; t0 += SU * stride) {
+    for (long long w0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); w0 < n; w0 += SU * stride) {
+        const long long t0 = w0 + lane;
         int src[SU], key4[SU];
 #pragma unroll
         for (int u = 0; u < SU; u++) {
@@ -707,9 +859,11 @@ __global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
                 pid[u] = d.PID[cur][i];
             }
         }
+        float lx[SU], ly[SU], lm[SU];
 #pragma unroll
         for (int u = 0; u < SU; u++) {
             const long long t = t0 + u * stride;
+            lx[u] = ly[u] = lm[u] = 0.f;
             if (t >= n) continue;
             const int key = key4[u] >> 2;
             const int s = find_seg(d.boff_tab, d.nsys, key);
@@ -730,6 +884,18 @@ __global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
             d.PD[2 * t] = make_float4(ox, ox, oy, oy);
             d.PD[2 * t + 1] = make_float4(mf, mf, __int_as_float((int)t), __int_as_float((kx << 16) | ky));
             d.skey[t] = key;
+            lx[u] = ox;
+            ly[u] = oy;
+            lm[u] = mf;
+        }
+#pragma unroll
+        for (int u = 0; u < SU; u++) {
+            const long long wu = w0 + u * stride;  // the chunk's first particle
+            if (wu >= n) break;                    // (warp-uniform)
+            const long long t = wu + lane;
+            float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (t < n) leaf_terms(lx[u], ly[u], lm[u], v);
+            leaf_chunk(d, wu >> 5, t < n ? key4[u] >> 2 : -1, v);
         }
     }
 }
@@ -794,81 +960,24 @@ __device__ __forceinline__ void cell_record(const DevPlan &d, long long c, int l
     }
 }
 
-// Leaf moments, balanced over the particles: a warp per chunk of 32 box-sorted particles sums
-// each box's part of the chunk with a segmented FP32 scan (offsets are box-relative, so 32 terms
-// keep ~1e-7 of a box edge).  A box that lies inside the chunk gets its FP64 moments written
-// here; a box that starts before the chunk leaves its part in the chunk's head partial, a box
-// that runs past it in the tail partial (a chunk of one box that runs both ways: both), and
-// k_summarize adds a multi-chunk box's partials in chunk order.  No atomics: fixed summation
-// order.
+// Leaf moments from the packed records, balanced over the particles: a warp per chunk of 32
+// box-sorted particles (k_gather does the same while it writes the records; this pass runs when
+// the leaf moments have been overwritten since, bh_set_leaf_moments).  No atomics: fixed
+// summation order.
 __global__ void __launch_bounds__(TPB) k_leaf(DevPlan d) {
     const int lane = threadIdx.x & 31;
     const long long nch = (d.n_total + 31) >> 5;
-    const long long cstride = ((long long)gridDim.x * blockDim.x) >> 5;
-    long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    // the next chunk's key and record are loaded while this one is summed
-    int nkey = -1;
-    float4 np = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (c < nch && (c << 5) + lane < d.n_total) {
-        nkey = d.skey[(c << 5) + lane];
-        np = d.P[(c << 5) + lane];
-    }
-    for (; c < nch; c += cstride) {
+    for (long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nch;
+         c += ((long long)gridDim.x * blockDim.x) >> 5) {
         const long long i = (c << 5) + lane;
-        const int ckey = nkey;
-        const float4 p = np;
-        const long long inx = ((c + cstride) << 5) + lane;
-        if (c + cstride < nch && inx < d.n_total) {
-            nkey = d.skey[inx];
-            np = d.P[inx];
-        }
         int key = -1;
         float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (i < d.n_total) {
-            key = ckey;
-            v[0] = p.z;
-            v[1] = p.z * p.x;
-            v[2] = p.z * p.y;
-            v[3] = v[1] * p.x;
-            v[4] = v[1] * p.y;
-            v[5] = v[2] * p.y;
+            key = d.skey[i];
+            const float4 p = d.P[i];
+            leaf_terms(p.x, p.y, p.z, v);
         }
-        // the keys just before and after the chunk tell whether its first and last boxes go on
-        int kprev = -1, knext_chunk = -1;
-        if (lane == 0 && c > 0) kprev = d.skey[(c << 5) - 1];
-        if (lane == 0 && (c << 5) + 32 < d.n_total) knext_chunk = d.skey[(c << 5) + 32];
-        kprev = __shfl_sync(0xffffffffu, kprev, 0);
-        knext_chunk = __shfl_sync(0xffffffffu, knext_chunk, 0);
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int k2 = __shfl_up_sync(0xffffffffu, key, o);
-#pragma unroll
-            for (int q = 0; q < 6; q++) {
-                const float y = __shfl_up_sync(0xffffffffu, v[q], o);
-                if (lane >= o && k2 == key) v[q] += y;
-            }
-        }
-        const int knext = __shfl_down_sync(0xffffffffu, key, 1);
-        const int kfirst = __shfl_sync(0xffffffffu, key, 0);
-        const bool last = key >= 0 && (lane == 31 || knext != key);  // the segment's last lane
-        if (last) {
-            const bool head = key == kfirst && key == kprev;        // began in an earlier chunk
-            const bool tail = lane == 31 && key == knext_chunk;     // goes on in a later chunk
-            if (head || tail) {
-                float *pt = d.leafpart + 12 * c;
-                if (head)
-#pragma unroll
-                    for (int q = 0; q < 6; q++) pt[q] = v[q];
-                if (tail)
-#pragma unroll
-                    for (int q = 0; q < 6; q++) pt[6 + q] = v[q];
-            } else {
-                const int s = find_seg(d.boff_tab, d.nsys, key);
-                double *m = d.mom + 6 * (d.sys[s].coff + (key - d.sys[s].boff));
-#pragma unroll
-                for (int q = 0; q < 6; q++) m[q] = f32_to_f64(v[q]);
-            }
-        }
+        leaf_chunk(d, c, key, v);
     }
 }
 
@@ -1054,12 +1163,12 @@ cudaError_t launch_prologue(const DevPlan &d, cudaStream_t st) {
 }
 cudaError_t launch_bbox(const DevPlan &d, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_bbox<<<grid_for(d.n_total, TPB * 16, d.nsm * 8LL), TPB, 0, st>>>(d);
+    k_bbox<<<d.nsys == 1 ? (unsigned)(d.nsm * 4) : grid_for(d.n_total, TPB * 16, d.nsm * 8LL), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
 cudaError_t launch_place(const DevPlan &d, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_place<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
+    k_place<<<grid_for(d.n_total, TPB * PLACE_PP, d.nsm * 8LL), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
 cudaError_t launch_scan(const DevPlan &d, cudaStream_t st) {
@@ -1098,8 +1207,10 @@ cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
     k_gather<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
-cudaError_t launch_summarize(const DevPlan &d, cudaStream_t st) {
-    if (d.n_total > 0) k_leaf<<<grid_for((d.n_total + 31) / 32, TPB / 32, d.nsm * 8LL), TPB, 0, st>>>(d);
+// leaves: the leaf sums of k_gather were overwritten since (bh_set_leaf_moments): redo them
+cudaError_t launch_summarize(const DevPlan &d, bool leaves, cudaStream_t st) {
+    if (leaves && d.n_total > 0)
+        k_leaf<<<grid_for((d.n_total + 31) / 32, TPB / 32, d.nsm * 8LL), TPB, 0, st>>>(d);
     // the normalised second moments feed only the learned correction
     k_summarize<<<grid_for(d.T_total, 1, d.nsm * 8LL), SUM_THREADS, 0, st>>>(d, d.learned != 0, 0);
     return cudaGetLastError();

@@ -116,6 +116,9 @@ def test_launch_count_host_logic(lib):
         return c.value
 
     stream = count()
+    # prologue, bbox, place, box scan, 4 scatter kernels, stream items, summarize, lists, item
+    # order (2), force
+    assert stream == 14
     # walk items and the walk's own tick in, stream items and lists out
     assert count(flags=native.BH_FLAG_WALK) == stream + 3 + 1 - 4
     assert count(flags=native.BH_FLAG_LEARNED) == stream + 3

@@ -402,6 +402,31 @@ def test_long_quadrants_sorted():
                           ref["ax"], ref["ay"]) <= 1e-5
 
 
+def test_summarize_after_set_leaf_moments():
+    """The leaf sums come with the scatter (k_gather); after bh_set_leaf_moments overwrote them,
+    bh_summarize sums the leaves from the particles again (the stand-alone leaf pass): the leaf
+    moments and the step equal those of a plan that never had them replaced, bit for bit.  Boxes
+    of 1 to ~600 particles cover single-chunk boxes and boxes over many chunks."""
+    from barneshut.gb300 import workloads
+
+    x, y, m, vx, vy = workloads.cluster_mixture(30000, seed=71)
+    kw = dict(grav_constant=1.0, tick_seconds=1e-5, softening=1e-3, cutoff_r2=0.0, theta=0.5)
+    a = make_plan(30000, 16, **kw)
+    b = make_plan(30000, 16, **kw)
+    for p in (a, b):
+        p.load(x, y, m, vx, vy)
+        p.create_tree()
+    a.summarize()
+    b.set_leaf_moments(torch.full((16, 16, 6), 3.0, dtype=torch.float64, device="cuda"))
+    b.summarize()
+    la, lb = a.leaf_moments(), b.leaf_moments()
+    assert torch.equal(la, lb)
+    assert la[..., 0].sum().item() == pytest.approx(float(np.sum(m)), rel=1e-6)
+    a.evaluate()
+    b.evaluate()
+    assert_same_run(a.store(), b.store(), exact=True)
+
+
 def test_graph_replay_equals_eager():
     from barneshut.gb300 import workloads
 
