@@ -48,6 +48,8 @@ struct bh_plan {
     // graph cache
     cudaGraphExec_t gexec = nullptr;
     size_t sst_bytes = 0;  // the single-pass scans' tile states
+    size_t o_upcnt = 0;
+    long long up_total = 0;  // pyramid cells above the summarize tiles, over all systems
     cudaEvent_t tev[2] = {nullptr, nullptr};  // bh_set_kernel_timing: around the force kernel
     bool timing = false;
     bool tev_recorded = false;
@@ -181,6 +183,8 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
         d.goff = p->goff[s];
         d.tps = (G + SUM_TILE - 1) / SUM_TILE;
         d.toff = p->toff[s];
+        d.upoff = p->up_total;
+        p->up_total += L > 5 ? cells - d.lvoff[5] : 0;
         p->poff[s + 1] = p->poff[s] + n[s];
         p->boff[s + 1] = p->boff[s] + (long long)G * G;
         p->coff[s + 1] = p->coff[s] + cells;
@@ -290,6 +294,7 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     p->o_sichk = take(8 * sitems);
     p->o_ibkt = take(p->stream ? 4 * 2 * ITEM_BUCKETS : 0);
     p->o_mom = take(48 * C);
+    p->o_upcnt = take(4 * (size_t)p->up_total);
     p->o_leafpart = take(48 * (N / 32 + 1));
     p->o_rec = take(16 * C);
     p->o_rec2 = take(16 * C);
@@ -367,6 +372,7 @@ static void fill_dev(bh_plan *p) {
     d.item_group = (int *)(w + p->o_igrp);
     d.mom = (double *)(w + p->o_mom);
     d.leafpart = (float *)(w + p->o_leafpart);
+    d.upcnt = (unsigned *)(w + p->o_upcnt);
     d.rec = (float4 *)(w + p->o_rec);
     d.rec2 = (float4 *)(w + p->o_rec2);
     d.org = (double *)(w + p->o_org);
@@ -429,6 +435,7 @@ extern "C" int bh_bind(bh_plan *p, void *workspace, size_t bytes, void *stream) 
                               cudaMemcpyHostToDevice, st), "scan generations");
         CK(p, cudaMemsetAsync(w + p->o_sst, 0, p->sst_bytes, st), "zero scan states");
     }
+    CK(p, cudaMemsetAsync(w + p->o_upcnt, 0, 4 * (size_t)p->up_total, st), "zero arrival counters");
     CK(p, cudaStreamSynchronize(st), "bind sync");
     p->has_tree = false;
     p->acc_stale = true;

@@ -60,6 +60,7 @@ struct SysDesc {
     long long ooff;              // first entry of the system's box-origin table (G x, then G y)
     int tps;                     // summarize tiles (SUM_TILE x SUM_TILE leaf boxes) per side
     long long toff;              // first summarize tile of the system
+    long long upoff;             // first arrival counter of the system's cells above the tiles
     int fixed_grid;              // 1: the square box comes from fg_ext, not from the particles
     double fg_ext[4];            // min x, min y, max x, max y of the whole system (bh_set_grid)
 };
@@ -72,7 +73,6 @@ struct SysDyn {
     float minx_f, miny_f;         // the origin rounded to float
     float inv_step_f;             // 1 / step rounded to float
     float key_tol;                // bound on |float quotient - exact quotient| (box edges)
-    unsigned int tiles_done;      // summarize tiles finished this step (the last one resets it)
 };
 
 struct Globals {
@@ -123,6 +123,8 @@ struct DevPlan {
     int *item_cnt, *item_off, *item_group;  // force work items (group, target chunk)
     double *org;  // per system: box origins mn + k step along x (k < G), then along y, FP64
     double *mom;
+    unsigned *upcnt;  // per pyramid cell above the summarize tiles (levels >= 5): children done
+                      // this step (the last child's CTA builds the cell and resets it)
     float *leafpart;  // per chunk of 32 box-sorted particles: head and tail partial moments (k_leaf)
     float4 *rec, *rec2;
     // interaction lists of every target group (list-streaming path), in fixed per-group slots

@@ -902,21 +902,21 @@ __global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
 
 // ---------------------------------------------------------------- summarize
 // One CTA per tile of SUM_TILE x SUM_TILE leaf boxes: the boxes' moments (M, Sx, Sy, Sxx, Sxy,
-// Syy about the box origin) from their box-sorted particles, then pyramid levels 1..4 inside the
-// tile, then the cell records of all of them; the CTA that finishes a system's last tile builds
-// the levels above (cells of 2^5 boxes and larger) from the tiles' level-4 cells.  A tile row (a
-// column of SUM_TILE boxes of one x) is contiguous in particle order; one warp streams it in
-// chunks of 32 particles, a segmented FP32 scan by box sums each box's part of a chunk (offsets
-// are box-relative, so 32 terms keep ~1e-7 of a box edge), and the segment's last lane adds it
-// to the box's FP64 sum in shared memory.  Every sum runs in a fixed order, so the moments do
-// not depend on scheduling.
+// Syy about the box origin; k_gather summed them per chunk of 32 box-sorted particles), then
+// pyramid levels 1..4 inside the tile, then the cell records of all of them.  Above the tiles
+// (cells of 2^5 boxes and larger) a cell is built by the CTA that finishes its last child: each
+// cell counts its children's arrivals, so the levels above rise along a reduction tree instead of
+// waiting for one CTA.  Every sum runs in a fixed order, so the moments do not depend on
+// scheduling.  Pyramid cells carry the second moments only for the learned correction (SECOND);
+// the leaves always carry all six.
 constexpr int SUM_THREADS = 256;
-constexpr int SUM_WARPS = SUM_THREADS / 32;
 constexpr int SUM_CELLS = 256 + 64 + 16 + 4 + 1;  // a tile's cells at levels 0..4
+constexpr int SUM_UP = 5;                         // the first level above the tiles (2^5 boxes)
+static_assert(SUM_TILE == 1 << (SUM_UP - 1), "a tile is one cell of level SUM_UP - 1");
 
 // The moments of child (a, b) of a level-l cell (q, FP64 about the child's origin) shifted to the
-// cell origin, into o[6]; zeros when the child lies outside the grid.  sum_children adds a cell's
-// four shifted children in (0, 0), (0, 1), (1, 0), (1, 1) order.
+// cell origin, into o[6] (o[0..2] without SECOND); zeros when the child lies outside the grid.
+template <bool SECOND>
 __device__ __forceinline__ void child_terms(const double *q, bool has, int a, int b, int l, double step,
                                             double *o) {
     if (!has) {
@@ -929,25 +929,30 @@ __device__ __forceinline__ void child_terms(const double *q, bool has, int a, in
     o[0] = M;
     o[1] = Sx + M * dx;
     o[2] = Sy + M * dy;
-    o[3] = q[3] + 2.0 * dx * Sx + M * dx * dx;
-    o[4] = q[4] + dx * Sy + dy * Sx + M * dx * dy;
-    o[5] = q[5] + 2.0 * dy * Sy + M * dy * dy;
+    if (SECOND) {
+        o[3] = q[3] + 2.0 * dx * Sx + M * dx * dx;
+        o[4] = q[4] + dx * Sy + dy * Sx + M * dx * dy;
+        o[5] = q[5] + 2.0 * dy * Sy + M * dy * dy;
+    }
 }
 
+// a cell's four shifted children added in (0, 0), (0, 1), (1, 0), (1, 1) order
+template <bool SECOND>
 __device__ __forceinline__ void sum_children(const double *t, double *p) {
 #pragma unroll
-    for (int k = 0; k < 6; k++) p[k] = ((t[k] + t[6 + k]) + t[12 + k]) + t[18 + k];
+    for (int k = 0; k < (SECOND ? 6 : 3); k++) p[k] = ((t[k] + t[6 + k]) + t[12 + k]) + t[18 + k];
 }
 
-// Float records of cell c (level l) of system s: centre of mass relative to the cell origin and
-// mass; with `second`, the second moments about the centre of mass normalised by M s^2.
+// Float records of cell c (level l): centre of mass relative to the cell origin and mass; with
+// SECOND, the second moments about the centre of mass normalised by M s^2.
+template <bool SECOND>
 __device__ __forceinline__ void cell_record(const DevPlan &d, long long c, int l, double step,
-                                            const double *q, int second) {
+                                            const double *q) {
     const double M = q[0];
     if (M > 0.0) {
         const double cx = q[1] / M, cy = q[2] / M;
         d.rec[c] = make_float4(f64_to_f32_rn(cx), f64_to_f32_rn(cy), f64_to_f32_rn(M), 0.f);
-        if (second) {
+        if (SECOND) {
             const double sz = (double)(1 << l) * step;
             const double nrm = 1.0 / (M * sz * sz);
             const double ixx = q[3] - q[1] * cx, ixy = q[4] - q[1] * cy, iyy = q[5] - q[2] * cy;
@@ -956,7 +961,7 @@ __device__ __forceinline__ void cell_record(const DevPlan &d, long long c, int l
         }
     } else {
         d.rec[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (second) d.rec2[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (SECOND) d.rec2[c] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
@@ -990,11 +995,12 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
 }
 
 // leaves_given: the leaf moments are already in d.mom (bh_set_leaf_moments); build the rest.
-__global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int second, int leaves_given) {
+template <bool SECOND>
+__global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int leaves_given) {
+    constexpr int NM = SECOND ? 6 : 3;  // moments a pyramid cell carries
     __shared__ double cm[SUM_CELLS * 6];  // the tile's cells, level by level
     __shared__ double chm[4 * 64 * 6];    // shifted child moments: 64 cells x 4 children
-    __shared__ unsigned ticket;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
     const int loff[5] = {0, 256, 320, 336, 340};
     for (long long t = blockIdx.x; t < d.T_total; t += gridDim.x) {
         const int s = find_seg(d.toff_tab, d.nsys, t);
@@ -1003,7 +1009,7 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
         const int G = sd.G, lt = (int)(t - sd.toff), ti = lt / sd.tps, tj = lt - ti * sd.tps;
         const int bx0 = ti * SUM_TILE, by0 = tj * SUM_TILE;
         const int nbx = min(SUM_TILE, G - bx0), nby = min(SUM_TILE, G - by0);
-        const int lmax = min(4, sd.L - 1);  // the tile's top level
+        const int lmax = min(SUM_UP - 1, sd.L - 1);  // the tile's top level
         // ---- level 0: the tile's boxes (zeros outside the grid)
         for (int k = tid; k < 6 * SUM_TILE * SUM_TILE; k += SUM_THREADS) {
             const int box = k / 6, cx = box / SUM_TILE, cy = box - cx * SUM_TILE;
@@ -1014,19 +1020,20 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
         }
         __syncthreads();
         if (!leaves_given) {
-            // a box inside one chunk has its moments from k_leaf; a box over several chunks adds
-            // its partials in chunk order: the first chunk's tail, whole middle chunks, the last
-            // chunk's head
+            // a box inside one chunk has its moments from the chunk's sums; a box over several
+            // chunks adds its partials in chunk order (the first chunk's tail, whole middle
+            // chunks, the last chunk's head) and writes the sum to mom
             for (int k = tid; k < SUM_TILE * SUM_TILE; k += SUM_THREADS) {
                 const int cx = k / SUM_TILE, cy = k - cx * SUM_TILE;
                 if (cx >= nbx || cy >= nby) continue;
                 const long long lb = (long long)(bx0 + cx) * G + (by0 + cy);
                 const int i0 = d.box_start[sd.boff + lb], i1 = d.box_start[sd.boff + lb + 1];
                 if (i1 == i0) continue;  // empty: zeros
+                double *mb = d.mom + 6 * (sd.coff + lb);
                 const long long c0 = i0 >> 5, c1 = (long long)(i1 - 1) >> 5;
                 if (c0 == c1) {
 #pragma unroll
-                    for (int q = 0; q < 6; q++) cm[6 * k + q] = d.mom[6 * (sd.coff + lb) + q];
+                    for (int q = 0; q < 6; q++) cm[6 * k + q] = mb[q];
                     continue;
                 }
                 float sm_[6], cc_[6];
@@ -1039,14 +1046,13 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
 #pragma unroll
                     for (int q = 0; q < 6; q++) kahan_add(sm_[q], cc_[q], d.leafpart[12 * c + q]);
 #pragma unroll
-                for (int q = 0; q < 6; q++) cm[6 * k + q] = f32_to_f64(__fsub_rn(sm_[q], cc_[q]));
+                for (int q = 0; q < 6; q++) {
+                    const double v = f32_to_f64(__fsub_rn(sm_[q], cc_[q]));
+                    cm[6 * k + q] = v;
+                    mb[q] = v;
+                }
             }
             __syncthreads();
-            for (int k = tid; k < 6 * SUM_TILE * SUM_TILE; k += SUM_THREADS) {
-                const int box = k / 6, cx = box / SUM_TILE, cy = box - cx * SUM_TILE;
-                if (cx < nbx && cy < nby)
-                    d.mom[6 * (sd.coff + (long long)(bx0 + cx) * G + (by0 + cy)) + (k - 6 * box)] = cm[k];
-            }
         }
         // ---- levels 1..lmax inside the tile: a thread per (cell, child) shifts the child's
         // moments to the cell origin, then a thread per cell adds its four children in order
@@ -1058,22 +1064,22 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
                 const int cell = t >> 2, a = (t >> 1) & 1, b = t & 1;
                 const int ci = cell / nl, cj = cell - ci * nl;
                 const bool has = 2 * (I0 + ci) + a < gc && 2 * (J0 + cj) + b < gc;
-                child_terms(cm + 6 * (loff[l - 1] + (2 * ci + a) * nc + (2 * cj + b)), has, a, b, l,
-                            step, chm + 6 * t);
+                child_terms<SECOND>(cm + 6 * (loff[l - 1] + (2 * ci + a) * nc + (2 * cj + b)), has, a, b,
+                                    l, step, chm + 6 * t);
             }
             __syncthreads();
             for (int c = tid; c < nl * nl; c += SUM_THREADS) {
                 const int ci = c / nl, cj = c - ci * nl;
                 const bool inside = I0 + ci < gl && J0 + cj < gl;
                 double p[6];
-                sum_children(chm + 24 * c, p);
+                sum_children<SECOND>(chm + 24 * c, p);
 #pragma unroll
-                for (int k = 0; k < 6; k++) cm[6 * (loff[l] + c) + k] = inside ? p[k] : 0.0;
+                for (int k = 0; k < NM; k++) cm[6 * (loff[l] + c) + k] = inside ? p[k] : 0.0;
                 if (inside) {
                     const long long cc = sd.coff + sd.lvoff[l] + (long long)(I0 + ci) * gl + (J0 + cj);
 #pragma unroll
-                    for (int k = 0; k < 6; k++) d.mom[6 * cc + k] = p[k];
-                    cell_record(d, cc, l, step, p, second);
+                    for (int k = 0; k < NM; k++) d.mom[6 * cc + k] = p[k];
+                    cell_record<SECOND>(d, cc, l, step, p);
                 }
             }
             __syncthreads();
@@ -1082,46 +1088,48 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int sec
         for (int k = tid; k < SUM_TILE * SUM_TILE; k += SUM_THREADS) {
             const int cx = k / SUM_TILE, cy = k - cx * SUM_TILE;
             if (cx >= nbx || cy >= nby) continue;
-            cell_record(d, sd.coff + (long long)(bx0 + cx) * G + (by0 + cy), 0, step, cm + 6 * k, second);
+            cell_record<SECOND>(d, sd.coff + (long long)(bx0 + cx) * G + (by0 + cy), 0, step, cm + 6 * k);
         }
-        // ---- the system's last tile builds the levels above the tiles, 64 cells at a time
-        __threadfence();
-        __syncthreads();
-        if (tid == 0) ticket = atomicAdd(&d.dyn[s].tiles_done, 1u);
-        __syncthreads();
-        if (ticket == (unsigned)(sd.tps * sd.tps) - 1u) {
+        // ---- above the tiles: the tile's top cell arrives at its parent; the CTA whose child
+        // arrives last builds the parent (children in (0, 0), (0, 1), (1, 0), (1, 1) order, the
+        // order of sum_children) and arrives at the next level
+        if (sd.L > SUM_UP) {
             __threadfence();
-            for (int l = lmax + 1; l < sd.L; l++) {
-                const int gl = sd.lvg[l], gc = sd.lvg[l - 1];
-                for (int c0 = 0; c0 < gl * gl; c0 += 64) {
-                    const int t = tid, cell = c0 + (t >> 2), a = (t >> 1) & 1, b = t & 1;
-                    if (cell < gl * gl) {
-                        const int I = cell / gl, J = cell - I * gl;
-                        const int ci = 2 * I + a, cj = 2 * J + b;
-                        const bool has = ci < gc && cj < gc;
-                        double q[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-                        if (has) {
-                            const double *src = d.mom + 6 * (sd.coff + sd.lvoff[l - 1] + (long long)ci * gc + cj);
+            __syncthreads();
+            if (tid == 0) {
+                int I = ti, J = tj;
+                for (int l = SUM_UP; l < sd.L; l++) {
+                    I >>= 1;
+                    J >>= 1;
+                    const int gl = sd.lvg[l], gc = sd.lvg[l - 1];
+                    const int nch = (2 * I + 1 < gc ? 2 : 1) * (2 * J + 1 < gc ? 2 : 1);
+                    const long long cl = sd.lvoff[l] + (long long)I * gl + J;  // relative to coff
+                    unsigned *cnt = d.upcnt + sd.upoff + (cl - sd.lvoff[SUM_UP]);
+                    if (atomicAdd(cnt, 1u) != (unsigned)nch - 1u) break;
+                    __threadfence();
+                    *cnt = 0u;  // ready for the next step
+                    double p[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+                    for (int a = 0; a < 2; a++)
+                        for (int b = 0; b < 2; b++) {
+                            const bool has = 2 * I + a < gc && 2 * J + b < gc;
+                            double q[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, o[6];
+                            if (has) {
+                                const double *src =
+                                    d.mom + 6 * (sd.coff + sd.lvoff[l - 1] + (long long)(2 * I + a) * gc + (2 * J + b));
 #pragma unroll
-                            for (int k = 0; k < 6; k++) q[k] = __ldcg(src + k);
+                                for (int k = 0; k < NM; k++) q[k] = __ldcg(src + k);
+                            }
+                            child_terms<SECOND>(q, has, a, b, l, step, o);
+#pragma unroll
+                            for (int k = 0; k < NM; k++) p[k] = (a | b) ? p[k] + o[k] : o[k];
                         }
-                        child_terms(q, has, a, b, l, step, chm + 6 * t);
-                    }
-                    __syncthreads();
-                    if (tid < 64 && c0 + tid < gl * gl) {
-                        double p[6];
-                        sum_children(chm + 24 * tid, p);
-                        const long long cc = sd.coff + sd.lvoff[l] + c0 + tid;
+                    const long long cc = sd.coff + cl;
 #pragma unroll
-                        for (int k = 0; k < 6; k++) d.mom[6 * cc + k] = p[k];
-                        cell_record(d, cc, l, step, p, second);
-                    }
-                    __syncthreads();
+                    for (int k = 0; k < NM; k++) d.mom[6 * cc + k] = p[k];
+                    cell_record<SECOND>(d, cc, l, step, p);
+                    __threadfence();
                 }
-                __threadfence();
-                __syncthreads();
             }
-            if (tid == 0) d.dyn[s].tiles_done = 0u;
         }
         __syncthreads();
     }
@@ -1211,12 +1219,16 @@ cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
 cudaError_t launch_summarize(const DevPlan &d, bool leaves, cudaStream_t st) {
     if (leaves && d.n_total > 0)
         k_leaf<<<grid_for((d.n_total + 31) / 32, TPB / 32, d.nsm * 8LL), TPB, 0, st>>>(d);
-    // the normalised second moments feed only the learned correction
-    k_summarize<<<grid_for(d.T_total, 1, d.nsm * 8LL), SUM_THREADS, 0, st>>>(d, d.learned != 0, 0);
+    // the second moments of the pyramid cells feed only the learned correction
+    const unsigned g = grid_for(d.T_total, 1, d.nsm * 8LL);
+    if (d.learned) k_summarize<true><<<g, SUM_THREADS, 0, st>>>(d, 0);
+    else k_summarize<false><<<g, SUM_THREADS, 0, st>>>(d, 0);
     return cudaGetLastError();
 }
 cudaError_t launch_pyramid(const DevPlan &d, cudaStream_t st) {
-    k_summarize<<<grid_for(d.T_total, 1, d.nsm * 8LL), SUM_THREADS, 0, st>>>(d, d.learned != 0, 1);
+    const unsigned g = grid_for(d.T_total, 1, d.nsm * 8LL);
+    if (d.learned) k_summarize<true><<<g, SUM_THREADS, 0, st>>>(d, 1);
+    else k_summarize<false><<<g, SUM_THREADS, 0, st>>>(d, 1);
     return cudaGetLastError();
 }
 cudaError_t launch_records(const DevPlan &d, bool second, cudaStream_t st) {
