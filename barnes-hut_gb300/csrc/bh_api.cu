@@ -853,9 +853,10 @@ extern "C" int bh_learned_pairs(bh_plan *p, double theta_hi, double theta_lo, in
     if (!(theta_hi > theta_lo) || !(theta_lo > 0.0) || item_stride < 1 || item_offset < 0 ||
         tpi < 1 || capacity < 0 || !feats || !targets || !counter)
         return fail(p, BH_ERR_INVALID, "bad learned_pairs arguments");
-    // a plan without the learned correction builds neither the cell records' second moments nor
-    // (when streaming) the walk items in its step
-    if (!p->dev.learned) CK(p, launch_records(p->dev, true, (cudaStream_t)stream), "cell records");
+    // a plan without the learned correction builds neither the pyramid's second moments nor
+    // (when streaming) the walk items in its step: rebuild the pyramid above the summed leaves
+    // with them (the same centres of mass and masses)
+    if (!p->dev.learned) CK(p, launch_pyramid(p->dev, (cudaStream_t)stream, true), "second moments");
     if (p->dev.stream && !p->dev.learned) CK(p, launch_walk_items(p->dev, (cudaStream_t)stream), "work items");
     CK(p, launch_learned_pairs(p->dev, theta_hi, theta_lo, max_level, item_offset, item_stride, tpi,
                                feats, targets, counter, capacity, (cudaStream_t)stream),

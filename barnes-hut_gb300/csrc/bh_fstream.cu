@@ -15,7 +15,9 @@
 //     swept; each pass's plain FP32 sum enters the running total through a Kahan-compensated
 //     addition (BH_PREC_FP32_KAHAN) or a plain one (BH_PREC_FP32);
 //   * near field: the near boxes' 32-byte packed records (x, x, y, y), (m, m, index, box) are
-//     copied box piece by box piece into the warp's staging by bulk asynchronous copies (TMA),
+//     copied piece by piece (a piece: a run of listed boxes whose particles are contiguous, as
+//     the boxes of one column of the near region are) into the warp's staging by bulk
+//     asynchronous copies (TMA),
 //     WSRC sources per pass, double-buffered on two mbarriers so the copy of pass p + 1 overlaps
 //     the sweep of pass p; the lanes shift each staged source from its box frame into the group
 //     frame in place before the sweep, the shift following from the box coordinates that the
@@ -346,6 +348,35 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                 __syncwarp();
                 if (nacc > 0) far_sweep(nacc, false);  // (also orders the staging for the copies)
                 nn = nkeep;
+            }
+            // boxes listed one after another whose particles are contiguous (a column of the
+            // near region: the lists are in box order) become one piece, copied at once
+            {
+                int bx[WDESC / 32], px[WDESC / 32];
+                bool head[WDESC / 32];
+#pragma unroll
+                for (int u = 0; u < WDESC / 32; u++) {
+                    const int k = lane + 32 * u;
+                    bx[u] = k < nn ? nbox[k] : 0;
+                    px[u] = k < nn ? npre[k] : 0;
+                    head[u] = k < nn && (k == 0 || nbox[k - 1] + (px[u] - npre[k - 1]) != bx[u]);
+                }
+                const int total = npre[nn];
+                __syncwarp();
+                int np = 0;
+#pragma unroll
+                for (int u = 0; u < WDESC / 32; u++) {
+                    const unsigned hm = __ballot_sync(0xffffffffu, head[u]);
+                    if (head[u]) {
+                        const int q = np + __popc(hm & ((1u << lane) - 1u));
+                        nbox[q] = bx[u];
+                        npre[q] = px[u];
+                    }
+                    np += __popc(hm);
+                }
+                if (lane == 0) npre[np] = total;
+                __syncwarp();
+                nn = np;
             }
             const int pbeg = npre[0], pend = npre[nn];
             const int npass = (pend - pbeg + WSRC - 1) / WSRC;

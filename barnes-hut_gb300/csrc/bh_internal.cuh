@@ -363,11 +363,11 @@ cudaError_t launch_place(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_scan(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_items(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_walk_items(const DevPlan &d, cudaStream_t st);
-cudaError_t launch_records(const DevPlan &d, bool second, cudaStream_t st);
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_summarize(const DevPlan &d, bool leaves, cudaStream_t st);
 // the pyramid levels above the leaves and the cell records, from the leaf moments
-cudaError_t launch_pyramid(const DevPlan &d, cudaStream_t st);
+// second: also the pyramid's second moments and their records (always with the learned correction)
+cudaError_t launch_pyramid(const DevPlan &d, cudaStream_t st, bool second = false);
 // ev (optional): two events recorded on st right before and after the force kernel proper
 cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st,
                          const cudaEvent_t *ev = nullptr);

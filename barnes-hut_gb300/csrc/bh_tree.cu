@@ -1135,34 +1135,6 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int lea
     }
 }
 
-// Float records: centre of mass relative to the cell origin and mass; second
-// moments about the centre of mass normalised by M s^2 (s = cell edge).
-__global__ void __launch_bounds__(TPB) k_records(DevPlan d, int second) {
-    long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < d.C_total; c += stride) {
-        const double *q = d.mom + 6 * c;
-        double M = q[0];
-        if (M > 0.0) {
-            double cx = q[1] / M, cy = q[2] / M;
-            d.rec[c] = make_float4(f64_to_f32_rn(cx), f64_to_f32_rn(cy), f64_to_f32_rn(M), 0.f);
-            if (!second) continue;
-            int s = find_seg(d.coff_tab, d.nsys, c);
-            const SysDesc &sd = d.sys[s];
-            long long loc = c - sd.coff;
-            int l = 0;
-            while (l + 1 < sd.L && sd.lvoff[l + 1] <= loc) l++;
-            double sz = (double)(1 << l) * d.dyn[s].step;
-            double nrm = 1.0 / (M * sz * sz);
-            double ixx = q[3] - q[1] * cx, ixy = q[4] - q[1] * cy, iyy = q[5] - q[2] * cy;
-            d.rec2[c] = make_float4(f64_to_f32_rn(ixx * nrm), f64_to_f32_rn(ixy * nrm),
-                                    f64_to_f32_rn(iyy * nrm), 0.f);
-        } else {
-            d.rec[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (second) d.rec2[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-    }
-}
-
 // ------------------------------------------------------------------ launches
 cudaError_t launch_prologue(const DevPlan &d, cudaStream_t st) {
     long long n = d.B_total > d.nsys ? d.B_total : d.nsys;
@@ -1225,14 +1197,10 @@ cudaError_t launch_summarize(const DevPlan &d, bool leaves, cudaStream_t st) {
     else k_summarize<false><<<g, SUM_THREADS, 0, st>>>(d, 0);
     return cudaGetLastError();
 }
-cudaError_t launch_pyramid(const DevPlan &d, cudaStream_t st) {
+cudaError_t launch_pyramid(const DevPlan &d, cudaStream_t st, bool second) {
     const unsigned g = grid_for(d.T_total, 1, d.nsm * 8LL);
-    if (d.learned) k_summarize<true><<<g, SUM_THREADS, 0, st>>>(d, 1);
+    if (d.learned || second) k_summarize<true><<<g, SUM_THREADS, 0, st>>>(d, 1);
     else k_summarize<false><<<g, SUM_THREADS, 0, st>>>(d, 1);
-    return cudaGetLastError();
-}
-cudaError_t launch_records(const DevPlan &d, bool second, cudaStream_t st) {
-    k_records<<<grid_for(d.C_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d, second ? 1 : 0);
     return cudaGetLastError();
 }
 
