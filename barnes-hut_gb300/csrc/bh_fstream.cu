@@ -33,7 +33,6 @@ namespace bh {
 
 constexpr int NR = FORCE_R;
 constexpr int FW = 4;       // warps per CTA
-constexpr int WFAR = 128;   // far entries per staging pass (per warp)
 constexpr int WDESC = 64;   // near descriptors per batch (per warp)
 constexpr int NRUN = MAX_TG * MAX_TG;                // target runs (boxes) of a work item
 
@@ -41,12 +40,16 @@ constexpr int NRUN = MAX_TG * MAX_TG;                // target runs (boxes) of a
 // item ends before its near phase starts, and the slice reduction follows both, so the far staging
 // and the reduction buffer share the two near-source buffers.  WSRC near sources per bulk-copy
 // pass: the largest pass that keeps MINB CTAs of FW warps within the SM's shared memory (the
-// 8-CTA build, which spills, also leaves L1 room for its spills): 88 at 8 CTAs, 120 at 6.
+// 8-CTA build, which spills, also leaves L1 room for its spills): 88 at 8 CTAs, 120 at 6.  WFAR
+// far entries per pass: two raw 16-byte buffers (bulk copies of the group's far list, the next
+// pass in flight while this one is swept) and the widened staging fit in the same space.
 template <int MINB>
 struct FsLayout {
     static constexpr int WSRC = MINB >= 8 ? 88 : 120;
+    static constexpr int WFAR = MINB >= 8 ? 96 : 128;
     static constexpr int W_SRC = 0;                             // 2 x WSRC x 32 bytes
-    static constexpr int W_FARXY = 0;                           // WFAR x float4 (x, x, y, y)
+    static constexpr int W_FRAW = 0;                            // 2 x WFAR x float4 (x, y, M, 0)
+    static constexpr int W_FARXY = W_FRAW + 2 * WFAR * 16;      // WFAR x float4 (x, x, y, y)
     static constexpr int W_FARM = W_FARXY + WFAR * 16;          // WFAR x float2 (M, M)
     static constexpr int W_NBOX = W_SRC + 2 * WSRC * 32;        // (WDESC + 1) x int
     static constexpr int W_NPRE = W_NBOX + (WDESC + 1) * 4;     // (WDESC + 1) x int
@@ -59,20 +62,21 @@ struct FsLayout {
     static_assert(2 * 32 * NR * sizeof(float) <= (size_t)W_NBOX, "slice partials alias the source buffers");
     static_assert((WSRC * 32) % 16 == 0 && W_BYTES % 128 == 0, "bulk-copy destinations must be 16-byte aligned");
     static_assert(MINB * (SMEM + 1024) <= 228 * 1024, "MINB CTAs must fit in the SM's shared memory");
+    static_assert(WFAR % 32 == 0, "far staging passes are whole lane rounds");
 };
 static_assert(32 * NR >= STREAM_CHUNK, "a warp must cover every target of a work item");
-static_assert(WFAR % 32 == 0, "far staging passes are whole lane rounds");
 
 template <bool KAHAN, int MINB>
 __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, int accumulate) {
     extern __shared__ __align__(128) unsigned char smem[];
     using Ly = FsLayout<MINB>;
-    constexpr int WSRC = Ly::WSRC;
+    constexpr int WSRC = Ly::WSRC, WFAR = Ly::WFAR;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned char *ws = smem + warp * Ly::W_BYTES;
     float4 *farxy = reinterpret_cast<float4 *>(ws + Ly::W_FARXY);
     float2 *farm = reinterpret_cast<float2 *>(ws + Ly::W_FARM);
     unsigned char *srcb = ws + Ly::W_SRC;
+    unsigned char *fraw = ws + Ly::W_FRAW;
     int *nbox = reinterpret_cast<int *>(ws + Ly::W_NBOX);
     int *npre = reinterpret_cast<int *>(ws + Ly::W_NPRE);
     int *rstart = reinterpret_cast<int *>(ws + Ly::W_RUN);  // first particle of target run r
@@ -94,11 +98,16 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
     }
     __syncwarp();
 
+    // lane 0 takes the queue slot of its next item one item ahead (the atomic's latency hides
+    // behind the current item)
+    int qnext = 0;
+    if (lane == 0) qnext = (int)atomicAdd(&d.glob->item_next, 1u);
     for (;;) {
         int item = 0;
         if (lane == 0) {
-            const int q = (int)atomicAdd(&d.glob->item_next, 1u);
+            const int q = qnext;
             item = q < nitems ? d.item_order[q] : q;  // heaviest items first
+            if (q < nitems) qnext = (int)atomicAdd(&d.glob->item_next, 1u);
         }
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= nitems) break;
@@ -118,6 +127,22 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         // a box outside the item's set is an empty run; a quadrant item's box run is the quadrant)
         const int nrun = TG * TG;
         const int qbox = sub >= nrun ? (sub - nrun) >> 2 : -1, quad = sub >= nrun ? (sub - nrun) & 3 : 0;
+        const int2 cnt = d.lcnt[g];
+        const float4 *lf = d.lfar + sd.lfoff + lg * sd.lfcap;
+        const int nfp = (cnt.x + WFAR - 1) / WFAR;  // far passes
+        // far pass p: one bulk copy of the list's entries into raw buffer p & 1 (the buffer's
+        // previous contents, if any, were widened before; lane 0 announces the bytes and copies)
+        auto issue_far = [&](int p) {
+            const int f0 = p * WFAR, nf = min(WFAR, cnt.x - f0);
+            __syncwarp();
+            tc::fence_async_smem();
+            if (lane == 0) {
+                tc::mbar_expect_tx(&mbar[p & 1], (uint32_t)nf * 16u);
+                tc::bulk_g2s(fraw + (p & 1) * (WFAR * 16), lf + f0, (uint32_t)nf * 16u, &mbar[p & 1]);
+            }
+        };
+        if (tma_ok && nfp > 0) issue_far(0);
+        if (tma_ok && nfp > 1) issue_far(1);
         {
             int carry = 0;
             for (int b0 = 0; b0 < nrun; b0 += 32) {
@@ -202,12 +227,11 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
             nax2[k] = nay2[k] = f2_pack(0.f, 0.f);
             fsx2[k] = fsy2[k] = fcx2[k] = fcy2[k] = f2_pack(0.f, 0.f);
         }
-        const int2 cnt = d.lcnt[g];
-        const float4 *lf = d.lfar + sd.lfoff + lg * sd.lfcap;
         const int4 *ln = d.lnear + sd.lnoff + lg * 2 * (sd.lncap + 1);
 
-        // sweep nf staged far entries; the pass's plain FP32 sum enters the running total through
-        // a Kahan-compensated addition when compensate (and the compensations are live) is set
+        // sweep nf staged far entries; the pass's plain FP32 sum enters the far total through a
+        // Kahan-compensated addition (compensate: the group's far list), or the near accumulators
+        // by a plain one (the far entries a dense item's own opening test accepts)
         auto far_sweep = [&](int nf, bool compensate) {
             if (active) {
                 const ulonglong2 *fp = reinterpret_cast<const ulonglong2 *>(farxy);
@@ -236,9 +260,12 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                         const f2_t yy = f2_fma(fcy2[kk], m1x2, py2[kk]), t2 = f2_add(fsy2[kk], yy);
                         fcy2[kk] = f2_fma(yy, m1x2, f2_fma(fsy2[kk], m1x2, t2));
                         fsy2[kk] = t2;
-                    } else {
+                    } else if (compensate) {
                         fsx2[kk] = f2_add(fsx2[kk], px2[kk]);
                         fsy2[kk] = f2_add(fsy2[kk], py2[kk]);
+                    } else {
+                        nax2[kk] = f2_add(nax2[kk], px2[kk]);
+                        nay2[kk] = f2_add(nay2[kk], py2[kk]);
                     }
                 }
             }
@@ -246,28 +273,42 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
             __syncwarp();  // the staging is rewritten next
         };
 
-        // ---- far field: the group's accepted cells
-        for (int f0 = 0; f0 < cnt.x; f0 += WFAR) {
-            const int nf = min(WFAR, cnt.x - f0);
-            // the entries (centre of mass in the group frame, mass) widen into the packed staging
+        // ---- far field: the group's accepted cells, pass by pass from the raw buffers (the
+        // entries, centre of mass in the group frame and mass, widen into the packed staging)
+        for (int p = 0; p < nfp && tma_ok; p++) {
+            const int nf = min(WFAR, cnt.x - p * WFAR);
+            const int buf = p & 1;
+            const bool ok = tc::mbar_wait(&mbar[buf], (phases >> buf) & 1u);
+            phases ^= 1u << buf;
+            if (!__all_sync(0xffffffffu, ok)) {
+                // flagged; give the copies in flight a second bounded wait, then stage nothing
+                // more in this launch (the barrier phases are no longer known)
+                if (lane == 0) raise_err(d.glob, 8u /*BH_DEV_WAIT_TIMEOUT*/);
+                tc::mbar_wait(&mbar[buf], ((phases >> buf) & 1u) ^ 1u);
+                if (p + 1 < nfp) tc::mbar_wait(&mbar[buf ^ 1], (phases >> (buf ^ 1)) & 1u);
+                tma_ok = false;
+                break;
+            }
+            const float4 *raw = reinterpret_cast<const float4 *>(fraw + buf * (WFAR * 16));
 #pragma unroll
             for (int u = 0; u < WFAR / 32; u++) {
                 const int k = lane + 32 * u;
                 if (k < nf) {
-                    const float4 e = lf[f0 + k];
+                    const float4 e = raw[k];
                     farxy[k] = make_float4(e.x, e.x, e.y, e.y);
                     farm[k] = make_float2(e.z, e.z);
                 }
             }
-            __syncwarp();
+            if (p + 2 < nfp) issue_far(p + 2);  // (its syncwarp also publishes the staging)
+            else __syncwarp();
             far_sweep(nf, true);
         }
-        // compensated far sums s - c; the compensations are dead from here on
+        // the compensated far sums s - c start the near accumulators; the far sums and their
+        // compensations are dead from here on
 #pragma unroll
         for (int kk = 0; kk < NR / 2; kk++) {
-            fsx2[kk] = f2_fma(fcx2[kk], m1x2, fsx2[kk]);
-            fsy2[kk] = f2_fma(fcy2[kk], m1x2, fsy2[kk]);
-            fcx2[kk] = fcy2[kk] = f2_pack(0.f, 0.f);
+            nax2[kk] = f2_fma(fcx2[kk], m1x2, fsx2[kk]);
+            nay2[kk] = f2_fma(fcy2[kk], m1x2, fsy2[kk]);
         }
 
         // ---- near field: descriptors in batches of WDESC; sources in double-buffered passes.
@@ -454,16 +495,14 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         if (active) {
 #pragma unroll
             for (int k = 0; k < NR / 2; k++) {
-                float a0, a1, b0, b1, s0, s1, t0, t1;
+                float a0, a1, b0, b1;
                 f2_unpack(nax2[k], a0, a1);
                 f2_unpack(nay2[k], b0, b1);
-                f2_unpack(fsx2[k], s0, s1);
-                f2_unpack(fsy2[k], t0, t1);
                 float *o = red + 2 * ((slice * nthr + tl) * NR + 2 * k);
-                o[0] = a0 + s0;
-                o[1] = b0 + t0;
-                o[2] = a1 + s1;
-                o[3] = b1 + t1;
+                o[0] = a0;
+                o[1] = b0;
+                o[2] = a1;
+                o[3] = b1;
             }
         }
         __syncwarp();

@@ -1022,14 +1022,18 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int lea
         if (!leaves_given) {
             // a box inside one chunk has its moments from the chunk's sums; a box over several
             // chunks adds its partials in chunk order (the first chunk's tail, whole middle
-            // chunks, the last chunk's head) and writes the sum to mom
+            // chunks, the last chunk's head) and writes the sum to mom, as an empty box its zeros
             for (int k = tid; k < SUM_TILE * SUM_TILE; k += SUM_THREADS) {
                 const int cx = k / SUM_TILE, cy = k - cx * SUM_TILE;
                 if (cx >= nbx || cy >= nby) continue;
                 const long long lb = (long long)(bx0 + cx) * G + (by0 + cy);
                 const int i0 = d.box_start[sd.boff + lb], i1 = d.box_start[sd.boff + lb + 1];
-                if (i1 == i0) continue;  // empty: zeros
                 double *mb = d.mom + 6 * (sd.coff + lb);
+                if (i1 == i0) {  // empty: zeros
+#pragma unroll
+                    for (int q = 0; q < 6; q++) mb[q] = 0.0;
+                    continue;
+                }
                 const long long c0 = i0 >> 5, c1 = (long long)(i1 - 1) >> 5;
                 if (c0 == c1) {
 #pragma unroll
