@@ -342,7 +342,8 @@ class Plan:
 
     def leaf_moments(self, sys=0):
         """(G, G, 6) device tensor: the last summarize's leaf moments (M, Sx, Sy, Sxx, Sxy, Syy
-        about each box origin)."""
+        about each box origin; the second moments only with the learned correction, zeros
+        otherwise)."""
         torch = self._torch
         G = self.grid_info(sys)["grid_dim"]
         out = torch.empty((G, G, 6), dtype=torch.float64, device=self.device)

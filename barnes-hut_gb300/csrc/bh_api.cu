@@ -44,6 +44,8 @@ struct bh_plan {
     DevPlan dev;
     bool has_tree = false;
     bool acc_stale = true;  // next bh_evaluate overwrites instead of accumulating
+    bool acc_valid = false;  // AX/AY hold accelerations (else they are zero by definition: a load
+                             // or a generation does not write them)
     bool leaves_stale = false;  // leaf moments overwritten since the last create_tree
     // graph cache
     cudaGraphExec_t gexec = nullptr;
@@ -439,6 +441,7 @@ extern "C" int bh_bind(bh_plan *p, void *workspace, size_t bytes, void *stream) 
     CK(p, cudaStreamSynchronize(st), "bind sync");
     p->has_tree = false;
     p->acc_stale = true;
+    p->acc_valid = false;
     if (p->gexec) {
         cudaGraphExecDestroy(p->gexec);
         p->gexec = nullptr;
@@ -461,6 +464,7 @@ extern "C" int bh_load(bh_plan *p, const double *x, const double *y, const doubl
     CK(p, launch_load(p->dev, x, y, m, vx, vy, 0, (cudaStream_t)stream), "load");
     p->has_tree = false;
     p->acc_stale = true;
+    p->acc_valid = false;
     return BH_OK;
 }
 
@@ -471,6 +475,7 @@ extern "C" int bh_load_records(bh_plan *p, const double *rec, void *stream) {
     CK(p, launch_load(p->dev, rec + 0, rec + 1, rec + 2, rec + 3, rec + 4, 10, (cudaStream_t)stream), "load records");
     p->has_tree = false;
     p->acc_stale = true;
+    p->acc_valid = false;
     return BH_OK;
 }
 
@@ -478,7 +483,7 @@ extern "C" int bh_store_records(bh_plan *p, double *rec, void *stream) {
     int r = need_bound(p);
     if (r) return r;
     if (p->n_total && !rec) return fail(p, BH_ERR_INVALID, "null records");
-    CK(p, launch_store(p->dev, p->has_tree ? 1 : 0, rec, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+    CK(p, launch_store(p->dev, p->has_tree ? 1 : 0, p->acc_valid, rec, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
                        (cudaStream_t)stream), "store records");
     return BH_OK;
 }
@@ -487,7 +492,8 @@ extern "C" int bh_store(bh_plan *p, double *x, double *y, double *vx, double *vy
                         double *ay, void *stream) {
     int r = need_bound(p);
     if (r) return r;
-    CK(p, launch_store(p->dev, p->has_tree ? 1 : 0, nullptr, x, y, vx, vy, ax, ay, (cudaStream_t)stream), "store");
+    CK(p, launch_store(p->dev, p->has_tree ? 1 : 0, p->acc_valid, nullptr, x, y, vx, vy, ax, ay, (cudaStream_t)stream),
+       "store");
     return BH_OK;
 }
 
@@ -533,14 +539,21 @@ extern "C" int bh_evaluate(bh_plan *p, void *stream) {
         CK(p, launch_learned_correct(p->dev, p->params.correction_theta, p->mlp_img, p->mlp_params,
                                      false, (cudaStream_t)stream), "learned correction");
     p->acc_stale = false;
+    p->acc_valid = true;
     return BH_OK;
 }
 
 extern "C" int bh_timestep(bh_plan *p, void *stream) {
     int r = need_bound(p);
     if (r) return r;
+    if (!p->acc_valid) {  // no evaluation since the load: the tick sees zero accelerations
+        const size_t nb = 8 * (size_t)p->n_total;
+        CK(p, cudaMemsetAsync(p->dev.AX, 0, nb, (cudaStream_t)stream), "zero accelerations");
+        CK(p, cudaMemsetAsync(p->dev.AY, 0, nb, (cudaStream_t)stream), "zero accelerations");
+    }
     CK(p, launch_tick(p->dev, (cudaStream_t)stream), "timestep");
     p->acc_stale = true;
+    p->acc_valid = true;  // (zeroed by the tick)
     return BH_OK;
 }
 
@@ -570,6 +583,7 @@ extern "C" int bh_step(bh_plan *p, int nsteps, void *stream) {
     if (nsteps > 0) {
         p->has_tree = true;
         p->acc_stale = true;
+        p->acc_valid = true;
     }
     return BH_OK;
 }
@@ -617,6 +631,7 @@ extern "C" int bh_step_graph(bh_plan *p, int nsteps, void *stream) {
     CK(p, cudaGraphLaunch(p->gexec, st), "graph launch");
     p->has_tree = true;
     p->acc_stale = true;
+    p->acc_valid = true;
     return BH_OK;
 }
 

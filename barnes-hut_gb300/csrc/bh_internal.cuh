@@ -366,7 +366,8 @@ cudaError_t launch_walk_items(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st);
 cudaError_t launch_summarize(const DevPlan &d, bool leaves, cudaStream_t st);
 // the pyramid levels above the leaves and the cell records, from the leaf moments
-// second: also the pyramid's second moments and their records (always with the learned correction)
+// second: also the second moments and their records (always with the learned correction; a plan
+// without it sums its leaves again from the particles for them)
 cudaError_t launch_pyramid(const DevPlan &d, cudaStream_t st, bool second = false);
 // ev (optional): two events recorded on st right before and after the force kernel proper
 cudaError_t launch_force(const DevPlan &d, bool tick, bool accumulate, cudaStream_t st,
@@ -380,7 +381,7 @@ cudaError_t launch_tick(const DevPlan &d, cudaStream_t st, bool keep_acc = false
 cudaError_t launch_load(const DevPlan &d, const double *x, const double *y, const double *m,
                         const double *vx, const double *vy, long long rec_stride,
                         cudaStream_t st);
-cudaError_t launch_store(const DevPlan &d, int has_tree, double *rec, double *x, double *y, double *vx,
+cudaError_t launch_store(const DevPlan &d, int has_tree, bool has_acc, double *rec, double *x, double *y, double *vx,
                          double *vy, double *ax, double *ay, cudaStream_t st);
 cudaError_t launch_direct(const DevPlan &d, int sys, const long long *targets, long long nt,
                           double *ax, double *ay, cudaStream_t st);

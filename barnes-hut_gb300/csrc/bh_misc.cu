@@ -15,6 +15,8 @@ static inline unsigned grid_of(long long n, int tpb, int nsm) {
 // Upload: state buffer (epoch + 1) & 1 receives the particles in the given
 // order; pid = concatenated index.  rec_stride = 0: SoA arrays; 10: the
 // reference's N x 10 record (internals/particle.py:3-15), x points at row 0.
+// The accelerations are not written: until the next evaluation they read as
+// zero (the host tracks it; k_store then writes zeros).
 __global__ void k_load(DevPlan d, const double *x, const double *y, const double *m,
                        const double *vx, const double *vy, long long rs) {
     const int b = (d.glob->epoch + 1) & 1;
@@ -27,22 +29,21 @@ __global__ void k_load(DevPlan d, const double *x, const double *y, const double
         d.VX[b][i] = vx[k];
         d.VY[b][i] = vy[k];
         d.PID[b][i] = (int)i;
-        d.AX[i] = 0.f;
-        d.AY[i] = 0.f;
     }
 }
 
 // Download in pid order.  rec: N x 10 records (px, py, mass, vx, vy, ax, ay,
 // gx, gy, pid) or NULL; SoA outputs may be NULL.  gx/gy come from the box
-// keys of the last create_tree (skey), 0 before the first one.
+// keys of the last create_tree (skey), 0 before the first one; ax/ay are 0
+// when no evaluation followed the last load (has_acc = 0).
 __global__ void k_store(DevPlan d, double *rec, double *x, double *y, double *vx, double *vy,
-                        double *ax, double *ay, int has_tree) {
+                        double *ax, double *ay, int has_tree, int has_acc) {
     const int b = (d.glob->epoch + 1) & 1;
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < d.n_total; i += stride) {
         long long p = d.PID[b][i];
         double px = d.X[b][i], py = d.Y[b][i], pvx = d.VX[b][i], pvy = d.VY[b][i];
-        double pax = (double)d.AX[i], pay = (double)d.AY[i];
+        const double pax = has_acc ? d.AX[i] : 0.0, pay = has_acc ? d.AY[i] : 0.0;
         if (rec) {
             double *r = rec + 10 * p;
             double gx = 0.0, gy = 0.0;
@@ -72,7 +73,7 @@ __global__ void k_tick(DevPlan d, int keep_acc) {
     const int b = (d.glob->epoch + 1) & 1;
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < d.n_total; i += stride) {
-        double ax = (double)d.AX[i], ay = (double)d.AY[i];
+        double ax = d.AX[i], ay = d.AY[i];
         double vx = d.VX[b][i] + ax * d.dt, vy = d.VY[b][i] + ay * d.dt;
         d.VX[b][i] = vx;
         d.VY[b][i] = vy;
@@ -198,10 +199,10 @@ cudaError_t launch_load(const DevPlan &d, const double *x, const double *y, cons
     return cudaGetLastError();
 }
 
-cudaError_t launch_store(const DevPlan &d, int has_tree, double *rec, double *x, double *y,
+cudaError_t launch_store(const DevPlan &d, int has_tree, bool has_acc, double *rec, double *x, double *y,
                          double *vx, double *vy, double *ax, double *ay, cudaStream_t st) {
     if (d.n_total == 0) return cudaSuccess;
-    k_store<<<grid_of(d.n_total, MT, d.nsm), MT, 0, st>>>(d, rec, x, y, vx, vy, ax, ay, has_tree);
+    k_store<<<grid_of(d.n_total, MT, d.nsm), MT, 0, st>>>(d, rec, x, y, vx, vy, ax, ay, has_tree, has_acc ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -776,24 +776,29 @@ __global__ void __launch_bounds__(TPB) k_segsort_big(DevPlan d) {
 // chunk gets its FP64 moments in mom, a box that starts before the chunk leaves its part in the
 // chunk's head partial, one that runs past it in the tail partial (k_summarize adds a multi-chunk
 // box's partials in chunk order).  The products are rounded one by one (no contraction), so the
-// fused pass in k_gather and the stand-alone k_leaf give the same sums.
+// fused pass in k_gather and the stand-alone k_leaf give the same sums.  The second moments
+// (Sxx, Sxy, Syy) are summed only with SECOND (a plan with the learned correction, or training
+// pairs on demand); otherwise they are zeros.
+template <bool SECOND>
 __device__ __forceinline__ void leaf_terms(float ox, float oy, float mf, float v[6]) {
     v[0] = mf;
     v[1] = __fmul_rn(mf, ox);
     v[2] = __fmul_rn(mf, oy);
-    v[3] = __fmul_rn(v[1], ox);
-    v[4] = __fmul_rn(v[1], oy);
-    v[5] = __fmul_rn(v[2], oy);
+    v[3] = SECOND ? __fmul_rn(v[1], ox) : 0.f;
+    v[4] = SECOND ? __fmul_rn(v[1], oy) : 0.f;
+    v[5] = SECOND ? __fmul_rn(v[2], oy) : 0.f;
 }
 
 // key: the lane's box (-1 past the end); c: the chunk (its first particle is 32 c)
+template <bool SECOND>
 __device__ __forceinline__ void leaf_chunk(const DevPlan &d, long long c, int key, float v[6]) {
+    constexpr int NL = SECOND ? 6 : 3;  // moments summed
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const int k2 = __shfl_up_sync(0xffffffffu, key, o);
 #pragma unroll
-        for (int q = 0; q < 6; q++) {
+        for (int q = 0; q < NL; q++) {
             const float y = __shfl_up_sync(0xffffffffu, v[q], o);
             if (lane >= o && k2 == key) v[q] = __fadd_rn(v[q], y);
         }
@@ -809,21 +814,22 @@ __device__ __forceinline__ void leaf_chunk(const DevPlan &d, long long c, int ke
         float *pt = d.leafpart + 12 * c;
         if (head)
 #pragma unroll
-            for (int q = 0; q < 6; q++) pt[q] = v[q];
+            for (int q = 0; q < NL; q++) pt[q] = v[q];
         if (tail)
 #pragma unroll
-            for (int q = 0; q < 6; q++) pt[6 + q] = v[q];
+            for (int q = 0; q < NL; q++) pt[6 + q] = v[q];
     } else {
         const int s = find_seg(d.boff_tab, d.nsys, key);
         double *m = d.mom + 6 * (d.sys[s].coff + (key - d.sys[s].boff));
 #pragma unroll
-        for (int q = 0; q < 6; q++) m[q] = f32_to_f64(v[q]);
+        for (int q = 0; q < 6; q++) m[q] = q < NL ? f32_to_f64(v[q]) : 0.0;
     }
 }
 
 // Output particle t takes input perm[t]; each warp's 32 consecutive outputs form a leaf chunk,
 // whose moments are summed on the spot (the stand-alone k_leaf repeats this from the packed
 // records when the leaf moments were overwritten since).
+template <bool SECOND>
 __global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
     const int cur = d.glob->epoch & 1, nxt = cur ^ 1;
     const int lane = threadIdx.x & 31;
@@ -894,8 +900,8 @@ __global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
             if (wu >= n) break;                    // (warp-uniform)
             const long long t = wu + lane;
             float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            if (t < n) leaf_terms(lx[u], ly[u], lm[u], v);
-            leaf_chunk(d, wu >> 5, t < n ? key4[u] >> 2 : -1, v);
+            if (t < n) leaf_terms<SECOND>(lx[u], ly[u], lm[u], v);
+            leaf_chunk<SECOND>(d, wu >> 5, t < n ? key4[u] >> 2 : -1, v);
         }
     }
 }
@@ -969,6 +975,7 @@ __device__ __forceinline__ void cell_record(const DevPlan &d, long long c, int l
 // box-sorted particles (k_gather does the same while it writes the records; this pass runs when
 // the leaf moments have been overwritten since, bh_set_leaf_moments).  No atomics: fixed
 // summation order.
+template <bool SECOND>
 __global__ void __launch_bounds__(TPB) k_leaf(DevPlan d) {
     const int lane = threadIdx.x & 31;
     const long long nch = (d.n_total + 31) >> 5;
@@ -980,9 +987,9 @@ __global__ void __launch_bounds__(TPB) k_leaf(DevPlan d) {
         if (i < d.n_total) {
             key = d.skey[i];
             const float4 p = d.P[i];
-            leaf_terms(p.x, p.y, p.z, v);
+            leaf_terms<SECOND>(p.x, p.y, p.z, v);
         }
-        leaf_chunk(d, c, key, v);
+        leaf_chunk<SECOND>(d, c, key, v);
     }
 }
 
@@ -1043,12 +1050,12 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int lea
                 float sm_[6], cc_[6];
 #pragma unroll
                 for (int q = 0; q < 6; q++) {
-                    sm_[q] = d.leafpart[12 * c0 + 6 + q];
+                    sm_[q] = q < NM ? d.leafpart[12 * c0 + 6 + q] : 0.f;
                     cc_[q] = 0.f;
                 }
                 for (long long c = c0 + 1; c <= c1; c++)
 #pragma unroll
-                    for (int q = 0; q < 6; q++) kahan_add(sm_[q], cc_[q], d.leafpart[12 * c + q]);
+                    for (int q = 0; q < NM; q++) kahan_add(sm_[q], cc_[q], d.leafpart[12 * c + q]);
 #pragma unroll
                 for (int q = 0; q < 6; q++) {
                     const double v = f32_to_f64(__fsub_rn(sm_[q], cc_[q]));
@@ -1188,13 +1195,17 @@ cudaError_t launch_scatter(const DevPlan &d, cudaStream_t st) {
     k_perm<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     k_segsort<<<grid_for(4 * d.B_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     k_segsort_big<<<(unsigned)(d.nsm * 4), TPB, 0, st>>>(d);
-    k_gather<<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
+    if (d.learned) k_gather<true><<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
+    else k_gather<false><<<grid_for(d.n_total, TPB, d.nsm * 8LL), TPB, 0, st>>>(d);
     return cudaGetLastError();
 }
 // leaves: the leaf sums of k_gather were overwritten since (bh_set_leaf_moments): redo them
 cudaError_t launch_summarize(const DevPlan &d, bool leaves, cudaStream_t st) {
-    if (leaves && d.n_total > 0)
-        k_leaf<<<grid_for((d.n_total + 31) / 32, TPB / 32, d.nsm * 8LL), TPB, 0, st>>>(d);
+    if (leaves && d.n_total > 0) {
+        const unsigned g = grid_for((d.n_total + 31) / 32, TPB / 32, d.nsm * 8LL);
+        if (d.learned) k_leaf<true><<<g, TPB, 0, st>>>(d);
+        else k_leaf<false><<<g, TPB, 0, st>>>(d);
+    }
     // the second moments of the pyramid cells feed only the learned correction
     const unsigned g = grid_for(d.T_total, 1, d.nsm * 8LL);
     if (d.learned) k_summarize<true><<<g, SUM_THREADS, 0, st>>>(d, 0);
@@ -1203,8 +1214,16 @@ cudaError_t launch_summarize(const DevPlan &d, bool leaves, cudaStream_t st) {
 }
 cudaError_t launch_pyramid(const DevPlan &d, cudaStream_t st, bool second) {
     const unsigned g = grid_for(d.T_total, 1, d.nsm * 8LL);
-    if (d.learned || second) k_summarize<true><<<g, SUM_THREADS, 0, st>>>(d, 1);
-    else k_summarize<false><<<g, SUM_THREADS, 0, st>>>(d, 1);
+    if (second && !d.learned) {
+        // a plan without the learned correction sums no second moments: the leaves again from
+        // the particles with them, then the pyramid
+        if (d.n_total > 0) k_leaf<true><<<grid_for((d.n_total + 31) / 32, TPB / 32, d.nsm * 8LL), TPB, 0, st>>>(d);
+        k_summarize<true><<<g, SUM_THREADS, 0, st>>>(d, 0);
+    } else if (d.learned) {
+        k_summarize<true><<<g, SUM_THREADS, 0, st>>>(d, 1);
+    } else {
+        k_summarize<false><<<g, SUM_THREADS, 0, st>>>(d, 1);
+    }
     return cudaGetLastError();
 }
 

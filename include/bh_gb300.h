@@ -204,7 +204,8 @@ int bh_box_moments(bh_plan *plan, int sys, double *out, void *stream);
  * whole system (host doubles; the all-reduce of the ranks' extents) instead of from the
  * plan's own particles; ext = NULL returns to the plan's own box.  bh_leaf_moments copies the
  * last summarize's leaf moments of `sys` -- per box, x-major, (M, Sx, Sy, Sxx, Sxy, Syy) about
- * the box origin, FP64 -- into out (device, G*G*6 doubles); bh_set_leaf_moments replaces them
+ * the box origin, FP64; the second moments only for a plan with BH_FLAG_LEARNED, zeros
+ * otherwise -- into out (device, G*G*6 doubles); bh_set_leaf_moments replaces them
  * with `in` (device, same layout: the sum over ranks of their own boxes' moments) and rebuilds
  * the pyramid levels above the leaves and the cell records, so the next bh_evaluate takes its
  * far field from the whole system (multigpu.py:149-155, 303-306). */

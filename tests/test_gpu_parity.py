@@ -402,6 +402,28 @@ def test_long_quadrants_sorted():
                           ref["ax"], ref["ay"]) <= 1e-5
 
 
+def test_accelerations_zero_until_evaluated():
+    """A load writes no accelerations: until an evaluation they read as zero (store), and a tick
+    right after the load moves the particles by their velocities alone (gpu/grid.py:159-174 with
+    a = 0), also after an earlier step left accelerations in the plan."""
+    from barneshut.gb300 import workloads
+
+    x, y, m, vx, vy = workloads.uniform(2000, seed=72)
+    plan = make_plan(2000, 8, **REF_KW)
+    plan.load(x, y, m, vx, vy)
+    plan.step(1)  # leaves non-zero accelerations behind
+    plan.load(x, y, m, vx, vy)
+    o = plan.store()
+    assert not o["ax"].any() and not o["ay"].any()
+    plan.timestep()
+    o = plan.store()
+    dt = REF_KW["tick_seconds"]
+    # (the device may fuse x + v dt into one rounding)
+    np.testing.assert_allclose(o["x"].cpu().numpy(), x + vx * dt, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(o["y"].cpu().numpy(), y + vy * dt, rtol=0, atol=1e-15)
+    assert not o["ax"].any()
+
+
 def test_summarize_after_set_leaf_moments():
     """The leaf sums come with the scatter (k_gather); after bh_set_leaf_moments overwrote them,
     bh_summarize sums the leaves from the particles again (the stand-alone leaf pass): the leaf
