@@ -26,8 +26,9 @@ namespace bh {
 
 constexpr int LW = 4;  // warps per list-building CTA; one warp walks one group
 constexpr int LU = 4;  // frontier cells per lane per round (their records are loaded together)
+constexpr int LISTS_MINB = 8;  // CTAs per SM (registers: 64 per thread)
 
-__global__ void __launch_bounds__(LW * 32) k_lists(DevPlan d) {
+__global__ void __launch_bounds__(LW * 32, LISTS_MINB) k_lists(DevPlan d) {
     __shared__ int front[LW][2][FR_CAP];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int(*fb)[FR_CAP] = front[warp];
@@ -163,33 +164,48 @@ __global__ void __launch_bounds__(LW * 32) k_lists(DevPlan d) {
                 }
         }
         int base = 0;
-        for (int k0 = 0; k0 <= nn; k0 += 32) {
-            const int k = k0 + lane;
-            int st = 0, c = 0, loc = 0;
-            if (k < nn) {
-                loc = nl[k];
-                st = d.box_start[sd.boff + loc];
-                c = d.box_start[sd.boff + loc + 1] - st;
-            }
-            int inc = c;
+        // LU rounds of 32 boxes at a time: their particle ranges and records are loaded together
+        for (int k0 = 0; k0 <= nn; k0 += 32 * LU) {
+            int loc[LU], st[LU], c[LU];
+            float4 rr[LU];
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= o) inc += y;
+            for (int u = 0; u < LU; u++) {
+                const int k = k0 + 32 * u + lane;
+                loc[u] = k < nn ? nl[k] : 0;
             }
-            const int pre = base + inc - c;
-            if (k < nn) {
-                const int kx = loc / sd.G, ky = loc - kx * sd.G;
-                const float shx = __fmul_rn((float)(kx - gx0), step_f), shy = __fmul_rn((float)(ky - gy0), step_f);
-                const float4 rr = d.rec[sd.coff + loc];  // the leaf's record (level 0)
-                near_out[2 * k] = make_int4(st, pre, __float_as_int(shx), __float_as_int(shy));
-                near_out[2 * k + 1] = make_int4(loc, __float_as_int(rr.z), __float_as_int(__fadd_rn(shx, rr.x)),
-                                                __float_as_int(__fadd_rn(shy, rr.y)));
-            } else if (k == nn) {
-                near_out[2 * k] = make_int4(0, pre, 0, 0);
-                near_out[2 * k + 1] = make_int4(0, 0, 0, 0);
+#pragma unroll
+            for (int u = 0; u < LU; u++) {
+                const int k = k0 + 32 * u + lane;
+                st[u] = c[u] = 0;
+                rr[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (k < nn) {
+                    st[u] = d.box_start[sd.boff + loc[u]];
+                    c[u] = d.box_start[sd.boff + loc[u] + 1] - st[u];
+                    rr[u] = d.rec[sd.coff + loc[u]];  // the leaf's record (level 0)
+                }
             }
-            base += __shfl_sync(0xffffffffu, inc, 31);
+#pragma unroll
+            for (int u = 0; u < LU; u++) {
+                const int k = k0 + 32 * u + lane;
+                int inc = c[u];
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += y;
+                }
+                const int pre = base + inc - c[u];
+                if (k < nn) {
+                    const int kx = loc[u] / sd.G, ky = loc[u] - kx * sd.G;
+                    const float shx = __fmul_rn((float)(kx - gx0), step_f), shy = __fmul_rn((float)(ky - gy0), step_f);
+                    near_out[2 * k] = make_int4(st[u], pre, __float_as_int(shx), __float_as_int(shy));
+                    near_out[2 * k + 1] = make_int4(loc[u], __float_as_int(rr[u].z), __float_as_int(__fadd_rn(shx, rr[u].x)),
+                                                    __float_as_int(__fadd_rn(shy, rr[u].y)));
+                } else if (k == nn) {
+                    near_out[2 * k] = make_int4(0, pre, 0, 0);
+                    near_out[2 * k + 1] = make_int4(0, 0, 0, 0);
+                }
+                base += __shfl_sync(0xffffffffu, inc, 31);
+            }
         }
         if (lane == 0) {
             if (ovf || nfar > sd.lfcap || nnear > sd.lncap) raise_err(d.glob, 2u /*BH_DEV_LIST_OVERFLOW*/);
@@ -284,7 +300,7 @@ __global__ void __launch_bounds__(256) k_item_order(DevPlan d) {
 
 cudaError_t launch_lists(const DevPlan &d, cudaStream_t st) {
     if (d.NG_total == 0) return cudaSuccess;
-    long long grid = (long long)d.nsm * 8;  // 64 registers x 128 threads: 8 CTAs per SM
+    long long grid = (long long)d.nsm * LISTS_MINB;
     if (grid * LW > d.NG_total) grid = (d.NG_total + LW - 1) / LW;
     k_lists<<<(unsigned)grid, LW * 32, 0, st>>>(d);
     cudaError_t e = cudaGetLastError();
