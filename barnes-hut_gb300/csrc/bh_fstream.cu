@@ -16,8 +16,8 @@
 //     addition (BH_PREC_FP32_KAHAN) or a plain one (BH_PREC_FP32);
 //   * near field: the near boxes' 32-byte packed records (x, x, y, y), (m, m, index, box) are
 //     copied piece by piece (a piece: a run of listed boxes whose particles are contiguous, as
-//     the boxes of one column of the near region are) into the warp's staging by bulk
-//     asynchronous copies (TMA),
+//     neighbouring boxes of one column are) into the warp's staging by bulk asynchronous copies
+//     (TMA),
 //     WSRC sources per pass, double-buffered on two mbarriers so the copy of pass p + 1 overlaps
 //     the sweep of pass p; the lanes shift each staged source from its box frame into the group
 //     frame in place before the sweep, the shift following from the box coordinates that the
@@ -390,8 +390,8 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                 if (nacc > 0) far_sweep(nacc, false);  // (also orders the staging for the copies)
                 nn = nkeep;
             }
-            // boxes listed one after another whose particles are contiguous (a column of the
-            // near region: the lists are in box order) become one piece, copied at once
+            // boxes listed one after another whose particles are contiguous (neighbours in one
+            // column of the near region) become one piece, copied at once
             {
                 int bx[WDESC / 32], px[WDESC / 32];
                 bool head[WDESC / 32];

@@ -15,8 +15,8 @@
 // Output per group g of system s: far entries (the accepted cell's centre of mass in the group
 // frame, as the opening test computed it, and its mass) at lfar[s.lfoff + lg * s.lfcap ..]; near descriptors -- (first particle, exclusive prefix of the
 // boxes' particle counts, box-origin shift in the group frame) and (box index, mass, centre of
-// mass in the group frame) -- at lnear[s.lnoff + lg * 2 * (s.lncap + 1) ..] in box order, with
-// the total in descriptor [count]; lcnt[g] = (far count, near count).  The slots are
+// mass in the group frame) -- at lnear[s.lnoff + lg * 2 * (s.lncap + 1) ..] with the total in
+// descriptor [count]; lcnt[g] = (far count, near count).  The slots are
 // sized on the host so that a level's accepted cells never exceed FRONTIER_CAP; the kernel still
 // checks and raises BH_DEV_LIST_OVERFLOW.
 #include "bh_internal.cuh"
@@ -136,33 +136,11 @@ __global__ void __launch_bounds__(LW * 32, LISTS_MINB) k_lists(DevPlan d) {
             nfr = ovf ? 0 : nnext;
         }
         // near descriptors: first particle, exclusive prefix of the particle counts, box shift.
-        // The near boxes were appended at the leaf level into the buffer that is now fb[cur];
-        // they are listed in box order (a warp bitonic sort, padded to a power of two), so boxes
-        // of one column that follow each other in the list are contiguous in particle order and
-        // the force kernel copies such a run of boxes at once.
+        // The near boxes were appended at the leaf level into the buffer that is now fb[cur]
+        // (children in (0, 0), (0, 1), (1, 0), (1, 1) order, so a pair of boxes of one column
+        // often follows each other: the force kernel copies such a run at once).
         const int nn = min(nnear, sd.lncap);
-        int *nl = fb[cur];
-        {
-            int m = 2;
-            while (m < nn) m <<= 1;  // <= FR_CAP: nn <= lncap <= FR_CAP
-            for (int k = nn + lane; k < m; k += 32) nl[k] = INT_MAX;
-            __syncwarp();
-            for (int size = 2; size <= m; size <<= 1)
-                for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                    for (int k = lane; k < m; k += 32) {
-                        const int j = k ^ stride;
-                        if (j > k) {
-                            const bool up = (k & size) == 0;
-                            const int x = nl[k], y = nl[j];
-                            if ((x > y) == up) {
-                                nl[k] = y;
-                                nl[j] = x;
-                            }
-                        }
-                    }
-                    __syncwarp();
-                }
-        }
+        const int *nl = fb[cur];
         int base = 0;
         // LU rounds of 32 boxes at a time: their particle ranges and records are loaded together
         for (int k0 = 0; k0 <= nn; k0 += 32 * LU) {
