@@ -33,7 +33,7 @@ struct bh_plan {
     size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_toff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
     size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_bstart, o_sst, o_leafpart, o_perm, o_bigseg, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
-        o_rec2, o_org, o_lfar, o_lnear, o_lcnt, o_iord, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk, o_qcnt;
+        o_rec2, o_org, o_lfar, o_lnear, o_lcnt, o_iord, o_icost, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk, o_qcnt;
     bool stream = false;  // theta-mode interaction lists built once per group and streamed
     int chunk = TARGET_CHUNK;
     int dense_min = BH_STREAM_DENSE_MIN;
@@ -289,6 +289,7 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
                                           (p->quad_min > 0 ? 4 * (N / p->quad_min) : 0) + N / STREAM_ITEM_DIV + 1
                                     : 0;
     p->o_iord = take(4 * sitems);
+    p->o_icost = take(sitems);
     p->o_sicnt = take(p->stream ? 4 * (size_t)p->NG_total : 0);
     p->o_sioff = take(p->stream ? 4 * ((size_t)p->NG_total + 1) : 0);
     p->o_sigrp = take(4 * sitems);
@@ -390,6 +391,7 @@ static void fill_dev(bh_plan *p) {
     d.dense_min = p->dense_min;
     d.quad_min = p->quad_min;
     d.item_bucket = (int *)(w + p->o_ibkt);
+    d.item_cost = (unsigned char *)(w + p->o_icost);
     d.nsm = p->nsm;
     d.stream = p->stream ? 1 : 0;
     d.chunk = p->chunk;

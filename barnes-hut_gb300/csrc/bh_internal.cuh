@@ -41,7 +41,7 @@ constexpr int FORCE_R = 4;                                   // targets per thre
 constexpr int TARGET_CHUNK = FORCE_THREADS * FORCE_R;        // targets per work item
 constexpr int FRONTIER_CAP = 512;                            // traversal frontier per level
 constexpr int SCAN_TILE = 4096;   // counts per tile of the single-pass scans (256 threads x 16)
-constexpr int SITEM_TILE = 256;   // target groups per tile of the streaming work-item kernel
+constexpr int SITEM_TILE = 64;    // target groups per tile of the streaming work-item kernel
 constexpr int SUM_TILE = 16;      // leaf boxes per side of a summarize tile (pyramid levels 0..4)
 constexpr int STREAM_CHUNK = 128;  // targets per work item of the list-streaming force kernel
 constexpr int LIST_MAX_G = 16384;  // largest G of the list-streaming path (32-bit group indices)
@@ -148,6 +148,7 @@ struct DevPlan {
                    // work items and near lists (0: none)
     int *item_order;  // list-streaming work items, heaviest cost bucket first
     int *item_bucket;  // ITEM_BUCKETS counts + ITEM_BUCKETS cursors
+    unsigned char *item_cost;  // per list-streaming work item, its cost bucket (k_item_hist)
     int nsm;     // streaming multiprocessors of the plan's device (queried at bh_bind): sizes the
                  // persistent and grid-stride launches
     int stream;  // 1: lists are built by k_lists and streamed by k_fstream

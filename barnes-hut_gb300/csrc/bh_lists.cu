@@ -238,8 +238,11 @@ __global__ void __launch_bounds__(256) k_item_hist(DevPlan d) {
     if (threadIdx.x < ITEM_BUCKETS) h[threadIdx.x] = 0;
     __syncthreads();
     const long long nitems = d.sitem_off[d.NG_total];
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += (long long)gridDim.x * blockDim.x)
-        atomicAdd(&h[item_cost_bucket(d, i)], 1);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += (long long)gridDim.x * blockDim.x) {
+        const int b = item_cost_bucket(d, i);
+        d.item_cost[i] = (unsigned char)b;  // for k_item_order
+        atomicAdd(&h[b], 1);
+    }
     __syncthreads();
     if (threadIdx.x < ITEM_BUCKETS && h[threadIdx.x]) atomicAdd(&d.item_bucket[threadIdx.x], h[threadIdx.x]);
 }
@@ -262,7 +265,7 @@ __global__ void __launch_bounds__(256) k_item_order(DevPlan d) {
         const long long i = r0 + threadIdx.x;
         int b = -1, rank = 0;
         if (i < nitems) {
-            b = item_cost_bucket(d, i);
+            b = d.item_cost[i];
             rank = atomicAdd(&h[b], 1);
         }
         __syncthreads();
