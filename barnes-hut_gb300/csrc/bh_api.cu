@@ -32,7 +32,7 @@ struct bh_plan {
     size_t ws_bytes = 0;
     size_t o_sys, o_dyn, o_glob, o_poff, o_boff, o_coff, o_goff, o_toff, o_lvl;
     size_t o_X[2], o_Y[2], o_VX[2], o_VY[2], o_M[2], o_PID[2];
-    size_t o_AX, o_AY, o_P, o_key, o_slot, o_skey, o_bstart, o_sst, o_leafpart, o_perm, o_bigseg, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
+    size_t o_AX, o_AY, o_key, o_slot, o_skey, o_bstart, o_sst, o_leafpart, o_perm, o_bigseg, o_icnt, o_ioff, o_igrp, o_mom, o_rec, o_PD,
         o_rec2, o_org, o_lfar, o_lnear, o_lcnt, o_iord, o_icost, o_ibkt, o_sicnt, o_sioff, o_sigrp, o_sisub, o_sichk, o_qcnt;
     bool stream = false;  // theta-mode interaction lists built once per group and streamed
     int chunk = TARGET_CHUNK;
@@ -266,7 +266,6 @@ extern "C" int bh_plan_create(bh_plan **out, int nsys, const long long *n, const
     }
     p->o_AX = take(8 * N);
     p->o_AY = take(8 * N);
-    p->o_P = take(16 * N);
     p->o_PD = take(32 * N);
     p->o_key = take(4 * N);
     p->o_slot = take(4 * N);
@@ -357,7 +356,6 @@ static void fill_dev(bh_plan *p) {
     }
     d.AX = (double *)(w + p->o_AX);
     d.AY = (double *)(w + p->o_AY);
-    d.P = (float4 *)(w + p->o_P);
     d.PD = (float4 *)(w + p->o_PD);
     d.key = (int *)(w + p->o_key);
     d.slot = (int *)(w + p->o_slot);

@@ -148,11 +148,11 @@ k_force(DevPlan d, int tick, int accumulate) {
             while (c + 1 < ncol && s_colpre[c + 1] <= u) c++;
             ti[r] = s_col0[c] + (u - s_colpre[c]);
             if (sizeof(R) == 4) {
-                float4 p = d.P[ti[r]];
+                const float4 p = d.PD[2 * (long long)ti[r]];  // (x, x, y, y) box-relative
                 int lb = d.skey[ti[r]] - (int)sd.boff;
                 int kx = lb / G, ky = lb - kx * G;
                 tx[r] = (R)__fadd_rn(__fmul_rn((float)(kx - gx0), step_f), p.x);
-                ty[r] = (R)__fadd_rn(__fmul_rn((float)(ky - gy0), step_f), p.y);
+                ty[r] = (R)__fadd_rn(__fmul_rn((float)(ky - gy0), step_f), p.z);
             } else {
                 tx[r] = (R)(Xs[ti[r]] - gox);
                 ty[r] = (R)(Ys[ti[r]] - goy);
@@ -357,10 +357,10 @@ k_force(DevPlan d, int tick, int accumulate) {
                     }
                     int idx = nbox[lo] + (J - npre[lo]);
                     if (sizeof(R) == 4) {
-                        float4 p = d.P[idx];
+                        const float4 pxy = d.PD[2 * (long long)idx], pm = d.PD[2 * (long long)idx + 1];
                         float2 sh = nshift[lo];
                         reinterpret_cast<float4 *>(src)[j] =
-                            make_float4(__fadd_rn(sh.x, p.x), __fadd_rn(sh.y, p.y), p.z, p.w);
+                            make_float4(__fadd_rn(sh.x, pxy.x), __fadd_rn(sh.y, pxy.z), pm.x, pm.z);
                     } else {
                         typename Src<double>::T q;
                         q.x = Xs[idx] - gox;

@@ -211,9 +211,9 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
         for (int r = 0; r < NR; r++) {
             int run;
             const int ti = target_index(r, run);
-            const float4 p = d.P[ti];
+            const float4 p = d.PD[2 * (long long)ti];  // (x, x, y, y) box-relative
             tx[r] = __fadd_rn(__fmul_rn((float)(run >> tgs), step_f), p.x);
-            ty[r] = __fadd_rn(__fmul_rn((float)(run & (TG - 1)), step_f), p.y);
+            ty[r] = __fadd_rn(__fmul_rn((float)(run & (TG - 1)), step_f), p.z);
         }
         // negated target coordinates, near accumulators, far sums and compensations, in pairs
         f2_t ntx2[NR / 2], nty2[NR / 2], nax2[NR / 2], nay2[NR / 2];

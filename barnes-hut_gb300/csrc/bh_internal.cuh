@@ -10,11 +10,11 @@
 //     buffer (epoch + 1) & 1, which summarize / force / tick then use.  The
 //     buffer choice is read on the device, so a captured CUDA graph of one
 //     step replays correctly any number of times.
-//   * P: packed float4 per box-sorted particle (x - box origin, y - box origin,
-//     mass, sorted index as int bits) -- targets and the walking kernel's near
-//     sources; PD: the same offsets duplicated for packed f32x2 arithmetic,
-//     32 bytes per particle -- the list-streaming kernel's near sources, copied
-//     into shared memory by bulk asynchronous copies.
+//   * PD: per box-sorted particle (x, x, y, y), (m, m, index, kx << 16 | ky)
+//     with x, y the offsets from the box origin (formed in FP64, rounded once),
+//     duplicated for packed f32x2 arithmetic, 32 bytes -- the list-streaming
+//     kernel's near sources (copied into shared memory by bulk asynchronous
+//     copies), every kernel's targets and the walking kernel's near sources.
 //   * AX, AY: FP64 accelerations, box-sorted order (aligned with the state).
 //   * key / slot: 4 * box key + quadrant, and rank in the quadrant, per particle
 //     (placement output); skey: box key per box-sorted particle.
@@ -41,7 +41,8 @@ constexpr int FORCE_R = 4;                                   // targets per thre
 constexpr int TARGET_CHUNK = FORCE_THREADS * FORCE_R;        // targets per work item
 constexpr int FRONTIER_CAP = 512;                            // traversal frontier per level
 constexpr int SCAN_TILE = 4096;   // counts per tile of the single-pass scans (256 threads x 16)
-constexpr int SITEM_TILE = 64;    // target groups per tile of the streaming work-item kernel
+constexpr int MAX_TG = 8;          // largest target group (boxes per side)
+constexpr int SITEM_TILE = 8;     // target groups per tile of the streaming work-item kernel (a warp each)
 constexpr int SUM_TILE = 16;      // leaf boxes per side of a summarize tile (pyramid levels 0..4)
 constexpr int STREAM_CHUNK = 128;  // targets per work item of the list-streaming force kernel
 constexpr int LIST_MAX_G = 16384;  // largest G of the list-streaming path (32-bit group indices)
@@ -106,7 +107,6 @@ struct DevPlan {
     double *X[2], *Y[2], *VX[2], *VY[2], *M[2];
     int *PID[2];
     double *AX, *AY;  // accelerations, box-sorted order
-    float4 *P;
     float4 *PD;  // per box-sorted particle: (x, x, y, y), (m, m, index, kx << 16 | ky) -- the
                  // packed near-field record (offsets from the box origin; box coordinates),
                  // staged into shared memory by bulk copies

@@ -295,11 +295,11 @@ __global__ void __launch_bounds__(LT) k_learned_correct(DevPlan d, float th2_lo,
         if (of && tid == 0) raise_err(d.glob, 2u /*BH_DEV_LIST_OVERFLOW*/);
         for (int v = tid; v < ig.T; v += LT) {
             int ti = item_target(ig, s_col0, s_colpre, v);
-            float4 p = d.P[ti];
+            const float4 p = d.PD[2 * (long long)ti];  // (x, x, y, y) box-relative
             int lb = d.skey[ti] - (int)d.sys[ig.s].boff;
             int kx = lb / ig.G, ky = lb - kx * ig.G;
             tpos[v] = make_float2(__fadd_rn(__fmul_rn((float)(kx - ig.gx0), step_f), p.x),
-                                  __fadd_rn(__fmul_rn((float)(ky - ig.gy0), step_f), p.y));
+                                  __fadd_rn(__fmul_rn((float)(ky - ig.gy0), step_f), p.z));
             corr[v] = make_float2(0.f, 0.f);
         }
         __syncthreads();

@@ -10,7 +10,6 @@ constexpr int FAR_CAP = 256;   // far entries per flush
 constexpr int NEAR_CAP = 256;  // near boxes per flush
 constexpr int SRC_CAP = 384;   // near sources per staging pass
 constexpr int FR_CAP = FRONTIER_CAP;
-constexpr int MAX_TG = 8;
 
 __device__ __forceinline__ float rcp_approx(float x) {
     float r;

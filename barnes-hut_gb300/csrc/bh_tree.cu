@@ -498,69 +498,19 @@ __global__ void __launch_bounds__(TPB) k_fill_items(DevPlan d) {
 // own (sub = cx * TG + cy), which use per-box refined near lists, and a box holding at least
 // quad_min particles gets items per quadrant instead (sub = TG^2 + 4 (cx * TG + cy) + quadrant),
 // which use per-quadrant refined near lists.  A set of nt targets splits into sitem_count(nt)
-// items: full chunks of STREAM_CHUNK and the remainder's pieces (sitem_range).  One kernel: each
-// thread counts its group's items, the CTA scans its SITEM_TILE groups, a look-back over the
-// preceding tiles gives their offset, and each thread writes its group's items.
-__device__ int group_items(const DevPlan &d, long long g, bool fill, int o) {
-    const int s = find_seg(d.goff_tab, d.nsys, g);
-    const SysDesc &sd = d.sys[s];
-    const long long lg = g - sd.goff;
-    const int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
-    const int gx0 = gi * sd.TG, gy0 = gj * sd.TG;
-    const int gx1 = min(sd.G, gx0 + sd.TG), gy1 = min(sd.G, gy0 + sd.TG);
-    int sparse = 0, cnt = 0;
-    for (int c = gx0; c < gx1; c++)
-        for (int r = gy0; r < gy1; r++) {
-            const long long b = sd.boff + (long long)c * sd.G + r;
-            const int nb = d.box_start[b + 1] - d.box_start[b];
-            const int kind = box_item_kind(nb, d.dense_min, d.quad_min);
-            if (kind == 2) {
-                for (int q = 0; q < 4; q++) cnt += sitem_count(d.qcounts[4 * b + q]);
-            } else if (kind == 1) {
-                cnt += sitem_count(nb);
-            } else {
-                sparse += nb;
-            }
-        }
-    const int ns = sitem_count(sparse);
-    if (!fill) return cnt + ns;
-    for (int k = 0; k < ns; k++, o++) {
-        d.sitem_group[o] = (int)g;
-        d.sitem_sub[o] = -1;
-        d.sitem_chunk[o] = make_int2(k, ns);
-    }
-    const int nbox = sd.TG * sd.TG;
-    for (int c = gx0; c < gx1; c++)
-        for (int r = gy0; r < gy1; r++) {
-            const long long b = sd.boff + (long long)c * sd.G + r;
-            const int nb = d.box_start[b + 1] - d.box_start[b];
-            const int kind = box_item_kind(nb, d.dense_min, d.quad_min);
-            const int bi = (c - gx0) * sd.TG + (r - gy0);
-            if (kind == 1) {
-                const int nk = sitem_count(nb);
-                for (int k = 0; k < nk; k++, o++) {
-                    d.sitem_group[o] = (int)g;
-                    d.sitem_sub[o] = bi;
-                    d.sitem_chunk[o] = make_int2(k, nk);
-                }
-            } else if (kind == 2) {
-                for (int q = 0; q < 4; q++) {
-                    const int nk = sitem_count(d.qcounts[4 * b + q]);
-                    for (int k = 0; k < nk; k++, o++) {
-                        d.sitem_group[o] = (int)g;
-                        d.sitem_sub[o] = nbox + 4 * bi + q;
-                        d.sitem_chunk[o] = make_int2(k, nk);
-                    }
-                }
-            }
-        }
-    return cnt + ns;
-}
+// items: full chunks of STREAM_CHUNK and the remainder's pieces (sitem_range).  A group's items
+// are the sparse ones, then the boxes' in (cx, cy) order, quadrant by quadrant.  One kernel: a
+// warp per group (a lane per box) counts the group's items, the CTA scans its SITEM_TILE groups,
+// a look-back over the preceding tiles gives their offset, and the lanes write their boxes'
+// items.
+constexpr int SITEM_WARPS = SITEM_TILE;  // one group per warp
+static_assert(MAX_TG * MAX_TG <= 64, "a lane holds at most two boxes of a group");
 
-__global__ void __launch_bounds__(SITEM_TILE) k_sitems(DevPlan d) {
-    __shared__ int sh[32];
+__global__ void __launch_bounds__(SITEM_WARPS * 32) k_sitems(DevPlan d) {
+    __shared__ int wtot[SITEM_WARPS], wpre[SITEM_WARPS];
     __shared__ int s_tile, s_excl;
     __shared__ unsigned s_gen;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long ntiles = (d.NG_total + SITEM_TILE - 1) / SITEM_TILE;
     if (threadIdx.x == 0) {
         s_tile = (int)atomicAdd(&d.glob->scan_ticket[2], 1u);
@@ -568,24 +518,104 @@ __global__ void __launch_bounds__(SITEM_TILE) k_sitems(DevPlan d) {
     }
     __syncthreads();
     const int tile = s_tile;
-    const long long g = (long long)tile * SITEM_TILE + threadIdx.x;
-    const int cnt = g < d.NG_total ? group_items(d, g, false, 0) : 0;
-    int tot;
-    const int pre = block_excl_scan(cnt, sh, &tot);
+    const long long g = (long long)tile * SITEM_TILE + warp;
+    // the lane's boxes bi = lane, lane + 32 of the group (bi = cx * TG + cy)
+    int nb[2] = {0, 0}, kind[2] = {0, 0}, cnt[2] = {0, 0};
+    int4 qc[2] = {make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0)};
+    int sparse = 0, nbox = 0;
+    if (g < d.NG_total) {
+        const int s = find_seg(d.goff_tab, d.nsys, g);
+        const SysDesc &sd = d.sys[s];
+        const long long lg = g - sd.goff;
+        const int gi = (int)(lg / sd.NGs), gj = (int)(lg - (long long)gi * sd.NGs);
+        const int TG = sd.TG, tgs = __ffs(TG) - 1;
+        nbox = TG * TG;
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int bi = lane + 32 * u;
+            const int cx = bi >> tgs, cy = bi & (TG - 1);
+            if (bi < nbox && gi * TG + cx < sd.G && gj * TG + cy < sd.G) {
+                const long long b = sd.boff + (long long)(gi * TG + cx) * sd.G + gj * TG + cy;
+                nb[u] = d.box_start[b + 1] - d.box_start[b];
+                kind[u] = box_item_kind(nb[u], d.dense_min, d.quad_min);
+                if (kind[u] == 2) {
+                    qc[u] = reinterpret_cast<const int4 *>(d.qcounts)[b];
+                    cnt[u] = sitem_count(qc[u].x) + sitem_count(qc[u].y) + sitem_count(qc[u].z) + sitem_count(qc[u].w);
+                } else if (kind[u] == 1) {
+                    cnt[u] = sitem_count(nb[u]);
+                } else {
+                    sparse += nb[u];
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) sparse += __shfl_xor_sync(0xffffffffu, sparse, o);
+    const int ns = sitem_count(sparse);
+    // exclusive prefix of the boxes' item counts in bi order (lane's first box, then second)
+    int inc0 = cnt[0], inc1 = cnt[1];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y0 = __shfl_up_sync(0xffffffffu, inc0, o), y1 = __shfl_up_sync(0xffffffffu, inc1, o);
+        if (lane >= o) {
+            inc0 += y0;
+            inc1 += y1;
+        }
+    }
+    const int tot0 = __shfl_sync(0xffffffffu, inc0, 31), tot1 = __shfl_sync(0xffffffffu, inc1, 31);
+    const int gtot = g < d.NG_total ? ns + tot0 + tot1 : 0;
+    if (lane == 0) wtot[warp] = gtot;
+    __syncthreads();
     if (threadIdx.x < 32) {
+        int v = lane < SITEM_WARPS ? wtot[lane] : 0, x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane < SITEM_WARPS) wpre[lane] = x - v;
+        const int tot = __shfl_sync(0xffffffffu, x, 31);
         const int e = lookback(d.sst_sitem, tile, s_gen, tot, d.glob);
-        if (threadIdx.x == 0) s_excl = e;
+        if (threadIdx.x == 0) {
+            s_excl = e;
+            if (tile == ntiles - 1) {
+                d.sitem_off[d.NG_total] = e + tot;
+                d.glob->scan_ticket[2] = 0u;
+                d.glob->scan_gen[2] = next_gen(s_gen);
+            }
+        }
     }
     __syncthreads();
-    const int off = s_excl + pre;
-    if (g < d.NG_total) {
-        d.sitem_off[g] = off;
-        group_items(d, g, true, off);
+    if (g >= d.NG_total) return;
+    const int off = s_excl + wpre[warp];
+    if (lane == 0) d.sitem_off[g] = off;
+    for (int k = lane; k < ns; k += 32) {  // the sparse boxes' items
+        d.sitem_group[off + k] = (int)g;
+        d.sitem_sub[off + k] = -1;
+        d.sitem_chunk[off + k] = make_int2(k, ns);
     }
-    if (tile == ntiles - 1 && threadIdx.x == 0) {
-        d.sitem_off[d.NG_total] = s_excl + tot;
-        d.glob->scan_ticket[2] = 0u;
-        d.glob->scan_gen[2] = next_gen(s_gen);
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        const int bi = lane + 32 * u;
+        int o = off + ns + (u ? tot0 : 0) + (u ? inc1 : inc0) - cnt[u];
+        if (kind[u] == 1) {
+            const int nk = cnt[u];
+            for (int k = 0; k < nk; k++, o++) {
+                d.sitem_group[o] = (int)g;
+                d.sitem_sub[o] = bi;
+                d.sitem_chunk[o] = make_int2(k, nk);
+            }
+        } else if (kind[u] == 2) {
+            const int qv[4] = {qc[u].x, qc[u].y, qc[u].z, qc[u].w};
+            for (int q = 0; q < 4; q++) {
+                const int nk = sitem_count(qv[q]);
+                for (int k = 0; k < nk; k++, o++) {
+                    d.sitem_group[o] = (int)g;
+                    d.sitem_sub[o] = nbox + 4 * bi + q;
+                    d.sitem_chunk[o] = make_int2(k, nk);
+                }
+            }
+        }
     }
 }
 
@@ -599,8 +629,8 @@ __global__ void __launch_bounds__(SITEM_TILE) k_sitems(DevPlan d) {
 //              a warp each, a bitonic network in its slice of shared memory; longer ones a CTA
 //              each, four stable 8-bit radix passes through the dead slot array);
 //   k_gather   output particle t takes input perm[t]: the FP64 state of the next buffer, the
-//              packed float4 record (offsets from the box origin computed in FP64, rounded once
-//              to float), the 32-byte near-source record and the sorted key.
+//              32-byte packed record (offsets from the box origin computed in FP64, rounded
+//              once to float) and the sorted key; and it sums the leaves (below).
 constexpr int SEG_REG = 16;
 constexpr int SEG_WARP = 1024;
 constexpr int SEG_CHECK = 128;  // stretches up to this long are checked for order by their thread
@@ -886,7 +916,6 @@ __global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
             const float ox = f64_to_f32_rn(__dsub_rn(x[u], org[kx]));
             const float oy = f64_to_f32_rn(__dsub_rn(y[u], org[sd.G + ky]));
             const float mf = f64_to_f32_rn(m[u]);
-            d.P[t] = make_float4(ox, oy, mf, __int_as_float((int)t));
             d.PD[2 * t] = make_float4(ox, ox, oy, oy);
             d.PD[2 * t + 1] = make_float4(mf, mf, __int_as_float((int)t), __int_as_float((kx << 16) | ky));
             d.skey[t] = key;
@@ -986,8 +1015,8 @@ __global__ void __launch_bounds__(TPB) k_leaf(DevPlan d) {
         float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (i < d.n_total) {
             key = d.skey[i];
-            const float4 p = d.P[i];
-            leaf_terms<SECOND>(p.x, p.y, p.z, v);
+            const float4 pxy = d.PD[2 * i], pm = d.PD[2 * i + 1];  // (x, x, y, y), (m, m, ., .)
+            leaf_terms<SECOND>(pxy.x, pxy.z, pm.x, v);
         }
         leaf_chunk<SECOND>(d, c, key, v);
     }
@@ -1184,7 +1213,7 @@ cudaError_t launch_items(const DevPlan &d, cudaStream_t st) {
         if (e != cudaSuccess) return e;
     }
     if (d.stream && d.NG_total > 0) {
-        k_sitems<<<(unsigned)((d.NG_total + SITEM_TILE - 1) / SITEM_TILE), SITEM_TILE, 0, st>>>(d);
+        k_sitems<<<(unsigned)((d.NG_total + SITEM_TILE - 1) / SITEM_TILE), SITEM_WARPS * 32, 0, st>>>(d);
     }
     return cudaGetLastError();
 }
