@@ -4,8 +4,8 @@ Tunables (per plan): group_dim -- target group edge in leaf boxes (1, 2, 4 or 8;
 TG^2 boxes share one interaction list) --, dense_min -- boxes holding at least
 this many particles get their own work items and per-box refined near lists
 (list-streaming path) --, quad_min -- boxes holding at least this many particles
-are refined quadrant by quadrant (-1: never) -- and tune -- the force-kernel variant (0: 8 CTAs per SM
-with 64 registers per thread, 1: 6 CTAs per SM with 80).  Every candidate keeps
+are refined quadrant by quadrant (-1: never) -- and tune -- the list-streaming kernel's build
+(0: 6 CTAs per SM with 80 registers per thread, 1: 8 CTAs per SM with 64).  Every candidate keeps
 the opening-angle rule for every target (a cell accepted for a group rectangle
 passes the test for each of its boxes); they differ in how far the lists are
 refined, so the chosen one's accuracy is measured and reported by the caller.

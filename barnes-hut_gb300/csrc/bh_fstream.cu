@@ -576,10 +576,10 @@ cudaError_t launch_fstream(const DevPlan &d, bool tick, bool accumulate, cudaStr
                            const cudaEvent_t *ev) {
     if (d.n_total == 0) return cudaSuccess;
     if (d.prec == 1)
-        return d.tune == 1 ? launch_fstream_t<true, 6>(d, tick, accumulate, st, ev)
-                           : launch_fstream_t<true, 8>(d, tick, accumulate, st, ev);
-    return d.tune == 1 ? launch_fstream_t<false, 6>(d, tick, accumulate, st, ev)
-                       : launch_fstream_t<false, 8>(d, tick, accumulate, st, ev);
+        return d.tune == 1 ? launch_fstream_t<true, 8>(d, tick, accumulate, st, ev)
+                           : launch_fstream_t<true, 6>(d, tick, accumulate, st, ev);
+    return d.tune == 1 ? launch_fstream_t<false, 8>(d, tick, accumulate, st, ev)
+                       : launch_fstream_t<false, 6>(d, tick, accumulate, st, ev);
 }
 
 }  // namespace bh

@@ -78,8 +78,10 @@ typedef struct bh_params {
                              0 = automatic); forced to 1 in flat mode */
     int precision;        /* BH_PREC_* */
     int flags;            /* BH_FLAG_* */
-    int tune;             /* force-kernel variant (0: 8 CTAs per SM, 1: 6 CTAs per
-                             SM with more registers), picked by the autotuner */
+    int tune;             /* force-kernel build, picked by the autotuner: 0 the path's
+                             default (list streaming: 6 CTAs per SM, 80 registers; walk:
+                             8 CTAs per SM), 1 the other (list streaming: 8 CTAs per SM,
+                             64 registers; walk: 6 CTAs per SM) */
     double correction_theta; /* with BH_FLAG_LEARNED: cells accepted at theta but
                                 not at correction_theta get the learned correction */
     int dense_min;        /* list streaming: boxes with at least this many particles get
