@@ -288,11 +288,22 @@ def batched_benchmark(torch, dev, nsys=512, steps=50, warmup=3):
     e1.record(stream)
     torch.cuda.synchronize()
     t = e0.elapsed_time(e1) / 1e3
+    # one more step's force kernel alone (CUDA events around it) with its pair counts: the
+    # batched line's FP32 roofline (12 flop per near pair, 20 per far pair)
+    plan.set_kernel_timing(True)
+    plan.create_tree()
+    plan.summarize()
+    plan.evaluate()
+    kms = plan.force_kernel_ms()
+    nn, nf = plan.pair_counts()
     flags = plan.error_flags(raise_on_error=False)
     out = {"metric": "particle-steps/s, 512 batched systems", "value": sum(n) * steps / t,
            "systems": nsys, "particles": int(sum(n)), "steps": steps, "ms_per_step": 1e3 * t / steps,
            "theta": 0.5, "dt": 1e-6, "tile": tile, "graph": f"{steps} steps in one CUDA graph",
-           "kernels_per_step": plan.kernels_per_step(), "device_error_flags": flags}
+           "kernels_per_step": plan.kernels_per_step(),
+           "force_kernel": {"ms": kms, "pairs_near": nn, "pairs_far": nf,
+                            "tflops": (12.0 * nn + 20.0 * nf) / kms / 1e9},
+           "device_error_flags": flags}
     plan.close()
     return out
 
@@ -783,6 +794,8 @@ def main():
     side = {}
     if not args.quick and rank == 0:
         side["batched"] = batched_benchmark(torch, dev)
+        fk = side["batched"]["force_kernel"]
+        fk["frac_of_sgemm"] = fk["tflops"] / peak if peak else None
         side["free_run_1m"] = free_run(torch, dev)
         side["precision"] = precision_study(torch, dev, batch)
         side["learned"] = learned_benchmark(torch, dev, batch)
