@@ -5,7 +5,10 @@
 * ``gb300``     this project's CUDA step (default semantics: the reference
                 CPU path's, i.e. r^2 <= 1e-5 pairs contribute nothing);
 * ``singlegpu`` the same CUDA step with the reference GPU path's semantics
-                (no cutoff; only coincident points are skipped).
+                (no cutoff; only coincident points are skipped);
+* ``gb300_ctypes`` the C ABI bound directly with ctypes
+                (``implementations/gb300_ctypes.py``: the module a python-bh
+                maintainer would add to the reference's own package).
 
 The reference's ``sequential``, ``multigpu``, ``parla`` and ``pykokkos``
 implementations are not provided: this package has one GPU code path and no
@@ -23,6 +26,9 @@ class BarnesHut:
         if impl in ("gb300", "singlegpu"):
             from .implementations.gb300 import GB300BarnesHut
             self.bh = GB300BarnesHut(reference_gpu_semantics=(impl == "singlegpu"))
+        elif impl == "gb300_ctypes":
+            from .implementations.gb300_ctypes import CtypesGB300BarnesHut
+            self.bh = CtypesGB300BarnesHut()
         else:
             raise ValueError(
                 f"implementation {impl!r} is not provided by this package; "

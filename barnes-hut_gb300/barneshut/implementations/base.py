@@ -15,6 +15,7 @@ import barneshut.internals.particle as p
 from barneshut.gb300 import particle_io
 from barneshut.internals import Config
 from barneshut.kernels.helpers import next_perfect_square
+from barneshut.kernels.helpers.grid import get_bounding_box
 from timer import Timer
 
 LEAF_OCCUPANCY = 0.7
@@ -51,6 +52,15 @@ class BaseBarnesHut:
     def set_particles(self, x, y, m, vx, vy):
         self.particles = particle_io.records_from_arrays(x, y, m, vx, vy)
         self.n_particles = len(x)
+
+    def set_particles_bounding_box(self):
+        """base.py:211-240: the square box around the particles, the grid dimension from the
+        particles per leaf, the box edge."""
+        bb_min, bb_max = get_bounding_box(self.particles[:, p.px:p.py + 1])
+        self.grid_dim = reference_grid_dim(len(self.particles), self.particles_per_leaf)
+        self.step = (bb_max[0] - bb_min[0]) / self.grid_dim
+        self.min_xy = np.array(bb_min)
+        self.max_xy = np.array(bb_max)
 
     def write_particles_to_file(self, filename):
         """Checkpoint in the input format (resume = read_particles_from_file)."""

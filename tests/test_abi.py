@@ -152,3 +152,17 @@ def test_workspace_budget(lib):
     assert 3.0e11 < big <= 3.7e11
     walk = _workspace(lib, 1 << 24, 16384, group_dim=8, flags=native.BH_FLAG_WALK)
     assert walk <= 3.9e10
+
+
+def test_ctypes_binding_params_layout():
+    """The standalone ctypes binding (implementations/gb300_ctypes.py) declares bh_params
+    field for field like the package's own binding: same size, same offsets."""
+    pytest.importorskip("torch")
+    from barneshut.gb300 import native
+    from barneshut.implementations import gb300_ctypes
+
+    a, b = gb300_ctypes.BhParams, native.make_params().__class__
+    assert ctypes.sizeof(a) == ctypes.sizeof(b)
+    assert [f[0] for f in a._fields_] == [f[0] for f in b._fields_]
+    for name, _ in a._fields_:
+        assert getattr(a, name).offset == getattr(b, name).offset, name
