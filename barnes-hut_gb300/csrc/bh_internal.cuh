@@ -82,7 +82,6 @@ struct Globals {
     unsigned long long near_pairs, far_pairs;
     unsigned int item_next;   // force work queue head (zeroed before each force launch)
     unsigned int item_next2;  // learned-correction work queue head
-    unsigned int group_next;  // list-build queue head (zeroed before each list build)
     unsigned long long corr_pairs;  // (target, cell) pairs the learned correction evaluated
     unsigned int scan_ticket[3];    // next tile of each single-pass scan (its last tile resets it)
     unsigned int scan_gen[3];       // generation of each scan's tile states (its last tile bumps it)

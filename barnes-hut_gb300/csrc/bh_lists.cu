@@ -34,13 +34,7 @@ __global__ void __launch_bounds__(LW * 32, LISTS_MINB) k_lists(DevPlan d) {
     int(*fb)[FR_CAP] = front[warp];
     const float theta2 = d.theta2_f;
     const unsigned lt_mask = (1u << lane) - 1u;
-    // groups from a queue (their walks differ in length: a group inside a cluster opens more
-    // cells), so the launch does not end with a few warps walking their last groups
-    for (;;) {
-        long long g = 0;
-        if (lane == 0) g = atomicAdd(&d.glob->group_next, 1u);
-        g = __shfl_sync(0xffffffffu, g, 0);
-        if (g >= d.NG_total) break;
+    for (long long g = (long long)blockIdx.x * LW + warp; g < d.NG_total; g += (long long)gridDim.x * LW) {
         const int s = find_seg(d.goff_tab, d.nsys, g);
         const SysDesc &sd = d.sys[s];
         const SysDyn &dy = d.dyn[s];
@@ -289,10 +283,8 @@ cudaError_t launch_lists(const DevPlan &d, cudaStream_t st) {
     if (d.NG_total == 0) return cudaSuccess;
     long long grid = (long long)d.nsm * LISTS_MINB;
     if (grid * LW > d.NG_total) grid = (d.NG_total + LW - 1) / LW;
-    cudaError_t e = cudaMemsetAsync(&d.glob->group_next, 0, sizeof(unsigned), st);
-    if (e != cudaSuccess) return e;
     k_lists<<<(unsigned)grid, LW * 32, 0, st>>>(d);
-    e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(d.item_bucket, 0, sizeof(int) * 2 * ITEM_BUCKETS, st);
     if (e != cudaSuccess) return e;

@@ -944,7 +944,7 @@ __global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
 // waiting for one CTA.  Every sum runs in a fixed order, so the moments do not depend on
 // scheduling.  Pyramid cells carry the second moments only for the learned correction (SECOND);
 // the leaves always carry all six.
-constexpr int SUM_THREADS = 256;
+constexpr int SUM_THREADS = 128;  // 7 CTAs per SM: the 1,024 tiles of G = 512 in one wave
 constexpr int SUM_CELLS = 256 + 64 + 16 + 4 + 1;  // a tile's cells at levels 0..4
 constexpr int SUM_UP = 5;                         // the first level above the tiles (2^5 boxes)
 static_assert(SUM_TILE == 1 << (SUM_UP - 1), "a tile is one cell of level SUM_UP - 1");
@@ -1032,7 +1032,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
 
 // leaves_given: the leaf moments are already in d.mom (bh_set_leaf_moments); build the rest.
 template <bool SECOND>
-__global__ void __launch_bounds__(SUM_THREADS, 4) k_summarize(DevPlan d, int leaves_given) {
+__global__ void __launch_bounds__(SUM_THREADS, 7) k_summarize(DevPlan d, int leaves_given) {
     constexpr int NM = SECOND ? 6 : 3;  // moments a pyramid cell carries
     __shared__ double cm[SUM_CELLS * 6];  // the tile's cells, level by level
     __shared__ double chm[4 * 64 * 6];    // shifted child moments: 64 cells x 4 children
