@@ -506,18 +506,23 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
             }
         }
         __syncwarp();
-        if (active && slice == 0) {
-#pragma unroll
-            for (int r = 0; r < NR; r++) {
-                if (tl * NR + r >= T) continue;
+        // every lane takes targets v = lane, lane + 32, ... (not only the first slice's lanes)
+        for (int v = lane; v < T; v += 32) {
+            {
+                const int vt = v / NR, r = v - vt * NR;  // the lane and register that held it
                 float sx = 0.f, sy = 0.f;
                 for (int k = 0; k < nslice; k++) {
-                    const float *o = red + 2 * ((k * nthr + tl) * NR + r);
+                    const float *o = red + 2 * ((k * nthr + vt) * NR + r);
                     sx += o[0];
                     sy += o[1];
                 }
-                int run;
-                const int t = target_index(r, run);
+                const int u = c0 + v;
+                int lo = 0, hi = nrun;  // the run with rpre[lo] <= u < rpre[lo + 1]
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (rpre[mid] <= u) lo = mid; else hi = mid;
+                }
+                const int t = rstart[lo] + (u - rpre[lo]);
                 double ax = d.gconst * (double)sx, ay = d.gconst * (double)sy;
                 if (accumulate) {
                     ax += d.AX[t];
