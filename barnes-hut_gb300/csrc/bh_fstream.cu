@@ -344,15 +344,30 @@ __global__ void __launch_bounds__(FW * 32, MINB) k_fstream(DevPlan d, int tick, 
                 const float s2 = __fmul_rn(step_f, step_f), theta2 = d.theta2_f;
                 const int own = (gx0 + bcx) * G + (gy0 + bcy);
                 int nkeep = 0, nacc = 0, base = 0;
-                for (int k0 = 0; k0 < nn; k0 += 32) {
+                // the batch's descriptors (WDESC = 2 rounds of 32) are loaded together
+                int4 pe0[WDESC / 32], pe1[WDESC / 32];
+                int pnx[WDESC / 32];
+#pragma unroll
+                for (int u = 0; u < WDESC / 32; u++) {
+                    const int k = 32 * u + lane;
+                    pe0[u] = make_int4(0, 0, 0, 0);
+                    pe1[u] = make_int4(-1, 0, 0, 0);
+                    pnx[u] = 0;
+                    if (k < nn) {
+                        pe0[u] = ln[2 * (b0 + k)];
+                        pe1[u] = ln[2 * (b0 + k) + 1];
+                        pnx[u] = ln[2 * (b0 + k + 1)].y;
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < WDESC / 32; u++) {
+                    const int k0 = 32 * u;
+                    if (k0 >= nn) break;
                     const int k = k0 + lane;
-                    int4 e0 = make_int4(0, 0, 0, 0), e1 = make_int4(-1, 0, 0, 0);
-                    int c = 0;
+                    const int4 e0 = pe0[u], e1 = pe1[u];
+                    const int c = k < nn ? pnx[u] - e0.y : 0;
                     bool acc = false;
                     if (k < nn) {
-                        e0 = ln[2 * (b0 + k)];
-                        e1 = ln[2 * (b0 + k) + 1];
-                        c = ln[2 * (b0 + k + 1)].y - e0.y;
                         if (e1.x != own) {
                             const float rxb = __fsub_rn(__int_as_float(e1.z), oxb);
                             const float ryb = __fsub_rn(__int_as_float(e1.w), oyb);
