@@ -42,7 +42,7 @@ DT = 1e-5
 SEED = 2
 METRIC = "particle-steps/s at N=4M on 1 GB300 (plain theta=0.5 step)"
 WORKLOAD = "cluster-mixture N=4,194,304, 512x512 boxes, theta=0.5, eps=1e-4, dt=1e-5, FP32+Kahan"
-K_FSTREAM_TRAFFIC = 1118.2e6  # bytes per force launch, dram read + write of one ncu capture
+K_FSTREAM_TRAFFIC = 1120.7e6  # bytes per force launch, dram read + write of one ncu capture
 
 
 def parse():
