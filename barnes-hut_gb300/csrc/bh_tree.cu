@@ -215,7 +215,8 @@ __global__ void __launch_bounds__(TPB) k_bbox(DevPlan d) {
 // four); a particle's slot is its rank within its quadrant.
 constexpr int PLACE_PP = 4;  // consecutive particles per thread
 
-__global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
+// (64 registers: 4 CTAs per SM)
+__global__ void __launch_bounds__(TPB, 4) k_place(DevPlan d) {
     constexpr int PT = TPB * PLACE_PP;  // particles per block round
     __shared__ int skeys[PT + 1], runold[PT], wmax[TPB / 32];
     const int cur = d.glob->epoch & 1;
@@ -242,6 +243,28 @@ __global__ void __launch_bounds__(TPB) k_place(DevPlan d) {
             }
         }
         int key[PLACE_PP];
+        // the thread's particles usually lie in one system: its constants are loaded once
+        const int s_first = find_seg(d.poff_tab, d.nsys, i0 < d.n_total ? i0 : d.n_total - 1);
+        const bool one_sys = d.poff_tab[s_first + 1] >= i0 + PLACE_PP;
+        if (one_sys) {
+            const SysDesc &sd = d.sys[s_first];
+            const SysDyn &dy = d.dyn[s_first];
+            const double mnx = dy.minx, mny = dy.miny, st = dy.step, inv = dy.inv_step;
+            const float mnxf = dy.minx_f, mnyf = dy.miny_f, invf = dy.inv_step_f, tol = dy.key_tol;
+            const int G = sd.G;
+            const long long boff = sd.boff;
+#pragma unroll
+            for (int j = 0; j < PLACE_PP; j++) {
+                const unsigned hx = (unsigned)(__double_as_longlong(x[j]) >> 52) & 0x7FFu;
+                const unsigned hy = (unsigned)(__double_as_longlong(y[j]) >> 52) & 0x7FFu;
+                if (hx == 0x7FFu || hy == 0x7FFu) raise_err(d.glob, 1u /*BH_DEV_NAN_POSITION*/);
+                const int k2x = half_key1_f32(x[j], mnx, st, inv, mnxf, invf, tol, G);
+                const int k2y = half_key1_f32(y[j], mny, st, inv, mnyf, invf, tol, G);
+                const int box = (int)(boff + (long long)(k2x >> 1) * G + (k2y >> 1));
+                key[j] = 4 * box + (k2x & 1) * 2 + (k2y & 1);
+                skeys[e0 + j] = key[j];
+            }
+        } else
 #pragma unroll
         for (int j = 0; j < PLACE_PP; j++) {
             const long long i = i0 + j;
