@@ -888,9 +888,13 @@ __global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
     const int lane = threadIdx.x & 31;
     // SU particles per thread per round, each stage's loads issued for all of them before the
     // next stage uses them; the loop runs per warp (its first lane's index), for the scans.
-    // Two per round keep the kernel at 48 registers, 5 CTAs per SM (four: 93, 2 CTAs, 9% slower)
+    // Two per round keep the kernel at 58 registers, 4 CTAs per SM (four: 93, 2 CTAs, 9% slower)
     constexpr int SU = 2;
     const long long n = d.n_total, stride = (long long)gridDim.x * blockDim.x;
+    // one system (the common case): its grid constants once, no search per particle
+    const bool one = d.nsys == 1;
+    const int G0 = d.sys[0].G;
+    const long long boff0 = d.sys[0].boff, ooff0 = d.sys[0].ooff;
     for (long long w0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); w0 < n; w0 += SU * stride) {
         const long long t0 = w0 + lane;
         int src[SU], key4[SU];
@@ -926,19 +930,20 @@ __global__ void __launch_bounds__(TPB) k_gather(DevPlan d) {
             lx[u] = ly[u] = lm[u] = 0.f;
             if (t >= n) continue;
             const int key = key4[u] >> 2;
-            const int s = find_seg(d.boff_tab, d.nsys, key);
-            const SysDesc &sd = d.sys[s];
-            const int lb = (int)(key - sd.boff);
-            const int kx = lb / sd.G, ky = lb - kx * sd.G;
+            const int s = one ? 0 : find_seg(d.boff_tab, d.nsys, key);
+            const int G = one ? G0 : d.sys[s].G;
+            const long long boff = one ? boff0 : d.sys[s].boff, ooff = one ? ooff0 : d.sys[s].ooff;
+            const int lb = (int)(key - boff);
+            const int kx = lb / G, ky = lb - kx * G;
             d.X[nxt][t] = x[u];
             d.Y[nxt][t] = y[u];
             d.VX[nxt][t] = vx[u];
             d.VY[nxt][t] = vy[u];
             d.M[nxt][t] = m[u];
             d.PID[nxt][t] = pid[u];
-            const double *org = d.org + sd.ooff;  // box origins (tabulated by k_bbox's last block)
+            const double *org = d.org + ooff;  // box origins (tabulated by k_bbox's last block)
             const float ox = f64_to_f32_rn(__dsub_rn(x[u], org[kx]));
-            const float oy = f64_to_f32_rn(__dsub_rn(y[u], org[sd.G + ky]));
+            const float oy = f64_to_f32_rn(__dsub_rn(y[u], org[G + ky]));
             const float mf = f64_to_f32_rn(m[u]);
             d.PD[2 * t] = make_float4(ox, ox, oy, oy);
             d.PD[2 * t + 1] = make_float4(mf, mf, __int_as_float((int)t), __int_as_float((kx << 16) | ky));
