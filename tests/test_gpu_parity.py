@@ -202,6 +202,36 @@ def test_theta_vs_fp64_oracle(theta, TG, G, prec, walk):
     assert plan.error_flags() == 0
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("walk", [False, True], ids=["lists", "walk"])
+def test_alternative_builds_vs_fp64_oracle(prec, walk):
+    """The force kernels' other builds (tune = 1: list streaming on 8 CTAs per SM with 64
+    registers and 88-source passes; the walk on 6 CTAs per SM), which the autotuner times, give
+    the oracle's interaction lists and forces like the default builds."""
+    from barneshut.gb300 import workloads
+    from oracle import oracle
+
+    x, y, m, vx, vy = workloads.cluster_mixture(20000, seed=33)
+    eps, theta, TG, G = 1e-3, 0.5, 4, 19
+    plan = make_plan(20000, G, grav_constant=1.0, tick_seconds=1e-5, softening=eps, cutoff_r2=0.0,
+                     theta=theta, group_dim=TG, precision=prec, tune=1,
+                     flags=native().BH_FLAG_WALK if walk else 0)
+    plan.load(x, y, m, vx, vy)
+    plan.create_tree()
+    plan.summarize()
+    plan.evaluate()
+    out = plan.store()
+    nn, nf = plan.pair_counts()
+    dense = 0 if walk else native().BH_STREAM_DENSE_MIN
+    quad = 0 if walk else native().BH_STREAM_QUAD_MIN
+    ax, ay, on, of = oracle.theta_evaluate(x, y, m, G, TG=TG, theta=theta, eps2=eps * eps, cutoff=0.0,
+                                           dense_min=dense, quad_min=quad)
+    assert (nn, nf) == (on, of), "interaction lists differ from the oracle's"
+    err = oracle.rel_rms(out["ax"].cpu().numpy(), out["ay"].cpu().numpy(), ax, ay)
+    assert err <= 1e-5, err
+    assert plan.error_flags() == 0
+
+
 @pytest.mark.parametrize("TG,dense_min,quad_min", [(2, 16, 32), (4, 8, 24), (4, 16, -1)])
 def test_refined_lists_vs_fp64_oracle(TG, dense_min, quad_min):
     """List streaming with per-box and per-quadrant refinement thresholds low enough that many
