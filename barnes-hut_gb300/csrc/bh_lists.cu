@@ -5,7 +5,7 @@
 // sequential/evaluation.py:73-109); in theta mode this project replaces the flat far field with
 // a walk of the cell pyramid, and this kernel does that walk once per target group instead of
 // once per work item.  One warp per group (grid-stride over groups) walks the pyramid level by
-// level, each lane testing LU frontier cells per round with their records loaded together: a
+// level, each lane testing LU frontier cells per round (their records loaded together): a
 // cell whose centre of mass lies at distance d from the group's box rectangle is accepted when
 // s^2 < theta^2 d^2 (s = cell edge) and goes to the far list, a rejected leaf goes to the near
 // list, any other rejected cell opens into its children.  Ballots and a warp scan place the
@@ -25,8 +25,8 @@
 namespace bh {
 
 constexpr int LW = 4;  // warps per list-building CTA; one warp walks one group
-constexpr int LU = 4;  // frontier cells per lane per round (their records are loaded together)
-constexpr int LISTS_MINB = 8;  // CTAs per SM (registers: 64 per thread)
+constexpr int LU = 1;  // frontier cells per lane per round (a level's frontier averages ~47 cells)
+constexpr int LISTS_MINB = 12;  // CTAs per SM (40 registers): the walk is latency-bound
 
 __global__ void __launch_bounds__(LW * 32, LISTS_MINB) k_lists(DevPlan d) {
     __shared__ int front[LW][2][FR_CAP];
