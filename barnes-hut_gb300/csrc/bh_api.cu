@@ -58,6 +58,11 @@ struct bh_plan {
     int gkernels = -1;  // kernel nodes of the captured step graph
     int gsteps = 0;
     cudaStream_t gstream = nullptr;
+    // create_tree's side branch: the work items (they need only the box scan) run on `side`
+    // while the scatter runs on the caller's stream; fork and join through two events, which
+    // a stream capture turns into graph edges
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     // learned correction (caller-owned device buffers)
     const uint8_t *mlp_img = nullptr;
     const float *mlp_params = nullptr;
@@ -310,7 +315,8 @@ extern "C" int bh_plan_destroy(bh_plan *p) {
     if (!p) return BH_ERR_INVALID;
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     if (p->gstream) cudaStreamDestroy(p->gstream);
-    for (cudaEvent_t e : p->tev)
+    if (p->side) cudaStreamDestroy(p->side);
+    for (cudaEvent_t e : {p->fork_ev, p->join_ev, p->tev[0], p->tev[1]})
         if (e) cudaEventDestroy(e);
     delete p;
     return BH_OK;
@@ -419,6 +425,9 @@ extern "C" int bh_bind(bh_plan *p, void *workspace, size_t bytes, void *stream) 
     if (p->nsm < 1) p->nsm = 1;
     CK(p, force_init(), "force kernel attributes");
     CK(p, learned_init(), "learned kernel attributes");
+    if (!p->side) CK(p, cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking), "side stream");
+    if (!p->fork_ev) CK(p, cudaEventCreateWithFlags(&p->fork_ev, cudaEventDisableTiming), "fork event");
+    if (!p->join_ev) CK(p, cudaEventCreateWithFlags(&p->join_ev, cudaEventDisableTiming), "join event");
     p->ws = workspace;
     fill_dev(p);
     char *w = (char *)workspace;
@@ -502,9 +511,14 @@ static int enqueue_tree(bh_plan *p, cudaStream_t st) {
     CK(p, launch_bbox(p->dev, st), "bbox");
     CK(p, launch_place(p->dev, st), "place");
     CK(p, launch_scan(p->dev, st), "scan");
+    // the work items need the box scan only: they run beside the scatter
+    CK(p, cudaEventRecord(p->fork_ev, st), "fork");
+    CK(p, cudaStreamWaitEvent(p->side, p->fork_ev, 0), "fork wait");
+    CK(p, launch_items(p->dev, p->side), "work items");
+    CK(p, cudaEventRecord(p->join_ev, p->side), "join");
     CK(p, launch_scatter(p->dev, st), "scatter");  // (and the leaf sums)
     p->leaves_stale = false;
-    CK(p, launch_items(p->dev, st), "work items");
+    CK(p, cudaStreamWaitEvent(st, p->join_ev, 0), "join wait");
     return BH_OK;
 }
 
