@@ -350,11 +350,14 @@ def test_nan_position_raises_flag():
 
 
 # ---------------------------------------------------------------- batching / graphs
-def test_batched_equals_separate():
+@pytest.mark.parametrize("sizes", [(1500, 5000, 700), (1501, 4999, 703)], ids=["aligned", "ragged"])
+def test_batched_equals_separate(sizes):
+    """Systems stepped together equal each system stepped alone; the ragged sizes put system
+    boundaries inside a placement thread's four particles and inside 32-particle leaf chunks."""
     from barneshut.gb300 import workloads
 
-    systems = [workloads.uniform(1500, seed=60), workloads.cluster_mixture(5000, seed=61),
-               workloads.uniform(700, seed=62)]
+    systems = [workloads.uniform(sizes[0], seed=60), workloads.cluster_mixture(sizes[1], seed=61),
+               workloads.uniform(sizes[2], seed=62)]
     grids = [5, 9, 3]
     kw = dict(grav_constant=1.0, tick_seconds=1e-5, softening=1e-3, cutoff_r2=0.0, theta=0.5,
               group_dim=2)
